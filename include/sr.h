@@ -1,0 +1,236 @@
+/*
+ * sr.h — C ABI of softrender-gb300, the GB300 (sm_103a) rendering hot path of
+ * softrender (novacrazy/rust-softrender).
+ *
+ * The reference exposes a typestate builder chain (src/pipeline):
+ *
+ *   Pipeline::from_framebuffer(fb, uniforms)                 mod.rs:120-122
+ *     .render_mesh(Triangle, mesh, Some(stencil_ref))        mod.rs:146-155
+ *     -> VertexShader::run(vs) | run_to_fragment(vp, vs)     stages/vertex.rs:87,123
+ *     -> GeometryShader::clip_primitives() / run(gs)         stages/geometry.rs:261,132
+ *        .finish(viewport)                                   stages/geometry.rs:60
+ *     -> FragmentShader.with_blend(b).cull_faces(c)
+ *        .tile_size(t).run(fs)                               stages/fragment.rs:82-168
+ *
+ * Across this ABI the chain collapses into one sr_draw descriptor handed to
+ * sr_render().  Shader stages are device functions compiled into the library
+ * and selected by name (sr_shader_lookup).  All calls return an sr_status;
+ * nothing aborts or traps.  Rendering calls are stream-ordered: sr_render
+ * returns after enqueue and sr_sync() reports completion and any error the
+ * device recorded (the reference panics at those points instead).
+ *
+ * Plain C types only: pointers, sizes and the POD structs below.
+ */
+#ifndef SR_H
+#define SR_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define SR_API
+#else
+#define SR_API __attribute__((visibility("default")))
+#endif
+
+/* ------------------------------------------------------------ status codes */
+typedef enum sr_status {
+    SR_OK = 0,
+    SR_EINVAL = 1,     /* invalid argument (reference: assert!/panic)            */
+    SR_ENOMEM = 2,     /* device or host allocation failed                      */
+    SR_EBUDGET = 3,    /* request exceeds the HBM admission budget              */
+    SR_EOVERFLOW = 4,  /* a fixed-capacity device buffer overflowed             */
+    SR_ETIMEOUT = 5,   /* a bounded device or host wait gave up                 */
+    SR_ECUDA = 6,      /* a CUDA runtime call failed                            */
+    SR_ENAN = 7,       /* a primitive had an all-NaN bounding box; the reference
+                          panics in clamp_as_int (triangle.rs:66-78); here the
+                          primitive is skipped and the draw reports this code   */
+    SR_ENOTFOUND = 8,  /* unknown shader name                                   */
+    SR_EBUSY = 9       /* resource in use                                       */
+} sr_status;
+
+/* ---------------------------------------------------------------- enums */
+typedef enum sr_color_format {
+    SR_COLOR_NONE = 0,
+    SR_COLOR_RGBA32F = 1,   /* Vector4<f32>, 16 B per pixel */
+    SR_COLOR_RGBA8 = 2      /* Vector4<u8>, 4 B per pixel, r in the low byte */
+} sr_color_format;
+
+typedef enum sr_prim { SR_PRIM_POINT = 1, SR_PRIM_LINE = 2, SR_PRIM_TRIANGLE = 3 } sr_prim;
+
+typedef enum sr_gs_mode {
+    SR_GS_NONE = 0,    /* VertexShader::run_to_fragment (vertex.rs:123-160)      */
+    SR_GS_CLIP = 1,    /* .run(vs).clip_primitives().finish(vp) (geometry.rs:261) */
+    SR_GS_NAMED = 2    /* .run(vs).run(named geometry shader).finish(vp)        */
+} sr_gs_mode;
+
+/* Option<FaceWinding> (src/geometry/winding.rs:11-44) */
+typedef enum sr_cull { SR_CULL_NONE = 0, SR_CULL_CLOCKWISE = 1, SR_CULL_COUNTER_CLOCKWISE = 2 } sr_cull;
+
+/* StencilTest (src/stencil.rs:94-129); `mask` is the mesh's stencil reference,
+ * `value` the framebuffer's stencil. */
+typedef enum sr_stencil_test {
+    SR_STENCIL_ALWAYS = 0,
+    SR_STENCIL_NEVER = 1,
+    SR_STENCIL_LESS_THAN = 2,         /* mask <  value */
+    SR_STENCIL_GREATER_THAN = 3,      /* mask >  value */
+    SR_STENCIL_LESS_THAN_EQ = 4,      /* mask <= value */
+    SR_STENCIL_GREATER_THAN_EQ = 5,   /* mask >= value */
+    SR_STENCIL_EQUAL = 6,             /* mask == value */
+    SR_STENCIL_NOT_EQUAL = 7          /* mask != value */
+} sr_stencil_test;
+
+/* StencilOp (src/stencil.rs:133-164); wrap selects Increment/Decrement{wrap}. */
+typedef enum sr_stencil_op {
+    SR_STENCIL_KEEP = 0,
+    SR_STENCIL_INVERT = 1,
+    SR_STENCIL_ZERO = 2,
+    SR_STENCIL_REPLACE = 3,
+    SR_STENCIL_INCREMENT = 4,
+    SR_STENCIL_DECREMENT = 5
+} sr_stencil_op;
+
+typedef enum sr_stage {
+    SR_STAGE_VERTEX = 0,
+    SR_STAGE_GEOMETRY = 1,
+    SR_STAGE_FRAGMENT = 2,
+    SR_STAGE_BLEND = 3
+} sr_stage;
+
+/* Sampling for the textured shaders (src/texture.rs:14-18,89-113). */
+typedef enum sr_filter { SR_SAMPLE_NEAREST = 0, SR_SAMPLE_BILINEAR = 1 } sr_filter;
+typedef enum sr_edge { SR_SAMPLE_CLAMP = 0, SR_SAMPLE_WRAP = 1 } sr_edge;
+
+/* --------------------------------------------------------------- structs */
+
+/* Framebuffer attachments (RenderBuffer<ColorDepthStencilAttachments<C,D,S>>,
+ * src/framebuffer/renderbuffer/mod.rs:16-30).  Planes are stored SoA on the
+ * device: colour plane, f32 depth plane, u8 stencil plane. */
+typedef struct sr_fb_desc {
+    uint32_t width;
+    uint32_t height;
+    uint32_t color_format;   /* sr_color_format */
+    uint32_t depth;          /* 1: f32 depth attachment, 0: () */
+    uint32_t stencil;        /* 1: u8 stencil attachment, 0: () */
+} sr_fb_desc;
+
+/* Viewport<f32> (src/geometry/clipvertex.rs:28-57) */
+typedef struct sr_viewport {
+    float x, y, width, height, near, far;
+} sr_viewport;
+
+typedef struct sr_pipeline sr_pipeline;
+typedef struct sr_mesh sr_mesh;
+typedef struct sr_texture sr_texture;
+
+/* One pass of the typestate chain, flattened.  Defaults (sr_draw_init):
+ * triangles, no GS, no culling, blend 0 (the `()` blend: replace), 128x128
+ * semantic tiles (DEFAULT_TILE_SIZE, fragment.rs:29), stencil ref 0. */
+typedef struct sr_draw {
+    const sr_mesh* mesh;
+    uint32_t prim;            /* sr_prim: T of render_mesh(T, ...)                 */
+    int32_t vs;               /* vertex shader id                                  */
+    uint32_t gs_mode;         /* sr_gs_mode                                        */
+    int32_t gs;               /* geometry shader id for SR_GS_NAMED                */
+    sr_viewport viewport;     /* run_to_fragment / finish viewport                 */
+    uint32_t cull;            /* sr_cull: FragmentShader::cull_faces               */
+    int32_t fs;               /* fragment shader id                                */
+    int32_t blend;            /* blend id; 0 = `()` (source replaces destination) */
+    uint32_t aa_lines;        /* FragmentShader::antialiased_lines                 */
+    uint32_t tile_w, tile_h;  /* FragmentShader::tile_size (semantic tile)         */
+    uint32_t stencil_ref;     /* render_mesh(.., Some(stencil)), default 0         */
+    const sr_texture* texture;/* texture read by textured fragment shaders         */
+    uint32_t tex_filter;      /* sr_filter */
+    uint32_t tex_edge;        /* sr_edge */
+} sr_draw;
+
+/* Per-draw counters gathered on the device. */
+typedef struct sr_stats {
+    uint64_t triangles_in;        /* input primitives (indices / 3)                */
+    uint64_t triangles_generated; /* primitives after the geometry stage           */
+    uint64_t triangles_raster;    /* primitives that can produce fragments         */
+    uint64_t unsafe_triangles;    /* primitives rasterised against every tile      */
+    uint64_t bin_entries;         /* (bin, primitive) pairs written by binning     */
+    uint64_t fragments;           /* covered pixel centres reaching the depth test,
+                                     counted once per pixel and primitive          */
+    uint32_t nan_bbox;            /* primitives skipped for an all-NaN bbox        */
+    uint32_t overflow;            /* nonzero if a fixed-capacity buffer overflowed */
+} sr_stats;
+
+/* -------------------------------------------------------------- pipeline */
+
+/* Pipeline::from_framebuffer (src/pipeline/mod.rs:110-140): width and height
+ * must be non-zero (asserted there); the stencil config starts as Always/Keep.
+ * `uniforms` points to an sr_uniforms (include/sr_shaders.h) and may be NULL. */
+SR_API int sr_pipeline_create(const sr_fb_desc* fb, const void* uniforms, size_t uniforms_size,
+                              sr_pipeline** out);
+/* PipelineObject::uniforms_mut (src/pipeline/mod.rs:43-45) */
+SR_API int sr_pipeline_set_uniforms(sr_pipeline* p, const void* uniforms, size_t uniforms_size);
+/* PipelineObject::stencil_config_mut with GenericStencilConfig
+ * (src/pipeline/mod.rs:86-88, src/stencil.rs:182-199) */
+SR_API int sr_pipeline_set_stencil(sr_pipeline* p, int test, int op, int wrap);
+/* PipelineObject::threadpool_mut (src/pipeline/mod.rs:78): the CUDA stream
+ * (cudaStream_t as void*) that render calls are ordered on; NULL = legacy default. */
+SR_API int sr_pipeline_set_stream(sr_pipeline* p, void* stream);
+SR_API int sr_pipeline_destroy(sr_pipeline* p);
+
+/* Framebuffer::clear (src/framebuffer/mod.rs:36, renderbuffer/mod.rs:125-133):
+ * colour <- *color (float[4] for RGBA32F, uint8[4] for RGBA8), depth <- f32::MIN,
+ * stencil <- 0. */
+SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color);
+/* PixelRead / UnsafeFramebuffer getters (src/pixels/mod.rs:46-77): copy planes
+ * to host memory (any pointer may be NULL); synchronises the pipeline stream. */
+SR_API int sr_framebuffer_read(sr_pipeline* p, void* color, float* depth, uint8_t* stencil);
+/* PixelWrite / UnsafeFramebuffer setters: host planes -> device (NULL skips). */
+SR_API int sr_framebuffer_write(sr_pipeline* p, const void* color, const float* depth,
+                                const uint8_t* stencil);
+/* Device addresses of the planes (for device-resident consumers). */
+SR_API int sr_framebuffer_device_ptrs(sr_pipeline* p, void** color, float** depth, uint8_t** stencil);
+
+/* ------------------------------------------------------------ resources */
+
+/* Mesh<V> (src/mesh.rs:38-64) uploaded as SoA f32 attribute planes (each
+ * n_verts floats; the vertex shader fixes their meaning) plus u32 indices.
+ * Host buffers are copied before return; the mesh is immutable afterwards. */
+SR_API int sr_mesh_upload(const float* const* planes, uint32_t n_planes, uint32_t n_verts,
+                          const uint32_t* indices, uint64_t n_indices, sr_mesh** out);
+SR_API int sr_mesh_free(sr_mesh* m);
+/* Device bytes held by a mesh (for HBM budgeting). */
+SR_API uint64_t sr_mesh_bytes(const sr_mesh* m);
+
+/* An RGBA8 texture (r in the low byte) read by the textured shaders. */
+SR_API int sr_texture_upload(const uint32_t* rgba8, uint32_t width, uint32_t height, sr_texture** out);
+SR_API int sr_texture_free(sr_texture* t);
+
+/* Shader registry: device functions compiled into the library, looked up by
+ * name.  Stage is sr_stage.  Names: vertex "mvp_pos_nrm", "mvp_pos_nrm_uv",
+ * "clip_color"; fragment "blinn_phong_dir", "textured_blinn_phong",
+ * "vertex_color", "aces_lights", "constant_color"; blend "replace", "over";
+ * geometry "clip", "vertex_normals", "face_normals". */
+SR_API int sr_shader_lookup(const char* name, int stage, int* id);
+
+/* --------------------------------------------------------------- render */
+
+SR_API void sr_draw_init(sr_draw* d);
+/* Runs one pass of the chain on the pipeline's stream (see sr_draw). */
+SR_API int sr_render(sr_pipeline* p, const sr_draw* d);
+/* Waits for the pipeline's stream; returns the first device-recorded error of
+ * the draws since the previous sync (SR_ENAN, SR_EOVERFLOW) or SR_ECUDA. */
+SR_API int sr_sync(sr_pipeline* p);
+/* Counters of the most recent sr_render (valid after sr_sync). */
+SR_API int sr_get_stats(sr_pipeline* p, sr_stats* out);
+
+/* Human-readable name of a status code. */
+SR_API const char* sr_status_string(int status);
+/* Library version, e.g. "softrender-gb300 0.1.0 sm_103a". */
+SR_API const char* sr_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SR_H */

@@ -1,0 +1,556 @@
+/*
+ * sr_shaders.h — shader arithmetic shared by the CUDA device code and host code.
+ *
+ * In softrender the vertex, fragment and blend stages are user closures written
+ * against nalgebra (examples/suzanne.rs:123-183, full_example/src/shaders.rs,
+ * full_example/src/texture.rs, full_example/src/color.rs).  This header restates
+ * the arithmetic of those closures once, as __host__ __device__ functions, so
+ * that the GPU kernels and any host-side caller execute the same IEEE-754 FP32
+ * operation sequence.  It must be compiled without FMA contraction
+ * (nvcc -fmad=false; gcc/clang -ffp-contract=off) and without fast-math.
+ *
+ * Operation-order conventions (nalgebra 0.12, num-traits 0.1 semantics):
+ *   - dot / norm_squared: left-to-right sum  ((a0*b0 + a1*b1) + a2*b2) + a3*b3
+ *   - Matrix4 * Vector4 and Matrix4 * Matrix4: each output element summed k=0..3
+ *   - Vector / scalar: component-wise IEEE division
+ *   - f32::min / f32::max: NaN-ignoring (fminf / fmaxf)
+ *   - f32::powi: square-and-multiply, the algorithm of LLVM's __powisf2
+ *   - `as u8`: truncate toward zero, saturate to [0,255], NaN -> 0
+ * f32::powf is libm's in the reference; here it is sr_powf below (double-float
+ * log2 + exp2, own implementation from the series stated in its comment).
+ *
+ * Matrices are 16 floats, row-major: m[row*4 + col].
+ */
+#ifndef SR_SHADERS_H
+#define SR_SHADERS_H
+
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define SR_HD __host__ __device__ __forceinline__
+#else
+#define SR_HD static inline
+#endif
+
+#if !defined(__CUDACC__)
+#include <math.h>
+#endif
+
+#ifdef __cplusplus
+extern "C++" {
+#endif
+
+struct sr_v4 { float x, y, z, w; };
+
+SR_HD sr_v4 sr_make_v4(float x, float y, float z, float w) { sr_v4 r; r.x = x; r.y = y; r.z = z; r.w = w; return r; }
+
+SR_HD uint32_t sr_f2u(float f) {
+#if defined(__CUDA_ARCH__)
+    return __float_as_uint(f);
+#else
+    uint32_t u; memcpy(&u, &f, 4); return u;
+#endif
+}
+SR_HD float sr_u2f(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+    return __uint_as_float(u);
+#else
+    float f; memcpy(&f, &u, 4); return f;
+#endif
+}
+
+SR_HD bool sr_isnan(float x) { return x != x; }
+SR_HD bool sr_isinf(float x) { return (sr_f2u(x) & 0x7fffffffu) == 0x7f800000u; }
+SR_HD float sr_fabs(float x) { return sr_u2f(sr_f2u(x) & 0x7fffffffu); }
+
+/* f32::min / f32::max: if one argument is NaN the other is returned. */
+SR_HD float sr_min(float a, float b) {
+    if (sr_isnan(a)) return b;
+    if (sr_isnan(b)) return a;
+    return a < b ? a : b;
+}
+SR_HD float sr_max(float a, float b) {
+    if (sr_isnan(a)) return b;
+    if (sr_isnan(b)) return a;
+    return a > b ? a : b;
+}
+
+SR_HD float sr_floor(float x) {
+#if defined(__CUDA_ARCH__)
+    return floorf(x);
+#else
+    return floorf(x);
+#endif
+}
+SR_HD float sr_rint(float x) {  /* round half to even */
+#if defined(__CUDA_ARCH__)
+    return rintf(x);
+#else
+    return rintf(x);
+#endif
+}
+SR_HD float sr_sqrt(float x) {  /* IEEE correctly rounded on both sides */
+#if defined(__CUDA_ARCH__)
+    return __fsqrt_rn(x);
+#else
+    return sqrtf(x);
+#endif
+}
+
+/* Rust `f as u8` (saturating cast): NaN -> 0, truncation toward zero. */
+SR_HD uint8_t sr_f32_to_u8(float x) {
+    if (!(x > 0.0f)) return 0;
+    if (x >= 255.0f) return 255;
+    return (uint8_t)(int)x;
+}
+
+/* ---------------------------------------------------------------- vectors */
+SR_HD sr_v4 sr_add4(sr_v4 a, sr_v4 b) { return sr_make_v4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w); }
+SR_HD sr_v4 sr_sub4(sr_v4 a, sr_v4 b) { return sr_make_v4(a.x - b.x, a.y - b.y, a.z - b.z, a.w - b.w); }
+SR_HD sr_v4 sr_scale4(sr_v4 a, float s) { return sr_make_v4(a.x * s, a.y * s, a.z * s, a.w * s); }
+SR_HD float sr_dot4(sr_v4 a, sr_v4 b) { return ((a.x * b.x + a.y * b.y) + a.z * b.z) + a.w * b.w; }
+/* nalgebra normalize(): self / self.norm(), norm = sqrt(norm_squared) */
+SR_HD sr_v4 sr_normalize4(sr_v4 a) {
+    float n = sr_sqrt(sr_dot4(a, a));
+    return sr_make_v4(a.x / n, a.y / n, a.z / n, a.w / n);
+}
+
+/* Matrix4 * Vector4 (row-major storage) */
+SR_HD sr_v4 sr_m4_mul_v4(const float* m, sr_v4 v) {
+    sr_v4 r;
+    r.x = ((m[0] * v.x + m[1] * v.y) + m[2] * v.z) + m[3] * v.w;
+    r.y = ((m[4] * v.x + m[5] * v.y) + m[6] * v.z) + m[7] * v.w;
+    r.z = ((m[8] * v.x + m[9] * v.y) + m[10] * v.z) + m[11] * v.w;
+    r.w = ((m[12] * v.x + m[13] * v.y) + m[14] * v.z) + m[15] * v.w;
+    return r;
+}
+/* Matrix4 * Matrix4 (row-major storage), out may not alias a or b */
+SR_HD void sr_m4_mul_m4(const float* a, const float* b, float* out) {
+    for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+            out[i * 4 + j] = ((a[i * 4 + 0] * b[0 * 4 + j] + a[i * 4 + 1] * b[1 * 4 + j])
+                              + a[i * 4 + 2] * b[2 * 4 + j]) + a[i * 4 + 3] * b[3 * 4 + j];
+}
+
+/* ------------------------------------------------------ powi (square-and-multiply) */
+SR_HD float sr_powi(float x, int n) {
+    int recip = n < 0;
+    unsigned b = recip ? (unsigned)(-(long long)n) : (unsigned)n;
+    float r = 1.0f;
+    for (;;) {
+        if (b & 1u) r = r * x;
+        b >>= 1;
+        if (b == 0) break;
+        x = x * x;
+    }
+    return recip ? 1.0f / r : r;
+}
+
+/* ---------------------------------------------- double-float building blocks
+ * Error-free transformations without FMA: Knuth's TwoSum, Dekker's FastTwoSum,
+ * Veltkamp splitting (splitter 2^12+1 for binary32) and Dekker's TwoProduct.  */
+SR_HD void sr_two_sum(float a, float b, float* s, float* e) {
+    float ss = a + b;
+    float bb = ss - a;
+    *e = (a - (ss - bb)) + (b - bb);
+    *s = ss;
+}
+SR_HD void sr_fast_two_sum(float a, float b, float* s, float* e) {  /* |a| >= |b| */
+    float ss = a + b;
+    *e = b - (ss - a);
+    *s = ss;
+}
+SR_HD void sr_split(float a, float* hi, float* lo) {
+    float c = 4097.0f * a;
+    float h = c - (c - a);
+    *hi = h;
+    *lo = a - h;
+}
+SR_HD void sr_two_prod(float a, float b, float* p, float* e) {
+    float pp = a * b;
+    float ah, al, bh, bl;
+    sr_split(a, &ah, &al);
+    sr_split(b, &bh, &bl);
+    *e = (((ah * bh - pp) + ah * bl) + al * bh) + al * bl;
+    *p = pp;
+}
+
+/* 2^n for integer n in [-126, 127] */
+SR_HD float sr_exp2i(int n) { return sr_u2f((uint32_t)(n + 127) << 23); }
+
+/*
+ * log2(x) for finite x > 0, returned as a double-float hi + lo.
+ * x = m * 2^e with m in [sqrt(1/2), sqrt(2)); ln(m) = 2*atanh(s), s = (m-1)/(m+1),
+ * atanh(s) = s + s^3/3 + s^5/5 + ... (|s| <= 0.1716, truncated after s^13,
+ * truncation error < 1e-12 relative).  The leading term 2s is carried as a
+ * double-float (compensated division), the odd-power tail in single precision.
+ */
+SR_HD void sr_log2_df(float x, float* lhi, float* llo) {
+    uint32_t bits = sr_f2u(x);
+    int e = (int)((bits >> 23) & 0xffu);
+    if (e == 0) {                     /* subnormal: rescale by 2^23 */
+        x = x * 8388608.0f;
+        bits = sr_f2u(x);
+        e = (int)((bits >> 23) & 0xffu) - 23;
+    }
+    e -= 127;
+    float m = sr_u2f((bits & 0x007fffffu) | 0x3f800000u);  /* [1,2) */
+    if (m > 1.41421353816986083984375f) { m = m * 0.5f; e += 1; }
+    float f = m - 1.0f;               /* exact (Sterbenz) */
+    float dh, dl;
+    sr_two_sum(m, 1.0f, &dh, &dl);    /* m + 1 as double-float */
+    float sh = f / dh;
+    float ph, pl;
+    sr_two_prod(sh, dh, &ph, &pl);
+    float r = ((f - ph) - pl) - sh * dl;
+    float sl = r / dh;
+    float s2 = sh * sh;
+    float poly = 0.1538461538461538f;                 /* 2/13 */
+    poly = 0.1818181818181818f + s2 * poly;           /* 2/11 */
+    poly = 0.2222222222222222f + s2 * poly;           /* 2/9  */
+    poly = 0.2857142857142857f + s2 * poly;           /* 2/7  */
+    poly = 0.4f + s2 * poly;                          /* 2/5  */
+    poly = 0.6666666666666666f + s2 * poly;           /* 2/3  */
+    float tail = (sh * s2) * poly;
+    float ln_h, ln_l;
+    sr_fast_two_sum(2.0f * sh, 2.0f * sl + tail, &ln_h, &ln_l);
+    /* multiply by log2(e) = LOG2E_HI + LOG2E_LO */
+    const float LOG2E_HI = 0x1.715476p+0f;
+    const float LOG2E_LO = 0x1.4ae0cp-26f;
+    float qh, ql;
+    sr_two_prod(ln_h, LOG2E_HI, &qh, &ql);
+    ql = ql + (ln_h * LOG2E_LO + ln_l * LOG2E_HI);
+    float th, tl;
+    sr_two_sum((float)e, qh, &th, &tl);
+    tl = tl + ql;
+    sr_fast_two_sum(th, tl, lhi, llo);
+}
+
+/*
+ * 2^(th + tl) for a double-float exponent.  n = rint(th), f = (th - n) + tl,
+ * r = f*ln2 (double-float), e^r by its Taylor series to r^8 (|r| <= 0.35,
+ * truncation < 2e-9 relative), then an exact scale by 2^n.
+ */
+SR_HD float sr_exp2_df(float th, float tl) {
+    if (sr_isnan(th)) return th;
+    if (th >= 128.0f) return sr_u2f(0x7f800000u);
+    if (th < -151.0f) return 0.0f;
+    float n = sr_rint(th);
+    float f = (th - n) + tl;
+    const float LN2_HI = 0x1.62e43p-1f;
+    const float LN2_LO = -0x1.05c61p-29f;
+    float rh, rl;
+    sr_two_prod(f, LN2_HI, &rh, &rl);
+    rl = rl + f * LN2_LO;
+    float p = 2.4801587301587302e-05f;                /* 1/8! */
+    p = 1.9841269841269841e-04f + rh * p;             /* 1/7! */
+    p = 1.3888888888888889e-03f + rh * p;             /* 1/6! */
+    p = 8.3333333333333332e-03f + rh * p;             /* 1/5! */
+    p = 4.1666666666666664e-02f + rh * p;             /* 1/4! */
+    p = 1.6666666666666666e-01f + rh * p;             /* 1/3! */
+    p = 0.5f + rh * p;                                /* 1/2! */
+    p = (rh * rh) * p;
+    float res = 1.0f + (rh + (rl + p));
+    int ni = (int)n;
+    if (ni >= -126 && ni <= 127) return res * sr_exp2i(ni);
+    int n1 = ni / 2;
+    int n2 = ni - n1;
+    return (res * sr_exp2i(n1)) * sr_exp2i(n2);
+}
+
+SR_HD bool sr_is_integer(float y) { return sr_floor(y) == y && !sr_isinf(y); }
+SR_HD bool sr_is_odd_integer(float y) {
+    if (!sr_is_integer(y)) return false;
+    float a = sr_fabs(y);
+    if (a >= 16777216.0f) return false;
+    return ((long long)a & 1LL) != 0;
+}
+
+/* f32::powf replacement with C99 Annex F special cases. */
+SR_HD float sr_powf(float x, float y) {
+    const float INF = sr_u2f(0x7f800000u);
+    if (y == 0.0f) return 1.0f;
+    if (x == 1.0f) return 1.0f;
+    if (sr_isnan(x) || sr_isnan(y)) return x + y;
+    float ax = sr_fabs(x);
+    if (sr_isinf(y)) {
+        if (ax == 1.0f) return 1.0f;
+        bool big = ax > 1.0f;
+        return (big == (y > 0.0f)) ? INF : 0.0f;
+    }
+    bool odd = sr_is_odd_integer(y);
+    if (x == 0.0f) {
+        if (y < 0.0f) return odd ? (sr_f2u(x) >> 31 ? -INF : INF) : INF;
+        return odd ? x : 0.0f;
+    }
+    if (sr_isinf(x)) {
+        bool neg = x < 0.0f;
+        if (y < 0.0f) return (neg && odd) ? -0.0f : 0.0f;
+        return (neg && odd) ? -INF : INF;
+    }
+    float sign = 1.0f;
+    if (x < 0.0f) {
+        if (!sr_is_integer(y)) return (x - x) / (x - x);  /* NaN */
+        if (odd) sign = -1.0f;
+    }
+    float lh, ll;
+    sr_log2_df(ax, &lh, &ll);
+    float th, tl;
+    sr_two_prod(y, lh, &th, &tl);
+    tl = tl + y * ll;
+    float t2h, t2l;
+    sr_fast_two_sum(th, tl, &t2h, &t2l);
+    return sign * sr_exp2_df(t2h, t2l);
+}
+
+/* ------------------------------------------------------------------ colour */
+/* full_example/src/color.rs:5-17, the alpha "over" operator on f32 RGBA. */
+SR_HD float sr_over_component(float x, float y, float a, float b) {
+    float a1 = 1.0f - a;
+    return (x * a + (y * b) * a1) / (a + b * a1);
+}
+SR_HD sr_v4 sr_blend_over_f32(sr_v4 src, sr_v4 dst) {
+    return sr_make_v4(sr_over_component(src.x, dst.x, src.w, dst.w),
+                      sr_over_component(src.y, dst.y, src.w, dst.w),
+                      sr_over_component(src.z, dst.z, src.w, dst.w),
+                      src.w + dst.w * (1.0f - src.w));
+}
+SR_HD uint32_t sr_pack_rgba8(uint8_t r, uint8_t g, uint8_t b, uint8_t a) {
+    return (uint32_t)r | ((uint32_t)g << 8) | ((uint32_t)b << 16) | ((uint32_t)a << 24);
+}
+/* RGBA f32 in [0,1] -> RGBA8 via (c * 255.0) as u8 per channel. */
+SR_HD uint32_t sr_to_rgba8(sr_v4 c) {
+    return sr_pack_rgba8(sr_f32_to_u8(c.x * 255.0f), sr_f32_to_u8(c.y * 255.0f),
+                         sr_f32_to_u8(c.z * 255.0f), sr_f32_to_u8(c.w * 255.0f));
+}
+/* RGBA8 -> f32 as in from_image_texel (full_example/src/texture.rs:38-45): c as f32 / 255.0 */
+SR_HD sr_v4 sr_from_rgba8(uint32_t p) {
+    return sr_make_v4((float)(p & 0xffu) / 255.0f, (float)((p >> 8) & 0xffu) / 255.0f,
+                      (float)((p >> 16) & 0xffu) / 255.0f, (float)(p >> 24) / 255.0f);
+}
+/* Over operator on RGBA8: channels to f32 (c/255), over, back with `as u8`. */
+SR_HD uint32_t sr_blend_over_rgba8(uint32_t src, uint32_t dst) {
+    return sr_to_rgba8(sr_blend_over_f32(sr_from_rgba8(src), sr_from_rgba8(dst)));
+}
+
+/* decode_gamma / encode_gamma (full_example/src/color.rs:41-57) */
+SR_HD sr_v4 sr_decode_gamma(sr_v4 c, float gamma) {
+    return sr_make_v4(sr_powf(c.x, gamma), sr_powf(c.y, gamma), sr_powf(c.z, gamma), c.w);
+}
+SR_HD sr_v4 sr_encode_gamma(sr_v4 c, float gamma) {
+    float inv = 1.0f / gamma;
+    return sr_make_v4(sr_powf(c.x, inv), sr_powf(c.y, inv), sr_powf(c.z, inv), c.w);
+}
+/* ACES filmic tonemap (full_example/src/color.rs:19-35) */
+SR_HD float sr_aces_component(float x) {
+    return (x * (2.51f * x + 0.03f)) / (x * (2.43f * x + 0.59f) + 0.14f);
+}
+
+/* ----------------------------------------------------------------- texture
+ * Bilinear / nearest sampling of an RGBA8 texture, restating
+ * full_example/src/texture.rs:47-84 (clamp: u.min(1).max(0); wrap: u.fract()).
+ * Divergence, documented: the reference reads texel x+1 == width when
+ * u*(W-1)+0.5 >= W-1 (an out-of-bounds panic at u == 1); here x+1 and y+1 are
+ * clamped to the last texel, and x, y to [0, W-1] / [0, H-1].
+ */
+enum { SR_FILTER_NEAREST = 0, SR_FILTER_BILINEAR = 1 };
+enum { SR_EDGE_CLAMP = 0, SR_EDGE_WRAP = 1 };
+
+SR_HD float sr_fract(float v) {  /* Rust f32::fract: v - trunc(v) */
+    return v - truncf(v);
+}
+SR_HD uint32_t sr_clamp_index(float f, uint32_t n) {
+    if (!(f > 0.0f)) return 0;                 /* NaN and negatives -> 0 */
+    if (f >= (float)(n - 1)) return n - 1;
+    return (uint32_t)f;
+}
+SR_HD sr_v4 sr_texel(const uint32_t* tex, uint32_t w, uint32_t x, uint32_t y) {
+#if defined(__CUDA_ARCH__)
+    return sr_from_rgba8(__ldg(tex + (size_t)y * w + x));
+#else
+    return sr_from_rgba8(tex[(size_t)y * w + x]);
+#endif
+}
+SR_HD sr_v4 sr_sample_rgba8(const uint32_t* tex, uint32_t w, uint32_t h, float u, float v,
+                            int filter, int edge) {
+    if (edge == SR_EDGE_CLAMP) {
+        u = sr_max(sr_min(u, 1.0f), 0.0f);
+        v = sr_max(sr_min(v, 1.0f), 0.0f);
+    } else {
+        u = sr_fract(u);
+        v = sr_fract(v);
+    }
+    if (filter == SR_FILTER_NEAREST) {
+        uint32_t x = sr_clamp_index(roundf(u * (float)(w - 1)), w);
+        uint32_t y = sr_clamp_index(roundf(v * (float)(h - 1)), h);
+        return sr_texel(tex, w, x, y);
+    }
+    float uu = (u * (float)(w - 1)) + 0.5f;
+    float vv = (v * (float)(h - 1)) + 0.5f;
+    uint32_t x = sr_clamp_index(sr_floor(uu), w);
+    uint32_t y = sr_clamp_index(sr_floor(vv), h);
+    float u_ratio = uu - (float)x;
+    float v_ratio = vv - (float)y;
+    float u_opp = 1.0f - u_ratio;
+    float v_opp = 1.0f - v_ratio;
+    uint32_t x1 = x + 1 < w ? x + 1 : w - 1;
+    uint32_t y1 = y + 1 < h ? y + 1 : h - 1;
+    sr_v4 a = sr_texel(tex, w, x, y);
+    sr_v4 b = sr_texel(tex, w, x1, y);
+    sr_v4 c = sr_texel(tex, w, x, y1);
+    sr_v4 d = sr_texel(tex, w, x1, y1);
+    sr_v4 r;
+    r.x = (a.x * u_opp + b.x * u_ratio) * v_opp + (c.x * u_opp + d.x * u_ratio) * v_ratio;
+    r.y = (a.y * u_opp + b.y * u_ratio) * v_opp + (c.y * u_opp + d.y * u_ratio) * v_ratio;
+    r.z = (a.z * u_opp + b.z * u_ratio) * v_opp + (c.z * u_opp + d.z * u_ratio) * v_ratio;
+    r.w = (a.w * u_opp + b.w * u_ratio) * v_opp + (c.w * u_opp + d.w * u_ratio) * v_ratio;
+    return r;
+}
+
+/* ------------------------------------------------------------------ uniforms
+ * Global uniforms for the shaders compiled into this library; the layout
+ * follows GlobalUniforms of full_example/src/uniforms.rs with the light set
+ * reduced to what each shader reads.  Set through sr_pipeline_set_uniforms.
+ */
+typedef struct sr_uniforms {
+    float model[16];        /* object -> world                         */
+    float mit[16];          /* inverse transpose of model (normals)    */
+    float view[16];         /* world -> camera                         */
+    float projection[16];   /* camera -> clip                          */
+    float camera[4];        /* camera position (w = 1)                 */
+    float light_dir[4];     /* directional light, normalised, w = 0    */
+    float light_pos[4];     /* point light position (w = 1)            */
+    float color[4];         /* linear surface colour                   */
+    float intensity;        /* light intensity                         */
+    float shininess;        /* Blinn-Phong shininess (suzanne: 32)     */
+    float ior;              /* Fresnel index of refraction (1.45)      */
+    float gamma;            /* display gamma (2.2)                     */
+    float light_color[4][4];/* 4-light ACES shader: colours            */
+    float light_pos4[4][4]; /* 4-light ACES shader: positions (w = 1)  */
+    float light_int4[4];    /* 4-light ACES shader: intensities        */
+    /* derived, filled by the library from the matrices above */
+    float pv[16];           /* projection * view                        */
+    float mvp[16];          /* (projection * view) * model              */
+} sr_uniforms;
+
+SR_HD void sr_uniforms_derive(sr_uniforms* u) {
+    sr_m4_mul_m4(u->projection, u->view, u->pv);
+    sr_m4_mul_m4(u->pv, u->model, u->mvp);
+}
+
+/* ----------------------------------------------------------- vertex shaders
+ * Each returns the clip-space position and writes the varyings (the
+ * declare_uniforms! structure, flattened field by field, component by
+ * component).  Attribute planes are addressed by the caller.
+ */
+
+/* examples/suzanne.rs:123-141: world = model*pos; n = normalize(mit*n4);
+ * clip = (projection*view)*world.  Varyings: world position (4), normal (4). */
+SR_HD sr_v4 sr_vs_mvp_pos_nrm(const sr_uniforms* U, const float* a, float* k) {
+    sr_v4 pos = sr_make_v4(a[0], a[1], a[2], 1.0f);
+    sr_v4 n4 = sr_make_v4(a[3], a[4], a[5], 0.0f);
+    sr_v4 world = sr_m4_mul_v4(U->model, pos);
+    sr_v4 nrm = sr_normalize4(sr_m4_mul_v4(U->mit, n4));
+    sr_v4 clip = sr_m4_mul_v4(U->pv, world);
+    k[0] = world.x; k[1] = world.y; k[2] = world.z; k[3] = world.w;
+    k[4] = nrm.x; k[5] = nrm.y; k[6] = nrm.z; k[7] = nrm.w;
+    return clip;
+}
+
+/* full_example/src/shaders.rs:8-31: world = model*pos; n = normalize(mit*n4);
+ * clip = ((projection*view)*model)*pos.  Varyings: position (4), normal (4), uv (2). */
+SR_HD sr_v4 sr_vs_mvp_pos_nrm_uv(const sr_uniforms* U, const float* a, float* k) {
+    sr_v4 pos = sr_make_v4(a[0], a[1], a[2], 1.0f);
+    sr_v4 n4 = sr_make_v4(a[3], a[4], a[5], 0.0f);
+    sr_v4 world = sr_m4_mul_v4(U->model, pos);
+    sr_v4 nrm = sr_normalize4(sr_m4_mul_v4(U->mit, n4));
+    sr_v4 clip = sr_m4_mul_v4(U->mvp, pos);
+    k[0] = world.x; k[1] = world.y; k[2] = world.z; k[3] = world.w;
+    k[4] = nrm.x; k[5] = nrm.y; k[6] = nrm.z; k[7] = nrm.w;
+    k[8] = a[6]; k[9] = a[7];
+    return clip;
+}
+
+/* Positions already in clip space (x, y, z, w) plus an RGBA colour given as
+ * four floats in [0,1]; the colour is passed through as varyings. */
+SR_HD sr_v4 sr_vs_clip_color(const sr_uniforms* U, const float* a, float* k) {
+    (void)U;
+    k[0] = a[4]; k[1] = a[5]; k[2] = a[6]; k[3] = a[7];
+    return sr_make_v4(a[0], a[1], a[2], a[3]);
+}
+
+/* Positions in clip space with w = 1 (x, y, z planes) plus a packed RGBA8
+ * colour plane (the u32 bit pattern stored in a float plane); the colour is
+ * passed through as four varyings c/255. */
+SR_HD sr_v4 sr_vs_clip_rgba8(const sr_uniforms* U, const float* a, float* k) {
+    (void)U;
+    sr_v4 c = sr_from_rgba8(sr_f2u(a[3]));
+    k[0] = c.x; k[1] = c.y; k[2] = c.z; k[3] = c.w;
+    return sr_make_v4(a[0], a[1], a[2], 1.0f);
+}
+
+/* --------------------------------------------------------- fragment shaders */
+
+/* Fresnel-Schlick (examples/suzanne.rs:163-168) */
+SR_HD float sr_fresnel_schlick(float cos_theta, float ior) {
+    float f0 = sr_powi((1.0f - ior) / (1.0f + ior), 2);
+    return f0 + (1.0f - f0) * sr_powi(1.0f - cos_theta, 5);
+}
+
+/* Blinn-Phong + Fresnel of examples/suzanne.rs:147-183 with one directional
+ * light: L is the constant U->light_dir instead of normalize(light - position).
+ * Returns the gamma-encoded RGBA f32 colour (alpha 1). */
+SR_HD sr_v4 sr_blinn_phong(const sr_uniforms* U, sr_v4 position, sr_v4 normal, sr_v4 color) {
+    sr_v4 camera = sr_make_v4(U->camera[0], U->camera[1], U->camera[2], U->camera[3]);
+    sr_v4 light_dir = sr_make_v4(U->light_dir[0], U->light_dir[1], U->light_dir[2], U->light_dir[3]);
+    sr_v4 view_dir = sr_normalize4(sr_sub4(camera, position));
+    sr_v4 halfway = sr_normalize4(sr_add4(light_dir, view_dir));
+    float NdotL = sr_max(sr_min(sr_dot4(light_dir, normal), 1.0f), 0.0f);
+    float NdotH = sr_max(sr_min(sr_dot4(normal, halfway), 1.0f), 0.0f);
+    float VdotH = sr_max(sr_min(sr_dot4(view_dir, halfway), 1.0f), 0.0f);
+    float f = sr_fresnel_schlick(VdotH, U->ior);
+    float diffuse = NdotL * (1.0f - f);
+    float specular = f * sr_powf(NdotH, U->shininess * 2.0f);
+    float inv_gamma = 1.0f / U->gamma;
+    float I = U->intensity;
+    return sr_make_v4(sr_powf(I * (specular + (diffuse * color.x)), inv_gamma),
+                      sr_powf(I * (specular + (diffuse * color.y)), inv_gamma),
+                      sr_powf(I * (specular + (diffuse * color.z)), inv_gamma),
+                      1.0f);
+}
+
+/* 4-point-light Blinn-Phong with ACES tonemap (full_example/src/shaders.rs:108-163). */
+SR_HD sr_v4 sr_aces_lights(const sr_uniforms* U, sr_v4 position, sr_v4 normal) {
+    sr_v4 camera = sr_make_v4(U->camera[0], U->camera[1], U->camera[2], U->camera[3]);
+    sr_v4 view_dir = sr_normalize4(sr_sub4(camera, position));
+    float g = U->gamma;
+    sr_v4 material = sr_decode_gamma(sr_make_v4(0.25f, 0.25f, 0.25f, 1.0f), g);
+    float albedo = 0.7f;
+    sr_v4 col = sr_make_v4(0.0f, 0.0f, 0.0f, 1.0f);
+    for (int i = 0; i < 4; ++i) {
+        sr_v4 lp = sr_make_v4(U->light_pos4[i][0], U->light_pos4[i][1], U->light_pos4[i][2], U->light_pos4[i][3]);
+        sr_v4 d = sr_sub4(lp, position);
+        float light_distance = sr_sqrt(sr_dot4(d, d));
+        sr_v4 light_dir = sr_normalize4(d);
+        sr_v4 halfway = sr_normalize4(sr_add4(light_dir, view_dir));
+        float intensity = U->light_int4[i] / sr_powi(light_distance, 2);
+        float NdotL = sr_max(sr_min(sr_dot4(light_dir, normal), 1.0f), 0.0f);
+        float NdotH = sr_max(sr_min(sr_dot4(normal, halfway), 1.0f), 0.0f);
+        float VdotH = sr_max(sr_min(sr_dot4(view_dir, halfway), 1.0f), 0.0f);
+        float f = sr_fresnel_schlick(VdotH, U->ior);
+        float diffuse = (1.0f - f) * NdotL;
+        float specular = f * sr_powi(NdotH, 32 * 2);
+        col.x = col.x + intensity * U->light_color[i][0] * (specular + (diffuse * albedo * material.x));
+        col.y = col.y + intensity * U->light_color[i][1] * (specular + (diffuse * albedo * material.y));
+        col.z = col.z + intensity * U->light_color[i][2] * (specular + (diffuse * albedo * material.z));
+    }
+    sr_v4 t = sr_make_v4(sr_aces_component(col.x), sr_aces_component(col.y), sr_aces_component(col.z), col.w);
+    return sr_encode_gamma(t, g);
+}
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SR_SHADERS_H */

@@ -1,0 +1,585 @@
+// sr_api.cu — the C ABI (include/sr.h): pipeline, framebuffer, resources,
+// shader registry and the stream-ordered draw orchestration.
+//
+// A draw is enqueued without host synchronisation: intermediate buffers have
+// grow-only capacities; a stage that would overflow one records the size it
+// needed and poisons the pipeline, after which every framebuffer-writing
+// kernel of that draw and of later draws skips.  sr_sync() then grows the
+// buffers and replays the draws from the first poisoned one, so the
+// framebuffer always ends up exactly as if capacities had been large enough.
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "sr_internal.cuh"
+#include "sr_scan.cuh"
+
+using namespace sr;
+
+#define SR_CK(x)                                   \
+    do {                                           \
+        cudaError_t e_ = (x);                      \
+        if (e_ != cudaSuccess) {                   \
+            last_cuda_error() = e_;                \
+            return e_ == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA; \
+        }                                          \
+    } while (0)
+
+static cudaError_t& last_cuda_error() {
+    static thread_local cudaError_t e = cudaSuccess;
+    return e;
+}
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;  // elements
+    int ensure(size_t n) {
+        if (n <= cap) return SR_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = n + n / 4 + 64;
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e != cudaSuccess) { last_cuda_error() = e; p = nullptr; return SR_ENOMEM; }
+        cap = want;
+        return SR_OK;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+};
+
+struct PendingDraw {
+    sr_draw d;
+    sr_uniforms U;
+    uint32_t stencil_test, stencil_op, stencil_wrap;
+};
+
+}  // namespace
+
+struct sr_pipeline {
+    sr_fb_desc fb;
+    void* color = nullptr;
+    float* depth = nullptr;
+    uint8_t* stencil = nullptr;
+    sr_uniforms U;
+    uint32_t stencil_test = SR_STENCIL_ALWAYS, stencil_op = SR_STENCIL_KEEP, stencil_wrap = 1;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    DeviceFlags* flags = nullptr;     // device
+    DeviceFlags* hflags = nullptr;    // pinned host mirror
+    // workspace
+    DevBuf<float4> clip4, scr4;
+    DevBuf<float> vary;
+    DevBuf<unsigned long long> clip_counts, clip_offsets, clip_tmp;
+    DevBuf<uint32_t> refs;
+    DevBuf<float4> setup;
+    DevBuf<uint2> binrect;
+    DevBuf<uint32_t> bin_counts, bin_off, bin_cursor, bin_tmp, entries;
+    DevBuf<int> st_diff, st_lines;
+    DevBuf<unsigned long long> st_glob;
+    // capacities (elements) requested for the generated geometry
+    uint64_t gen_tri_cap = 0, gen_vert_cap = 0, entry_cap = 0;
+    std::vector<PendingDraw> pending;
+    sr_stats last_stats;
+    bool stats_valid = false;
+};
+
+namespace {
+
+uint32_t bytes_per_color(uint32_t f) { return f == SR_COLOR_RGBA32F ? 16 : f == SR_COLOR_RGBA8 ? 4 : 0; }
+
+struct ShaderName { const char* name; int stage; int id; };
+const ShaderName kShaders[] = {
+    {"mvp_pos_nrm", SR_STAGE_VERTEX, VS_MVP_POS_NRM},
+    {"mvp_pos_nrm_uv", SR_STAGE_VERTEX, VS_MVP_POS_NRM_UV},
+    {"clip_color", SR_STAGE_VERTEX, VS_CLIP_COLOR},
+    {"clip_rgba8", SR_STAGE_VERTEX, VS_CLIP_RGBA8},
+    {"clip", SR_STAGE_GEOMETRY, GS_CLIP},
+    {"vertex_normals", SR_STAGE_GEOMETRY, GS_VERTEX_NORMALS},
+    {"face_normals", SR_STAGE_GEOMETRY, GS_FACE_NORMALS},
+    {"blinn_phong_dir", SR_STAGE_FRAGMENT, FS_BLINN_PHONG_DIR},
+    {"textured_blinn_phong", SR_STAGE_FRAGMENT, FS_TEXTURED_BLINN_PHONG},
+    {"vertex_color", SR_STAGE_FRAGMENT, FS_VERTEX_COLOR},
+    {"aces_lights", SR_STAGE_FRAGMENT, FS_ACES_LIGHTS},
+    {"constant_color", SR_STAGE_FRAGMENT, FS_CONSTANT_COLOR},
+    {"replace", SR_STAGE_BLEND, BLEND_REPLACE},
+    {"over", SR_STAGE_BLEND, BLEND_OVER},
+};
+
+__global__ void fill_u32_kernel(uint32_t* p, size_t n, uint32_t v) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+__global__ void fill_f4_kernel(float4* p, size_t n, float4 v) {
+    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+int fs_min_varyings(int fs) {
+    switch (fs) {
+    case FS_TEXTURED_BLINN_PHONG: return 10;
+    case FS_VERTEX_COLOR: return 4;
+    case FS_CONSTANT_COLOR: return 0;
+    default: return 8;
+    }
+}
+
+}  // namespace
+
+// =================================================================== misc
+extern "C" SR_API const char* sr_status_string(int s) {
+    switch (s) {
+    case SR_OK: return "SR_OK";
+    case SR_EINVAL: return "SR_EINVAL";
+    case SR_ENOMEM: return "SR_ENOMEM";
+    case SR_EBUDGET: return "SR_EBUDGET";
+    case SR_EOVERFLOW: return "SR_EOVERFLOW";
+    case SR_ETIMEOUT: return "SR_ETIMEOUT";
+    case SR_ECUDA: return "SR_ECUDA";
+    case SR_ENAN: return "SR_ENAN";
+    case SR_ENOTFOUND: return "SR_ENOTFOUND";
+    case SR_EBUSY: return "SR_EBUSY";
+    default: return "SR_UNKNOWN";
+    }
+}
+
+extern "C" SR_API const char* sr_version(void) { return "softrender-gb300 0.1.0 sm_103a"; }
+
+extern "C" SR_API int sr_shader_lookup(const char* name, int stage, int* id) {
+    if (!name || !id) return SR_EINVAL;
+    for (const auto& s : kShaders)
+        if (s.stage == stage && std::strcmp(s.name, name) == 0) { *id = s.id; return SR_OK; }
+    return SR_ENOTFOUND;
+}
+
+extern "C" SR_API void sr_draw_init(sr_draw* d) {
+    std::memset(d, 0, sizeof(*d));
+    d->prim = SR_PRIM_TRIANGLE;
+    d->vs = VS_MVP_POS_NRM;
+    d->gs_mode = SR_GS_NONE;
+    d->gs = GS_CLIP;
+    d->cull = SR_CULL_NONE;
+    d->fs = FS_BLINN_PHONG_DIR;
+    d->blend = BLEND_REPLACE;
+    d->tile_w = 128;
+    d->tile_h = 128;
+    d->tex_filter = SR_SAMPLE_BILINEAR;
+    d->tex_edge = SR_SAMPLE_CLAMP;
+}
+
+// =============================================================== pipeline
+extern "C" SR_API int sr_pipeline_create(const sr_fb_desc* fb, const void* uniforms, size_t usz, sr_pipeline** out) {
+    if (!fb || !out) return SR_EINVAL;
+    *out = nullptr;
+    if (fb->width == 0 || fb->height == 0) return SR_EINVAL;               // mod.rs:129-130
+    if (fb->width > 32767 || fb->height > 32767) return SR_EINVAL;
+    if (fb->color_format > SR_COLOR_RGBA8) return SR_EINVAL;
+    if (uniforms && usz != sizeof(sr_uniforms)) return SR_EINVAL;
+    sr_pipeline* p = new (std::nothrow) sr_pipeline();
+    if (!p) return SR_ENOMEM;
+    p->fb = *fb;
+    std::memset(&p->U, 0, sizeof(p->U));
+    if (uniforms) std::memcpy(&p->U, uniforms, sizeof(sr_uniforms));
+    sr_uniforms_derive(&p->U);
+    size_t n = (size_t)fb->width * fb->height;
+    cudaError_t e = cudaSuccess;
+    if (bytes_per_color(fb->color_format)) e = cudaMalloc(&p->color, n * bytes_per_color(fb->color_format));
+    if (e == cudaSuccess && fb->depth) e = cudaMalloc(&p->depth, n * 4);
+    if (e == cudaSuccess && fb->stencil) e = cudaMalloc(&p->stencil, n);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&p->flags, sizeof(DeviceFlags));
+    if (e == cudaSuccess) e = cudaMallocHost(&p->hflags, sizeof(DeviceFlags));
+    if (e != cudaSuccess) {
+        last_cuda_error() = e;
+        sr_pipeline_destroy(p);
+        return e == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA;
+    }
+    p->stream = p->own_stream;
+    DeviceFlags z;
+    std::memset(&z, 0, sizeof(z));
+    z.poison_draw = 0xffffffffu;
+    cudaMemcpy(p->flags, &z, sizeof(z), cudaMemcpyHostToDevice);
+    std::memset(&p->last_stats, 0, sizeof(p->last_stats));
+    // Framebuffer starts cleared (colour 0), like RenderBuffer::with_dimensions
+    uint8_t zero[16] = {0};
+    int st = sr_framebuffer_clear(p, zero);
+    if (st != SR_OK) { sr_pipeline_destroy(p); return st; }
+    cudaStreamSynchronize(p->stream);
+    *out = p;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_pipeline_destroy(sr_pipeline* p) {
+    if (!p) return SR_EINVAL;
+    if (p->stream) cudaStreamSynchronize(p->stream);
+    if (p->color) cudaFree(p->color);
+    if (p->depth) cudaFree(p->depth);
+    if (p->stencil) cudaFree(p->stencil);
+    if (p->flags) cudaFree(p->flags);
+    if (p->hflags) cudaFreeHost(p->hflags);
+    p->clip4.release(); p->scr4.release(); p->vary.release();
+    p->clip_counts.release(); p->clip_offsets.release(); p->clip_tmp.release(); p->refs.release();
+    p->setup.release(); p->binrect.release();
+    p->bin_counts.release(); p->bin_off.release(); p->bin_cursor.release(); p->bin_tmp.release(); p->entries.release();
+    p->st_diff.release(); p->st_lines.release(); p->st_glob.release();
+    if (p->own_stream) cudaStreamDestroy(p->own_stream);
+    delete p;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_pipeline_set_uniforms(sr_pipeline* p, const void* uniforms, size_t usz) {
+    if (!p || !uniforms || usz != sizeof(sr_uniforms)) return SR_EINVAL;
+    std::memcpy(&p->U, uniforms, sizeof(sr_uniforms));
+    sr_uniforms_derive(&p->U);
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_pipeline_set_stencil(sr_pipeline* p, int test, int op, int wrap) {
+    if (!p || test < 0 || test > SR_STENCIL_NOT_EQUAL || op < 0 || op > SR_STENCIL_DECREMENT) return SR_EINVAL;
+    p->stencil_test = (uint32_t)test;
+    p->stencil_op = (uint32_t)op;
+    p->stencil_wrap = wrap ? 1u : 0u;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_pipeline_set_stream(sr_pipeline* p, void* stream) {
+    if (!p) return SR_EINVAL;
+    p->stream = stream ? (cudaStream_t)stream : p->own_stream;
+    return SR_OK;
+}
+
+// ============================================================ framebuffer
+extern "C" SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color) {
+    if (!p || !color) return SR_EINVAL;
+    size_t n = (size_t)p->fb.width * p->fb.height;
+    dim3 b(256), g((unsigned)((n + 255) / 256));
+    if (p->fb.color_format == SR_COLOR_RGBA32F) {
+        float4 c;
+        std::memcpy(&c, color, 16);
+        fill_f4_kernel<<<g, b, 0, p->stream>>>(reinterpret_cast<float4*>(p->color), n, c);
+    } else if (p->fb.color_format == SR_COLOR_RGBA8) {
+        uint32_t c;
+        std::memcpy(&c, color, 4);
+        fill_u32_kernel<<<g, b, 0, p->stream>>>(reinterpret_cast<uint32_t*>(p->color), n, c);
+    }
+    if (p->depth) {
+        float far_ = -3.40282347e+38f;  // f32::MIN (attachments/depth.rs:31)
+        uint32_t fb;
+        std::memcpy(&fb, &far_, 4);
+        fill_u32_kernel<<<g, b, 0, p->stream>>>(reinterpret_cast<uint32_t*>(p->depth), n, fb);
+    }
+    if (p->stencil) SR_CK(cudaMemsetAsync(p->stencil, 0, n, p->stream));
+    SR_CK(cudaGetLastError());
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_sync(sr_pipeline* p);
+
+extern "C" SR_API int sr_framebuffer_read(sr_pipeline* p, void* color, float* depth, uint8_t* stencil) {
+    if (!p) return SR_EINVAL;
+    int st = sr_sync(p);
+    size_t n = (size_t)p->fb.width * p->fb.height;
+    if (color && p->color) SR_CK(cudaMemcpyAsync(color, p->color, n * bytes_per_color(p->fb.color_format), cudaMemcpyDeviceToHost, p->stream));
+    if (depth && p->depth) SR_CK(cudaMemcpyAsync(depth, p->depth, n * 4, cudaMemcpyDeviceToHost, p->stream));
+    if (stencil && p->stencil) SR_CK(cudaMemcpyAsync(stencil, p->stencil, n, cudaMemcpyDeviceToHost, p->stream));
+    SR_CK(cudaStreamSynchronize(p->stream));
+    return st;
+}
+
+extern "C" SR_API int sr_framebuffer_write(sr_pipeline* p, const void* color, const float* depth, const uint8_t* stencil) {
+    if (!p) return SR_EINVAL;
+    size_t n = (size_t)p->fb.width * p->fb.height;
+    if (color && p->color) SR_CK(cudaMemcpyAsync(p->color, color, n * bytes_per_color(p->fb.color_format), cudaMemcpyHostToDevice, p->stream));
+    if (depth && p->depth) SR_CK(cudaMemcpyAsync(p->depth, depth, n * 4, cudaMemcpyHostToDevice, p->stream));
+    if (stencil && p->stencil) SR_CK(cudaMemcpyAsync(p->stencil, stencil, n, cudaMemcpyHostToDevice, p->stream));
+    SR_CK(cudaStreamSynchronize(p->stream));
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_framebuffer_device_ptrs(sr_pipeline* p, void** color, float** depth, uint8_t** stencil) {
+    if (!p) return SR_EINVAL;
+    if (color) *color = p->color;
+    if (depth) *depth = p->depth;
+    if (stencil) *stencil = p->stencil;
+    return SR_OK;
+}
+
+// ============================================================== resources
+extern "C" SR_API int sr_mesh_upload(const float* const* planes, uint32_t n_planes, uint32_t n_verts,
+                                     const uint32_t* indices, uint64_t n_indices, sr_mesh** out) {
+    if (!out || (n_planes && !planes) || n_planes > (uint32_t)MAX_PLANES || (n_indices && !indices)) return SR_EINVAL;
+    *out = nullptr;
+    for (uint64_t i = 0; i < n_indices; ++i)
+        if (indices[i] >= n_verts) return SR_EINVAL;
+    if (n_indices / 3 > (1ull << 30)) return SR_EINVAL;
+    sr_mesh* m = new (std::nothrow) sr_mesh();
+    if (!m) return SR_ENOMEM;
+    m->n_planes = n_planes;
+    m->n_verts = n_verts;
+    m->n_pad = (n_verts + 3) & ~3u;
+    m->n_indices = n_indices;
+    m->planes = nullptr;
+    m->indices = nullptr;
+    size_t pb = (size_t)m->n_pad * n_planes * 4;
+    cudaError_t e = cudaSuccess;
+    if (pb) e = cudaMalloc(&m->planes, pb);
+    if (e == cudaSuccess && pb) e = cudaMemset(m->planes, 0, pb);
+    for (uint32_t j = 0; e == cudaSuccess && j < n_planes; ++j)
+        e = cudaMemcpy(m->planes + (size_t)j * m->n_pad, planes[j], (size_t)n_verts * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && n_indices) e = cudaMalloc(&m->indices, n_indices * 4);
+    if (e == cudaSuccess && n_indices) e = cudaMemcpy(m->indices, indices, n_indices * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        last_cuda_error() = e;
+        if (m->planes) cudaFree(m->planes);
+        if (m->indices) cudaFree(m->indices);
+        delete m;
+        return e == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA;
+    }
+    m->bytes = pb + n_indices * 4;
+    *out = m;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_mesh_free(sr_mesh* m) {
+    if (!m) return SR_EINVAL;
+    if (m->planes) cudaFree(m->planes);
+    if (m->indices) cudaFree(m->indices);
+    delete m;
+    return SR_OK;
+}
+
+extern "C" SR_API uint64_t sr_mesh_bytes(const sr_mesh* m) { return m ? m->bytes : 0; }
+
+extern "C" SR_API int sr_texture_upload(const uint32_t* rgba8, uint32_t w, uint32_t h, sr_texture** out) {
+    if (!out || !rgba8 || w == 0 || h == 0) return SR_EINVAL;
+    *out = nullptr;
+    sr_texture* t = new (std::nothrow) sr_texture();
+    if (!t) return SR_ENOMEM;
+    t->w = w;
+    t->h = h;
+    cudaError_t e = cudaMalloc(&t->data, (size_t)w * h * 4);
+    if (e == cudaSuccess) e = cudaMemcpy(t->data, rgba8, (size_t)w * h * 4, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        last_cuda_error() = e;
+        if (t->data) cudaFree(t->data);
+        delete t;
+        return e == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA;
+    }
+    *out = t;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_texture_free(sr_texture* t) {
+    if (!t) return SR_EINVAL;
+    if (t->data) cudaFree(t->data);
+    delete t;
+    return SR_OK;
+}
+
+// ================================================================ render
+namespace {
+
+int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
+    const sr_draw* d = &pd.d;
+    const sr_mesh* m = d->mesh;
+    cudaStream_t st = p->stream;
+    const uint32_t W = p->fb.width, H = p->fb.height;
+    DrawParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.W = W; P.H = H;
+    P.tile_w = d->tile_w; P.tile_h = d->tile_h;
+    P.ncols = W >= 2 ? (W - 1 + d->tile_w - 1) / d->tile_w : 0;
+    P.nrows = H >= 2 ? (H - 1 + d->tile_h - 1) / d->tile_h : 0;
+    P.n_verts = m->n_verts;
+    P.gen_base = m->n_pad;
+    P.n_in = (uint32_t)(m->n_indices / 3);
+    P.cull = d->cull;
+    P.vs = d->vs; P.fs = d->fs; P.blend = d->blend;
+    std::memcpy(P.vp, &d->viewport, sizeof(P.vp));
+    P.has_depth = p->depth != nullptr;
+    P.has_stencil = p->stencil != nullptr;
+    P.color_format = p->fb.color_format;
+    P.draw_id = draw_id;
+    if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; }
+    P.tex_filter = d->tex_filter; P.tex_edge = d->tex_edge;
+    // stencil mode (src/stencil.rs; a missing attachment behaves as `()`)
+    uint32_t test = pd.stencil_test, op = pd.stencil_op;
+    P.stencil_test = test; P.stencil_op = op; P.stencil_wrap = pd.stencil_wrap;
+    P.sref = P.has_stencil ? (d->stencil_ref & 0xffu) : 0u;
+    bool nothing = false;
+    uint32_t gate = 0;
+    if (!P.has_stencil) {
+        nothing = !stencil_test(test, 0, 0);
+    } else if (test == SR_STENCIL_NEVER) {
+        nothing = true;
+    } else if (op == SR_STENCIL_KEEP) {
+        gate = test != SR_STENCIL_ALWAYS;
+    } else if (test == SR_STENCIL_ALWAYS) {
+        P.stencil_active = 1;
+    } else {
+        P.mode_b = 1;
+        P.stencil_active = 1;
+    }
+    if (W < 2 || H < 2 || P.n_in == 0) nothing = true;   // no semantic tiles / no primitives
+    const bool ordered = P.mode_b || d->blend != BLEND_REPLACE;
+    const bool indexed = d->gs_mode == SR_GS_NONE;
+    P.keep_degenerate = P.stencil_active ? 1u : 0u;
+    if (ordered) { P.bin_w_log2 = 4; P.bin_h_log2 = 4; }
+    else { P.bin_w_log2 = 5; P.bin_h_log2 = 5; }
+    P.bins_x = (W + (1u << P.bin_w_log2) - 1) >> P.bin_w_log2;
+    P.bins_y = (H + (1u << P.bin_h_log2) - 1) >> P.bin_h_log2;
+    const uint32_t n_bins = P.bins_x * P.bins_y;
+
+    // per-draw statistics start from zero
+    SR_CK(cudaMemsetAsync(reinterpret_cast<char*>(p->flags) + FLAGS_STATS_OFFSET, 0,
+                          sizeof(DeviceFlags) - FLAGS_STATS_OFFSET, st));
+    if (nothing) return SR_OK;
+
+    // ---- capacities
+    if (!indexed) {
+        if (p->gen_tri_cap < 2ull * P.n_in + 4096) p->gen_tri_cap = 2ull * P.n_in + 4096;
+        if (p->gen_vert_cap < 2ull * P.n_in + 4096) p->gen_vert_cap = 2ull * P.n_in + 4096;
+        if (p->gen_tri_cap > (1ull << 30)) p->gen_tri_cap = 1ull << 30;
+        if (p->gen_vert_cap > (1ull << 30)) p->gen_vert_cap = 1ull << 30;
+    }
+    uint64_t n_raster_cap = indexed ? P.n_in : p->gen_tri_cap;
+    if (p->entry_cap < 2 * n_raster_cap + n_bins) p->entry_cap = 2 * n_raster_cap + n_bins;
+    if (p->entry_cap > 0xffffffffull) p->entry_cap = 0xffffffffull;
+    P.gen_tri_cap = (uint32_t)p->gen_tri_cap;
+    P.gen_vert_cap = (uint32_t)p->gen_vert_cap;
+    P.entry_cap = p->entry_cap;
+    P.n_raster_host = indexed ? P.n_in : 0;
+    int rc;
+    uint64_t vslots = (uint64_t)m->n_pad + (indexed ? 0 : p->gen_vert_cap);
+    if ((rc = p->scr4.ensure(vslots)) || (rc = p->vary.ensure(vslots * VSTRIDE))) return rc;
+    if (!indexed) {
+        if ((rc = p->clip4.ensure(m->n_pad)) || (rc = p->clip_counts.ensure(P.n_in)) ||
+            (rc = p->clip_offsets.ensure((size_t)P.n_in + 1)) || (rc = p->clip_tmp.ensure(scan_blocks(P.n_in) + 2)) ||
+            (rc = p->refs.ensure(3 * p->gen_tri_cap)))
+            return rc;
+    }
+    if ((rc = p->setup.ensure(4 * n_raster_cap)) || (rc = p->binrect.ensure(n_raster_cap)) ||
+        (rc = p->bin_counts.ensure(n_bins)) || (rc = p->bin_off.ensure((size_t)n_bins + 1)) ||
+        (rc = p->bin_cursor.ensure(n_bins)) || (rc = p->bin_tmp.ensure(scan_blocks(n_bins) + 2)) ||
+        (rc = p->entries.ensure(p->entry_cap)))
+        return rc;
+    StencilCountArgs S{nullptr, nullptr, nullptr};
+    if (P.stencil_active && !P.mode_b) {
+        size_t nd = (size_t)(W + 1) * (H + 1);
+        size_t nl = 3 * (size_t)(W + 1) + 3 * (size_t)(H + 1);
+        if ((rc = p->st_diff.ensure(nd)) || (rc = p->st_lines.ensure(nl)) || (rc = p->st_glob.ensure(16))) return rc;
+        SR_CK(cudaMemsetAsync(p->st_diff.p, 0, nd * 4, st));
+        SR_CK(cudaMemsetAsync(p->st_lines.p, 0, nl * 4, st));
+        SR_CK(cudaMemsetAsync(p->st_glob.p, 0, 16 * 8, st));
+        S = StencilCountArgs{p->st_diff.p, p->st_lines.p, p->st_glob.p};
+    }
+    VertexStore vs{p->clip4.p, p->scr4.p, p->vary.p, (uint32_t)vslots};
+
+    // ---- vertex stage
+    launch_vertex(P, pd.U, m, vs, !indexed, st);
+    // ---- geometry stage
+    const uint32_t* vidx = m->indices;
+    if (!indexed) {
+        launch_clip(P, m, vs, p->clip_counts.p, p->clip_offsets.p, p->clip_tmp.p, p->refs.p, p->flags, st);
+        vidx = p->refs.p;
+    }
+    // ---- setup + binning (+ stencil event counts)
+    launch_setup_bin(P, vidx, vs, p->setup.p, reinterpret_cast<uint32_t*>(p->binrect.p), p->bin_counts.p, p->bin_off.p,
+                     p->bin_cursor.p, p->entries.p, p->bin_tmp.p, S, p->flags, st);
+    // ---- raster
+    const uint32_t* tex = d->texture ? d->texture->data : nullptr;
+    launch_raster_any(ordered, P, pd.U, p->setup.p, p->bin_off.p, p->entries.p, vidx, p->vary.p, tex, p->color,
+                      p->depth, p->stencil, gate, p->flags, st);
+    if (P.stencil_active && !P.mode_b) launch_stencil_apply(P, S, p->stencil, p->flags, st);
+    SR_CK(cudaGetLastError());
+    return SR_OK;
+}
+
+}  // namespace
+
+extern "C" SR_API int sr_render(sr_pipeline* p, const sr_draw* d) {
+    if (!p || !d || !d->mesh) return SR_EINVAL;
+    const sr_mesh* m = d->mesh;
+    if (d->prim != SR_PRIM_TRIANGLE) return SR_EINVAL;
+    if (m->n_indices % 3 != 0) return SR_EINVAL;                          // mod.rs:148
+    if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT || d->blend < 0 || d->blend >= BLEND_COUNT)
+        return SR_EINVAL;
+    if (d->gs_mode != SR_GS_NONE && d->gs_mode != SR_GS_CLIP) return SR_EINVAL;
+    if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
+    if (d->cull > SR_CULL_COUNTER_CLOCKWISE) return SR_EINVAL;
+    if (m->n_planes < (uint32_t)vs_planes(d->vs)) return SR_EINVAL;
+    if (vs_nk(d->vs) < fs_min_varyings(d->fs)) return SR_EINVAL;
+    if (d->fs == FS_TEXTURED_BLINN_PHONG && !d->texture) return SR_EINVAL;
+    if (p->stencil && d->stencil_ref > 255) return SR_EINVAL;
+    PendingDraw pd;
+    pd.d = *d;
+    pd.U = p->U;
+    pd.stencil_test = p->stencil_test;
+    pd.stencil_op = p->stencil_op;
+    pd.stencil_wrap = p->stencil_wrap;
+    uint32_t id = (uint32_t)p->pending.size();
+    p->pending.push_back(pd);
+    int rc = enqueue_draw(p, pd, id);
+    if (rc != SR_OK) p->pending.pop_back();
+    return rc;
+}
+
+extern "C" SR_API int sr_sync(sr_pipeline* p) {
+    if (!p) return SR_EINVAL;
+    int status = SR_OK;
+    for (int attempt = 0; attempt < 8; ++attempt) {
+        SR_CK(cudaMemcpyAsync(p->hflags, p->flags, sizeof(DeviceFlags), cudaMemcpyDeviceToHost, p->stream));
+        cudaError_t e = cudaStreamSynchronize(p->stream);
+        if (e != cudaSuccess) { last_cuda_error() = e; return SR_ECUDA; }
+        DeviceFlags f = *p->hflags;
+        if (!f.poison) {
+            if (p->pending.empty()) break;
+            std::memset(&p->last_stats, 0, sizeof(p->last_stats));
+            p->last_stats.triangles_generated = f.triangles_generated;
+            p->last_stats.triangles_raster = f.triangles_raster;
+            p->last_stats.unsafe_triangles = f.unsafe;
+            p->last_stats.bin_entries = f.entries;
+            p->last_stats.fragments = f.fragments;
+            p->last_stats.nan_bbox = f.nan_bbox;
+            p->last_stats.overflow = f.overflow_bits;
+            const sr_mesh* m = p->pending.back().d.mesh;
+            p->last_stats.triangles_in = m ? m->n_indices / 3 : 0;
+            if (f.nan_total) status = SR_ENAN;
+            break;
+        }
+        // grow what overflowed and replay from the first poisoned draw
+        if (f.overflow_bits & OVF_GEN_TRIS) p->gen_tri_cap = f.need_gen_tris + f.need_gen_tris / 4 + 1024;
+        if (f.overflow_bits & OVF_GEN_VERTS) p->gen_vert_cap = f.need_gen_verts + f.need_gen_verts / 4 + 1024;
+        if (f.overflow_bits & OVF_ENTRIES) p->entry_cap = f.need_entries + f.need_entries / 4 + 1024;
+        if (f.overflow_bits & OVF_SORT) { status = SR_EOVERFLOW; }
+        uint32_t from = f.poison_draw;
+        DeviceFlags z;
+        std::memset(&z, 0, sizeof(z));
+        z.poison_draw = 0xffffffffu;
+        z.nan_total = f.nan_total;
+        SR_CK(cudaMemcpyAsync(p->flags, &z, sizeof(z), cudaMemcpyHostToDevice, p->stream));
+        SR_CK(cudaStreamSynchronize(p->stream));
+        if (status == SR_EOVERFLOW || from >= p->pending.size()) break;
+        for (uint32_t i = from; i < p->pending.size(); ++i) {
+            int rc = enqueue_draw(p, p->pending[i], i);
+            if (rc != SR_OK) { status = rc; break; }
+        }
+        if (status != SR_OK) break;
+    }
+    p->pending.clear();
+    DeviceFlags z;
+    std::memset(&z, 0, sizeof(z));
+    z.poison_draw = 0xffffffffu;
+    SR_CK(cudaMemcpyAsync(p->flags, &z, sizeof(z), cudaMemcpyHostToDevice, p->stream));
+    SR_CK(cudaStreamSynchronize(p->stream));
+    return status;
+}
+
+extern "C" SR_API int sr_get_stats(sr_pipeline* p, sr_stats* out) {
+    if (!p || !out) return SR_EINVAL;
+    *out = p->last_stats;
+    return SR_OK;
+}

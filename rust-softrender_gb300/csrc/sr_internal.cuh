@@ -1,0 +1,214 @@
+// sr_internal.cuh — types shared by the kernels and the C-ABI host runtime.
+//
+// Device data layout (all in HBM, owned by the pipeline / mesh objects):
+//   mesh planes      SoA f32, each plane padded to a multiple of 4 vertices
+//                    (16-byte aligned, read with 128-bit loads)
+//   mesh indices     u32, 3 per triangle
+//   vertex store     clip4[v]  AoS float4 clip-space position (clip GS only)
+//                    scr4[v]   AoS float4 screen position (x, y, z, 1/w)
+//                    vary[v]   AoS varyings, stride VSTRIDE floats
+//                    slots [0, n_verts) are mesh vertices, slots from
+//                    gen_base on are vertices created by the clipper
+//   raster triangles refs (3 u32 vertex-store slots per triangle) for
+//                    generated primitives, or the mesh indices directly
+//   setup records    4 float4 per raster triangle (edge terms, z, bbox)
+//   bins             per-bin entry lists of raster-triangle indices
+//   framebuffer      SoA planes: colour (RGBA f32 or RGBA8), f32 depth, u8 stencil
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "sr.h"
+#include "sr_shaders.h"
+
+namespace sr {
+
+constexpr int VSTRIDE = 12;        // varying floats per vertex (10 used at most)
+constexpr int MAX_PLANES = 8;      // attribute planes read by a vertex shader
+
+enum VsId { VS_MVP_POS_NRM = 0, VS_MVP_POS_NRM_UV = 1, VS_CLIP_COLOR = 2, VS_CLIP_RGBA8 = 3, VS_COUNT };
+enum FsId { FS_BLINN_PHONG_DIR = 0, FS_TEXTURED_BLINN_PHONG = 1, FS_VERTEX_COLOR = 2,
+            FS_ACES_LIGHTS = 3, FS_CONSTANT_COLOR = 4, FS_COUNT };
+enum BlendId { BLEND_REPLACE = 0, BLEND_OVER = 1, BLEND_COUNT };
+enum GsId { GS_CLIP = 0, GS_VERTEX_NORMALS = 1, GS_FACE_NORMALS = 2, GS_COUNT };
+
+__host__ __device__ inline int vs_planes(int vs) { return vs == VS_MVP_POS_NRM ? 6 : vs == VS_CLIP_RGBA8 ? 4 : 8; }
+__host__ __device__ inline int vs_nk(int vs) { return vs == VS_MVP_POS_NRM ? 8 : vs == VS_MVP_POS_NRM_UV ? 10 : 4; }
+
+// Device error / counter block (one per pipeline).  The first part persists
+// until sr_sync; the statistics part is zeroed at the start of every draw.
+struct DeviceFlags {
+    unsigned int poison;          // a stage overflowed: later framebuffer stages skip
+    unsigned int overflow_bits;   // OVF_* bits
+    unsigned int poison_draw;     // id of the first draw that overflowed (atomicMin)
+    unsigned int nan_total;       // primitives met with an all-NaN bbox since the last sync
+    unsigned long long need_gen_tris;
+    unsigned long long need_gen_verts;
+    unsigned long long need_entries;
+    // ---- per-draw statistics (sr_stats) and device-side sizes
+    unsigned long long triangles_generated;
+    unsigned long long triangles_raster;
+    unsigned long long unsafe;
+    unsigned long long entries;
+    unsigned long long fragments;
+    unsigned long long n_gen_tris;     // raster triangles produced by the geometry stage
+    unsigned long long n_gen_verts;
+    unsigned int nan_bbox;
+    unsigned int pad;
+};
+constexpr size_t FLAGS_STATS_OFFSET = 40;
+static_assert(offsetof(DeviceFlags, triangles_generated) == FLAGS_STATS_OFFSET, "DeviceFlags layout");
+
+enum { OVF_GEN_TRIS = 1, OVF_GEN_VERTS = 2, OVF_ENTRIES = 4, OVF_SORT = 8 };
+
+// Per-draw parameters passed by value to the kernels (constant bank).
+struct DrawParams {
+    uint32_t W, H;
+    uint32_t tile_w, tile_h;
+    uint32_t ncols, nrows;        // semantic tile grid
+    uint32_t bin_w_log2, bin_h_log2;
+    uint32_t bins_x, bins_y;
+    uint32_t n_verts, gen_base;   // vertex-store slot of the first generated vertex
+    uint32_t n_in;                // input primitives
+    uint32_t n_raster_host;       // raster primitives when known on the host (0: read flags->n_gen_tris)
+    uint32_t cull;
+    uint32_t stencil_test, stencil_op, stencil_wrap, sref;
+    uint32_t has_depth, has_stencil, color_format;
+    uint32_t keep_degenerate;     // keep exactly-degenerate clip outputs (stencil events)
+    uint32_t gen_tri_cap, gen_vert_cap;
+    uint64_t entry_cap;
+    float vp[6];
+    int vs, fs, blend;
+    uint32_t tex_w, tex_h, tex_filter, tex_edge;
+    uint32_t mode_b;              // exhaustive raster (stencil events gate fragments)
+    uint32_t stencil_active;      // stencil plane changes during this draw
+    uint32_t draw_id;             // sequence number of the draw since the last sync
+};
+
+// Setup record of a raster triangle (64 bytes):
+//   r0 = {A = y2-y3, B = x3-x2, C = y3-y1, D = x1-x3}
+//   r1 = {x3, y3, det, z1}
+//   r2 = {z2, z3, flags (bits), unused}
+//   r3 = {ix0, iy0, ix1, iy1} integer bbox (floor), as int bits
+enum { REC_UNSAFE = 1u, REC_RASTER = 2u };
+
+struct Workspace;  // host side, defined in sr_api.cu
+
+// Stencil event counters (see sr_stencil.cu)
+struct StencilCountArgs {
+    int* diff2d;                 // (W+1) x (H+1) 2D difference array
+    int* lines;                  // CX, CXa, CXb (W+1 each), CY, CYl, CYr (H+1 each)
+    unsigned long long* globals; // N, L, R, A, B, LA, LB, RA, RB
+};
+
+// ------------------------------------------------------------ device helpers
+__device__ __forceinline__ uint32_t zkey(float z) {
+    uint32_t u = __float_as_uint(z);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float zkey_inv(uint32_t k) {
+    uint32_t u = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    return __uint_as_float(u);
+}
+// floor(v) saturated to [lo, hi] as int; v must not be NaN
+__device__ __forceinline__ int floor_sat(float v, int lo, int hi) {
+    if (!(v >= (float)lo)) return lo;      // also -inf
+    if (v >= (float)hi) return hi;
+    return (int)floorf(v);
+}
+
+// StencilTest::test(value, mask) and StencilOp::op (src/stencil.rs:114-164)
+__host__ __device__ __forceinline__ bool stencil_test(uint32_t test, uint32_t value, uint32_t mask) {
+    switch (test) {
+    case 0: return true;
+    case 1: return false;
+    case 2: return mask < value;
+    case 3: return mask > value;
+    case 4: return mask <= value;
+    case 5: return mask >= value;
+    case 6: return mask == value;
+    default: return mask != value;
+    }
+}
+__host__ __device__ __forceinline__ uint32_t stencil_op(uint32_t op, uint32_t wrap, uint32_t value, uint32_t mask) {
+    switch (op) {
+    case 0: return value;
+    case 1: return (~value) & 0xffu;
+    case 2: return 0;
+    case 3: return mask;
+    case 4: return wrap ? ((value + 1) & 0xffu) : (value == 255 ? 255 : value + 1);
+    default: return wrap ? ((value - 1) & 0xffu) : (value == 0 ? 0 : value - 1);
+    }
+}
+
+// Semantic tile geometry (fragment.rs:188-216): tile column C spans
+// [C*tw, min((C+1)*tw, W-1)] inclusive; adjacent tiles share a column.
+struct TileSpan {
+    int first;   // first tile index containing the pixel
+    int count;   // 1 or 2
+};
+__device__ __forceinline__ TileSpan tiles_of(uint32_t p, uint32_t t, uint32_t n, uint32_t last) {
+    TileSpan s;
+    if (p > 0 && p < last && (p % t) == 0) { s.first = (int)(p / t) - 1; s.count = 2; }
+    else { uint32_t c = p / t; if (c > n - 1) c = n - 1; s.first = (int)c; s.count = 1; }
+    return s;
+}
+// Is coordinate p inside the projection of [i0, i1] clamped to tile index c?
+// (clamp_as_int of triangle.rs:66-78, with floor-rounded bbox ends)
+__device__ __forceinline__ bool clamp_axis(int i0, int i1, uint32_t p, uint32_t c, uint32_t t, uint32_t last) {
+    uint32_t lo = c * t;
+    uint32_t hi = min((c + 1) * t, last);
+    int pi = (int)p;
+    if (p == lo) return i0 <= pi;
+    if (p == hi) return i1 >= pi;
+    return i0 <= pi && pi <= i1;
+}
+
+}  // namespace sr
+
+// Opaque handles of the C ABI
+struct sr_mesh {
+    float* planes;        // n_planes planes of n_pad floats
+    uint32_t n_planes;
+    uint32_t n_verts;
+    uint32_t n_pad;
+    uint32_t* indices;
+    uint64_t n_indices;
+    uint64_t bytes;
+};
+
+struct sr_texture {
+    uint32_t* data;
+    uint32_t w, h;
+};
+
+// ---------------------------------------------------------------- launches
+// Kernel launchers implemented in the .cu files (host-callable).
+namespace sr {
+
+struct VertexStore {
+    float4* clip4;
+    float4* scr4;
+    float* vary;
+    uint32_t cap;
+};
+
+void launch_vertex(const DrawParams& P, const sr_uniforms& U, const sr_mesh* m, VertexStore vs,
+                   bool write_clip, cudaStream_t st);
+void launch_clip(const DrawParams& P, const sr_mesh* m, VertexStore vs, unsigned long long* counts,
+                 unsigned long long* offsets, unsigned long long* scan_tmp, uint32_t* refs,
+                 DeviceFlags* flags, cudaStream_t st);
+void launch_setup_bin(const DrawParams& P, const uint32_t* vidx, VertexStore vs, float4* setup,
+                      uint32_t* binrect, uint32_t* bin_counts, uint32_t* bin_off, uint32_t* bin_cursor,
+                      uint32_t* entries, uint32_t* scan_tmp, const StencilCountArgs& S,
+                      DeviceFlags* flags, cudaStream_t st);
+void launch_raster_any(bool ordered, const DrawParams& P, const sr_uniforms& U, const float4* setup,
+                       const uint32_t* bin_off, const uint32_t* entries, const uint32_t* vidx,
+                       const float* vary, const uint32_t* tex, void* color, float* depth,
+                       uint8_t* stencil, uint32_t gate, DeviceFlags* flags, cudaStream_t st);
+void launch_stencil_apply(const DrawParams& P, const StencilCountArgs& S, uint8_t* stencil,
+                          DeviceFlags* flags, cudaStream_t st);
+
+}  // namespace sr

@@ -1,0 +1,345 @@
+"""softrender — Python host mirror of softrender's Pipeline builder API over
+the GB300 C ABI (include/sr.h).
+
+The reference chain (src/pipeline/mod.rs, stages/{vertex,geometry,fragment}.rs)
+
+    let mut pipeline = Pipeline::from_framebuffer(framebuffer, uniforms);
+    pipeline.render_mesh(Triangle, mesh, Some(stencil))
+            .run(vertex_shader)              // or .run_to_fragment(viewport, vs)
+            .clip_primitives()
+            .finish(viewport)
+            .with_blend(blend)
+            .run(fragment_shader);
+
+reads here as
+
+    pipeline = Pipeline.from_framebuffer(Framebuffer(w, h, RGBA8), uniforms)
+    (pipeline.render_mesh(Triangle, mesh, stencil)
+             .run("mvp_pos_nrm_uv")
+             .clip_primitives()
+             .finish(viewport)
+             .with_blend("over")
+             .run("textured_blinn_phong"))
+
+with shader stages named device functions compiled into the library.  Every
+call goes through the CUDA library; there is no CPU path.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import _abi as A
+from ._lib import SoftrenderError, check, lib
+
+__all__ = ["Framebuffer", "Pipeline", "Mesh", "Texture", "Viewport", "Point", "Line", "Triangle",
+           "SoftrenderError", "render_scene", "shader_id"]
+
+Point, Line, Triangle = A.SR_PRIM_POINT, A.SR_PRIM_LINE, A.SR_PRIM_TRIANGLE
+
+
+def shader_id(name, stage):
+    i = C.c_int()
+    check(lib().sr_shader_lookup(name.encode(), stage, C.byref(i)), "sr_shader_lookup(%s)" % name)
+    return i.value
+
+
+class Viewport:
+    """Viewport<f32> (src/geometry/clipvertex.rs:28-57)."""
+
+    def __init__(self, x, y, width, height, near=0.0, far=1.0):
+        self.x, self.y, self.width, self.height, self.near, self.far = x, y, width, height, near, far
+
+    @classmethod
+    def from_dimensions(cls, width, height, near=0.0, far=1.0):
+        return cls(0.0, 0.0, float(width), float(height), near, far)
+
+    def c(self):
+        return A.SrViewport(self.x, self.y, self.width, self.height, self.near, self.far)
+
+
+class Framebuffer:
+    """RenderBuffer<ColorDepthStencilAttachments<C, D, S>> description."""
+
+    def __init__(self, width, height, color_format=A.SR_COLOR_RGBA32F, depth=True, stencil=False):
+        self.width, self.height = width, height
+        self.color_format, self.depth, self.stencil = color_format, depth, stencil
+
+
+class Mesh:
+    """Mesh<V> (src/mesh.rs:38-64) uploaded as SoA f32 planes + u32 indices."""
+
+    def __init__(self, planes, indices):
+        planes = [np.ascontiguousarray(p, dtype=np.float32) for p in planes]
+        idx = np.ascontiguousarray(indices, dtype=np.uint32)
+        n = planes[0].shape[0] if planes else 0
+        arr = (C.c_void_p * max(1, len(planes)))(*[p.ctypes.data for p in planes])
+        h = C.c_void_p()
+        check(lib().sr_mesh_upload(arr, len(planes), n, idx.ctypes.data if idx.size else None, idx.size,
+                                   C.byref(h)), "sr_mesh_upload")
+        self.handle = h
+        self.n_verts = n
+        self.n_indices = int(idx.size)
+
+    @property
+    def nbytes(self):
+        return int(lib().sr_mesh_bytes(self.handle))
+
+    def free(self):
+        if self.handle:
+            lib().sr_mesh_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Texture:
+    def __init__(self, rgba8):
+        t = np.ascontiguousarray(rgba8, dtype=np.uint32)
+        h = C.c_void_p()
+        check(lib().sr_texture_upload(t.ctypes.data, t.shape[1], t.shape[0], C.byref(h)), "sr_texture_upload")
+        self.handle = h
+        self.width, self.height = t.shape[1], t.shape[0]
+
+    def free(self):
+        if self.handle:
+            lib().sr_texture_free(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Pipeline:
+    """Pipeline<U, F, S> (src/pipeline/mod.rs:60-155)."""
+
+    def __init__(self, framebuffer, uniforms=None):
+        self.framebuffer = framebuffer
+        desc = A.SrFbDesc(framebuffer.width, framebuffer.height, framebuffer.color_format,
+                          1 if framebuffer.depth else 0, 1 if framebuffer.stencil else 0)
+        h = C.c_void_p()
+        u = C.byref(uniforms) if uniforms is not None else None
+        check(lib().sr_pipeline_create(C.byref(desc), u, C.sizeof(A.SrUniforms) if uniforms is not None else 0,
+                                       C.byref(h)), "sr_pipeline_create")
+        self.handle = h
+        self._uniforms = uniforms
+        self._keep = []
+
+    @classmethod
+    def from_framebuffer(cls, framebuffer, uniforms=None):
+        return cls(framebuffer, uniforms)
+
+    # PipelineObject accessors
+    def set_uniforms(self, uniforms):
+        check(lib().sr_pipeline_set_uniforms(self.handle, C.byref(uniforms), C.sizeof(A.SrUniforms)),
+              "sr_pipeline_set_uniforms")
+        self._uniforms = uniforms
+
+    def set_stencil(self, test, op, wrap=True):
+        """stencil_config_mut() = GenericStencilConfig { op, test } (src/stencil.rs:182-199)."""
+        check(lib().sr_pipeline_set_stencil(self.handle, test, op, 1 if wrap else 0), "sr_pipeline_set_stencil")
+
+    def set_stream(self, stream_ptr):
+        check(lib().sr_pipeline_set_stream(self.handle, C.c_void_p(stream_ptr) if stream_ptr else None),
+              "sr_pipeline_set_stream")
+
+    def clear(self, color):
+        """Framebuffer::clear: colour, depth <- f32::MIN, stencil <- 0."""
+        if self.framebuffer.color_format == A.SR_COLOR_RGBA8:
+            buf = (C.c_uint8 * 4)(*[int(c) for c in color])
+        else:
+            buf = (C.c_float * 4)(*[float(c) for c in color])
+        check(lib().sr_framebuffer_clear(self.handle, buf), "sr_framebuffer_clear")
+
+    def write(self, color=None, depth=None, stencil=None):
+        c = np.ascontiguousarray(color) if color is not None else None
+        d = np.ascontiguousarray(depth, dtype=np.float32) if depth is not None else None
+        s = np.ascontiguousarray(stencil, dtype=np.uint8) if stencil is not None else None
+        check(lib().sr_framebuffer_write(self.handle, c.ctypes.data if c is not None else None,
+                                         d.ctypes.data if d is not None else None,
+                                         s.ctypes.data if s is not None else None), "sr_framebuffer_write")
+
+    def read(self):
+        """Returns (color, depth, stencil) host arrays (None for absent planes)."""
+        fb = self.framebuffer
+        h, w = fb.height, fb.width
+        color = None
+        if fb.color_format == A.SR_COLOR_RGBA32F:
+            color = np.empty((h, w, 4), dtype=np.float32)
+        elif fb.color_format == A.SR_COLOR_RGBA8:
+            color = np.empty((h, w), dtype=np.uint32)
+        depth = np.empty((h, w), dtype=np.float32) if fb.depth else None
+        stencil = np.empty((h, w), dtype=np.uint8) if fb.stencil else None
+        st = lib().sr_framebuffer_read(self.handle, color.ctypes.data if color is not None else None,
+                                       depth.ctypes.data if depth is not None else None,
+                                       stencil.ctypes.data if stencil is not None else None)
+        if st not in (A.SR_OK, A.SR_ENAN):
+            raise SoftrenderError(st, "sr_framebuffer_read")
+        return color, depth, stencil
+
+    def sync(self):
+        return lib().sr_sync(self.handle)
+
+    def stats(self):
+        s = A.SrStats()
+        check(lib().sr_get_stats(self.handle, C.byref(s)), "sr_get_stats")
+        return {f: getattr(s, f) for f, _ in A.SrStats._fields_}
+
+    def render_mesh(self, primitive, mesh, stencil=None):
+        """Pipeline::render_mesh (mod.rs:146-155) -> VertexShader."""
+        if mesh.n_indices % primitive != 0:
+            raise SoftrenderError(A.SR_EINVAL, "render_mesh: indices.len() % num_vertices != 0")
+        d = A.SrDraw()
+        lib().sr_draw_init(C.byref(d))
+        d.mesh = mesh.handle
+        d.prim = primitive
+        d.stencil_ref = 0 if stencil is None else int(stencil)
+        return VertexShader(self, d, [mesh])
+
+    def destroy(self):
+        if self.handle:
+            lib().sr_pipeline_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+
+class VertexShader:
+    """stages/vertex.rs: run(vs) -> GeometryShader, run_to_fragment(vp, vs) -> FragmentShader."""
+
+    def __init__(self, pipeline, draw, keep):
+        self.pipeline, self.draw, self.keep = pipeline, draw, keep
+
+    def run(self, vs):
+        self.draw.vs = shader_id(vs, A.SR_STAGE_VERTEX)
+        return GeometryShader(self.pipeline, self.draw, self.keep)
+
+    def run_to_fragment(self, viewport, vs):
+        self.draw.vs = shader_id(vs, A.SR_STAGE_VERTEX)
+        self.draw.gs_mode = A.SR_GS_NONE
+        self.draw.viewport = viewport.c()
+        return FragmentShader(self.pipeline, self.draw, self.keep)
+
+
+class GeometryShader:
+    """stages/geometry.rs: clip_primitives(), run(gs), finish(viewport)."""
+
+    def __init__(self, pipeline, draw, keep):
+        self.pipeline, self.draw, self.keep = pipeline, draw, keep
+
+    def clip_primitives(self):
+        self.draw.gs_mode = A.SR_GS_CLIP
+        self.draw.gs = shader_id("clip", A.SR_STAGE_GEOMETRY)
+        return self
+
+    def run(self, gs):
+        self.draw.gs_mode = A.SR_GS_NAMED
+        self.draw.gs = shader_id(gs, A.SR_STAGE_GEOMETRY)
+        return self
+
+    def finish(self, viewport):
+        self.draw.viewport = viewport.c()
+        return FragmentShader(self.pipeline, self.draw, self.keep)
+
+
+class FragmentShader:
+    """stages/fragment.rs: with_blend, cull_faces, antialiased_lines, tile_size, run."""
+
+    def __init__(self, pipeline, draw, keep):
+        self.pipeline, self.draw, self.keep = pipeline, draw, keep
+
+    def with_blend(self, blend):
+        self.draw.blend = shader_id(blend, A.SR_STAGE_BLEND)
+        return self
+
+    def with_default_blend(self):
+        self.draw.blend = 0
+        return self
+
+    def cull_faces(self, cull):
+        self.draw.cull = cull
+        return self
+
+    with_faces_culled = cull_faces
+
+    def antialiased_lines(self, enable):
+        self.draw.aa_lines = 1 if enable else 0
+        return self
+
+    with_antialiased_lines = antialiased_lines
+
+    def tile_size(self, w, h):
+        self.draw.tile_w, self.draw.tile_h = w, h
+        return self
+
+    with_tile_size = tile_size
+
+    def with_texture(self, texture, filter=A.SR_SAMPLE_BILINEAR, edge=A.SR_SAMPLE_CLAMP):
+        self.draw.texture = texture.handle
+        self.draw.tex_filter, self.draw.tex_edge = filter, edge
+        self.keep.append(texture)
+        return self
+
+    def run(self, fs):
+        self.draw.fs = shader_id(fs, A.SR_STAGE_FRAGMENT)
+        check(lib().sr_render(self.pipeline.handle, C.byref(self.draw)), "sr_render")
+        self.pipeline._keep.extend(self.keep)
+        return self.pipeline
+
+
+def prepare_scene(scene):
+    """(pipeline, mesh, texture) for a softrender.scenes.Scene, framebuffer cleared."""
+    fb = Framebuffer(scene.width, scene.height, scene.color_format, scene.depth, scene.stencil)
+    pl = Pipeline.from_framebuffer(fb, scene.uniforms)
+    pl.set_stencil(scene.stencil_test, scene.stencil_op, scene.stencil_wrap)
+    if scene.color_format == A.SR_COLOR_RGBA8:
+        pl.clear(list(scene.clear_bytes()))
+    else:
+        pl.clear(scene.clear_color)
+    mesh = Mesh(scene.planes, scene.indices)
+    tex = Texture(scene.texture) if scene.texture is not None else None
+    return pl, mesh, tex
+
+
+def submit_scene(pl, mesh, tex, scene):
+    """Enqueues the draw of `scene` through the builder chain."""
+    vp = Viewport(*scene.viewport)
+    vs = pl.render_mesh(scene.prim, mesh, scene.stencil_ref if scene.stencil else None)
+    if scene.gs_mode == A.SR_GS_NONE:
+        fs = vs.run_to_fragment(vp, scene.vs)
+    else:
+        gs = vs.run(scene.vs)
+        gs = gs.clip_primitives() if scene.gs_mode == A.SR_GS_CLIP else gs.run(scene.gs)
+        fs = gs.finish(vp)
+    fs = fs.with_blend(scene.blend).cull_faces(scene.cull).tile_size(*scene.tile)
+    fs = fs.antialiased_lines(scene.aa_lines)
+    if tex is not None:
+        fs = fs.with_texture(tex, scene.tex_filter, scene.tex_edge)
+    fs.run(scene.fs)
+
+
+def render_scene(scene, initial=None):
+    """Renders one Scene on the GPU; returns (color, depth, stencil, stats, status).
+    `initial` optionally gives (color, depth, stencil) host planes to start from."""
+    pl, mesh, tex = prepare_scene(scene)
+    if initial is not None:
+        pl.write(*initial)
+    submit_scene(pl, mesh, tex, scene)
+    status = pl.sync()
+    color, depth, stencil = pl.read()
+    stats = pl.stats()
+    pl.destroy()
+    mesh.free()
+    if tex is not None:
+        tex.free()
+    return color, depth, stencil, stats, status

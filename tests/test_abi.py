@@ -1,0 +1,88 @@
+"""The C-ABI library: loads, exports exactly what include/sr.h declares, and
+its host-side argument checking (no GPU work is launched here)."""
+import ctypes as C
+import os
+import re
+
+import pytest
+
+import softrender._lib as L
+from softrender import _abi as A
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    for f in os.listdir(os.path.join(ROOT, "include")):
+        if not f.endswith(".h"):
+            continue
+        txt = open(os.path.join(ROOT, "include", f)).read()
+        names |= set(re.findall(r"SR_API\s+[\w\s\*]+?\b(sr_\w+)\s*\(", txt))
+    return names
+
+
+def test_header_declares_entry_points():
+    names = declared_symbols()
+    for must in ("sr_pipeline_create", "sr_render", "sr_sync", "sr_mesh_upload", "sr_shader_lookup",
+                 "sr_framebuffer_read", "sr_texture_upload"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = L.lib()
+    missing = [n for n in sorted(declared_symbols()) if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_python_binding_covers_header(built_lib):
+    assert declared_symbols() <= set(L.SIGNATURES), declared_symbols() - set(L.SIGNATURES)
+
+
+def test_only_declared_symbols_are_exported(built_lib):
+    import subprocess
+    out = subprocess.run(["nm", "-D", "--defined-only", built_lib], capture_output=True, text=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if " T " in l and l.split()[-1].startswith("sr_")}
+    assert exported == declared_symbols(), exported ^ declared_symbols()
+
+
+def test_shader_registry(built_lib):
+    lib = L.lib()
+    i = C.c_int()
+    for name, stage in [("mvp_pos_nrm", A.SR_STAGE_VERTEX), ("mvp_pos_nrm_uv", A.SR_STAGE_VERTEX),
+                        ("clip_rgba8", A.SR_STAGE_VERTEX), ("clip", A.SR_STAGE_GEOMETRY),
+                        ("blinn_phong_dir", A.SR_STAGE_FRAGMENT), ("textured_blinn_phong", A.SR_STAGE_FRAGMENT),
+                        ("over", A.SR_STAGE_BLEND), ("replace", A.SR_STAGE_BLEND)]:
+        assert lib.sr_shader_lookup(name.encode(), stage, C.byref(i)) == A.SR_OK
+    assert lib.sr_shader_lookup(b"no_such_shader", A.SR_STAGE_FRAGMENT, C.byref(i)) == A.SR_ENOTFOUND
+    assert lib.sr_shader_lookup(b"over", A.SR_STAGE_VERTEX, C.byref(i)) == A.SR_ENOTFOUND
+
+
+def test_status_strings_and_version(built_lib):
+    lib = L.lib()
+    assert lib.sr_status_string(A.SR_ENAN) == b"SR_ENAN"
+    assert lib.sr_version().startswith(b"softrender-gb300")
+
+
+def test_draw_defaults(built_lib):
+    d = A.SrDraw()
+    L.lib().sr_draw_init(C.byref(d))
+    assert (d.tile_w, d.tile_h) == (128, 128)          # DEFAULT_TILE_SIZE (fragment.rs:29)
+    assert d.prim == A.SR_PRIM_TRIANGLE and d.blend == 0 and d.cull == A.SR_CULL_NONE
+
+
+def test_invalid_arguments_rejected_on_host(built_lib):
+    lib = L.lib()
+    h = C.c_void_p()
+    bad = A.SrFbDesc(0, 10, A.SR_COLOR_RGBA8, 1, 0)         # mod.rs:129: non-zero width
+    assert lib.sr_pipeline_create(C.byref(bad), None, 0, C.byref(h)) == A.SR_EINVAL
+    bad = A.SrFbDesc(10, 0, A.SR_COLOR_RGBA8, 1, 0)
+    assert lib.sr_pipeline_create(C.byref(bad), None, 0, C.byref(h)) == A.SR_EINVAL
+    assert lib.sr_render(None, None) == A.SR_EINVAL
+    assert lib.sr_shader_lookup(None, 0, C.byref(C.c_int())) == A.SR_EINVAL
+    # indices out of range are rejected before any device work
+    import numpy as np
+    plane = np.zeros(3, dtype=np.float32)
+    idx = np.array([0, 1, 5], dtype=np.uint32)
+    arr = (C.c_void_p * 1)(plane.ctypes.data)
+    assert lib.sr_mesh_upload(arr, 1, 3, idx.ctypes.data, 3, C.byref(h)) == A.SR_EINVAL

@@ -1,0 +1,123 @@
+"""GPU (through the C ABI) versus the CPU oracle on seeded inputs.
+
+Coverage, depth, stencil and RGBA8 colour must match bit for bit; RGBA f32
+colour too (tolerance 0 ULP: the shader arithmetic is the same FP32
+operation sequence on both sides, compiled without FMA contraction).
+"""
+import numpy as np
+import pytest
+
+import softrender as sr
+from softrender import _abi as A
+from softrender import scenes
+from util import compare_frame
+
+pytestmark = pytest.mark.gpu
+
+COLOR_ULPS = 0
+
+
+def run_both(scene, oracle_mod, initial=None):
+    gpu = sr.render_scene(scene, initial=initial)
+    fb = oracle_mod.framebuffer_for(scene)
+    if initial is not None:
+        c, d, s = initial
+        if c is not None:
+            fb.color[...] = c
+        if d is not None:
+            fb.depth[...] = d
+        if s is not None:
+            fb.stencil[...] = s
+    fb, ostats, ostatus = oracle_mod.render(scene, fb)
+    return gpu, fb, ostats, ostatus
+
+
+def check(scene, oracle_mod, initial=None):
+    (color, depth, stencil, stats, status), fb, ostats, ostatus = run_both(scene, oracle_mod, initial)
+    compare_frame((color, depth, stencil), fb, COLOR_ULPS)
+    assert stats["fragments"] == ostats["fragments"], (stats, ostats)
+    assert (status == A.SR_ENAN) == (ostatus == 7)
+    return stats, ostats
+
+
+def test_icosphere_small(built_lib, oracle_mod):
+    check(scenes.icosphere_scene(256, 256), oracle_mod)
+
+
+def test_icosphere_1024(built_lib, oracle_mod):
+    check(scenes.icosphere_scene(1024, 1024), oracle_mod)
+
+
+def test_icosphere_rgba8_nonsquare(built_lib, oracle_mod):
+    sc = scenes.icosphere_scene(300, 170, color_format=A.SR_COLOR_RGBA8)
+    check(sc, oracle_mod)
+
+
+@pytest.mark.parametrize("tile", [(128, 128), (16, 16), (7, 13), (1, 1), (1000, 3)])
+def test_tile_sizes(built_lib, oracle_mod, tile):
+    sc = scenes.icosphere_scene(160, 120, tile=tile)
+    check(sc, oracle_mod)
+
+
+@pytest.mark.parametrize("cull", [A.SR_CULL_CLOCKWISE, A.SR_CULL_COUNTER_CLOCKWISE])
+def test_culling(built_lib, oracle_mod, cull):
+    check(scenes.icosphere_scene(200, 200, cull=cull), oracle_mod)
+
+
+def test_clip_gs_icosphere(built_lib, oracle_mod):
+    sc = scenes.icosphere_scene(256, 256, gs_mode=A.SR_GS_CLIP)
+    check(sc, oracle_mod)
+
+
+def test_grid_sphere_clip_textured(built_lib, oracle_mod):
+    sc = scenes.grid_sphere_scene(width=384, height=216, n_lat=32, n_lon=64, tex_size=64)
+    stats, _ = check(sc, oracle_mod)
+    assert stats["triangles_generated"] > 0
+
+
+# ----------------------------------------------------------- ordered paths
+@pytest.mark.parametrize("wrap", [1, 0])
+def test_stress_blend_stencil_increment(built_lib, oracle_mod, wrap):
+    """Tiny triangles + large alpha triangles, over-blend in submission order,
+    stencil Always/Increment (wrap and saturate) with 32x24 semantic tiles."""
+    sc = scenes.stress_scene(n_tiny=3000, n_large=24, size=160, wrap=wrap, tile=(32, 24))
+    check(sc, oracle_mod)
+
+
+def test_stress_saturates(built_lib, oracle_mod):
+    """Enough events on tile edges to saturate / wrap the u8 stencil."""
+    sc = scenes.stress_scene(n_tiny=2000, n_large=300, size=96, wrap=0, tile=(8, 8))
+    check(sc, oracle_mod)
+
+
+@pytest.mark.parametrize("test_op", [(A.SR_STENCIL_LESS_THAN, A.SR_STENCIL_KEEP),
+                                     (A.SR_STENCIL_EQUAL, A.SR_STENCIL_KEEP),
+                                     (A.SR_STENCIL_NEVER, A.SR_STENCIL_INCREMENT),
+                                     (A.SR_STENCIL_ALWAYS, A.SR_STENCIL_REPLACE),
+                                     (A.SR_STENCIL_ALWAYS, A.SR_STENCIL_INVERT),
+                                     (A.SR_STENCIL_ALWAYS, A.SR_STENCIL_DECREMENT)])
+def test_stencil_modes_opaque(built_lib, oracle_mod, test_op):
+    sc = scenes.icosphere_scene(150, 110, stencil=True, tile=(32, 32), stencil_ref=3,
+                                stencil_test=test_op[0], stencil_op=test_op[1])
+    rng = np.random.default_rng(11)
+    st0 = rng.integers(0, 7, (sc.height, sc.width)).astype(np.uint8)
+    check(sc, oracle_mod, initial=(None, None, st0))
+
+
+@pytest.mark.parametrize("test_op", [(A.SR_STENCIL_LESS_THAN, A.SR_STENCIL_INCREMENT),
+                                     (A.SR_STENCIL_GREATER_THAN_EQ, A.SR_STENCIL_ZERO),
+                                     (A.SR_STENCIL_NOT_EQUAL, A.SR_STENCIL_REPLACE)])
+def test_stencil_exhaustive(built_lib, oracle_mod, test_op):
+    """Tests whose outcome changes with the stencil value: the exhaustive path."""
+    sc = scenes.icosphere_scene(96, 80, stencil=True, tile=(24, 20), stencil_ref=2, subdiv=2,
+                                stencil_test=test_op[0], stencil_op=test_op[1])
+    rng = np.random.default_rng(12)
+    st0 = rng.integers(0, 5, (sc.height, sc.width)).astype(np.uint8)
+    check(sc, oracle_mod, initial=(None, None, st0))
+
+
+def test_blend_over_f32(built_lib, oracle_mod):
+    sc = scenes.stress_scene(n_tiny=1500, n_large=20, size=128, tile=(48, 40))
+    sc.color_format = A.SR_COLOR_RGBA32F
+    sc.stencil = False
+    check(sc, oracle_mod)

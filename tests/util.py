@@ -1,0 +1,53 @@
+"""Comparison helpers shared by the parity tests."""
+import numpy as np
+
+
+def ulp_diff_f32(a, b):
+    """Per-element distance in units in the last place between two f32 arrays
+    (NaN == NaN counts as 0; mixed NaN as a huge distance)."""
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    b = np.ascontiguousarray(b, dtype=np.float32)
+    ia = a.view(np.int32).astype(np.int64)
+    ib = b.view(np.int32).astype(np.int64)
+    ia = np.where(ia < 0, -(ia & 0x7fffffff), ia)
+    ib = np.where(ib < 0, -(ib & 0x7fffffff), ib)
+    d = np.abs(ia - ib)
+    na, nb = np.isnan(a), np.isnan(b)
+    d = np.where(na & nb, 0, d)
+    d = np.where(na ^ nb, 1 << 40, d)
+    return d
+
+
+def assert_bitexact(name, got, want):
+    if got is None and want is None:
+        return
+    got = np.asarray(got)
+    want = np.asarray(want)
+    assert got.shape == want.shape, (name, got.shape, want.shape)
+    gb = got.view(np.uint8) if got.dtype != np.uint8 else got
+    wb = want.view(np.uint8) if want.dtype != np.uint8 else want
+    if not np.array_equal(gb, wb):
+        if got.dtype == np.float32:
+            bad = np.argwhere(ulp_diff_f32(got, want) != 0)
+        else:
+            bad = np.argwhere(got != want)
+        first = tuple(bad[0]) if len(bad) else None
+        raise AssertionError("%s differs at %d positions; first %s got %r want %r" % (
+            name, len(bad), first, got[first] if first else None, want[first] if first else None))
+
+
+def compare_frame(gpu, ref, color_ulps=0):
+    """gpu = (color, depth, stencil) from the library, ref = oracle Framebuffer.
+    Depth, stencil and RGBA8 colour must match bit for bit; RGBA f32 colour
+    within `color_ulps` ULP (0: bit-exact)."""
+    color, depth, stencil = gpu
+    if ref.color is not None:
+        if ref.color.dtype == np.float32 and color_ulps:
+            d = ulp_diff_f32(color, ref.color)
+            assert d.max() <= color_ulps, "colour differs by %d ULP" % d.max()
+        else:
+            assert_bitexact("color", color, ref.color)
+    if ref.depth is not None:
+        assert_bitexact("depth", depth, ref.depth)
+    if ref.stencil is not None:
+        assert_bitexact("stencil", stencil, ref.stencil)
