@@ -1,0 +1,380 @@
+"""Benchmark of the rendering hot path on one GB300 (or N replicas).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Workload: the large plain-pipeline frame -- a 1,048,576-triangle displaced
+grid-sphere (3-octave value noise, 5%) seen from a camera close to the
+surface, the clipping geometry shader, 3840x2160 RGBA8 + f32 depth, bilinear
+textured Blinn-Phong (seeded synthetic inputs; no dataset).  One step = one
+frame: framebuffer clear + vertex stage + clip GS + setup/binning + raster.
+
+Reported (one JSON line on rank 0):
+  value  input triangles per second (Mtris/s) with mesh, texture and
+         framebuffer resident in HBM, device time of the K steps (CUDA events
+         on the pipeline's stream; L2 flushed with a 256 MiB write between
+         steps, outside the timed events)
+  e2e    the same metric through the C ABI with host buffers: every step
+         copies mesh + texture from pinned host memory, renders, and reads the
+         colour and depth planes back (wall clock per step)
+  roofline  HBM roofline of the raster kernel (and of the whole frame)
+  cpu_baseline  the CPU restatement of the reference path (oracle/), all
+         host threads, on a bounded sample extrapolated to the frame
+
+--impl reference times the reference's CPU path (the oracle restatement; the
+Rust reference cannot be built here) on the same workload and metric.
+Multi-GPU: replicas only (each rank renders its own frame; no collective on
+the data path).
+"""
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "rust-softrender_gb300"))
+
+WORKLOAD = "gridsphere_1048576tri_clipgs_3840x2160_rgba8_depth_textured_blinn_phong"
+METRIC = "Mtris/s (1,048,576-tri clipped textured grid-sphere, 3840x2160 RGBA8+f32 depth, 1 GB300)"
+L2_FLUSH_BYTES = 256 << 20
+
+
+# ---------------------------------------------------------------- helpers
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms while running."""
+    FIELDS = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid):
+        self.uuid = uuid
+        self.out = tempfile.NamedTemporaryFile(prefix="clocks", suffix=".csv", delete=False)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.out, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.out.close()
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        with open(self.out.name) as f:
+            for line in f:
+                c = [x.strip() for x in line.split(",")]
+                if len(c) < 9 or (self.uuid and self.uuid not in c[0]):
+                    continue
+                try:
+                    sm.append(float(c[1]))
+                    mx = float(c[2])
+                except ValueError:
+                    continue
+                for n, v in zip(names, c[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(n)
+        os.unlink(self.out.name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def subsample_scene(scene, every):
+    """Every `every`-th triangle of the scene (all vertices kept)."""
+    import copy
+    sc = copy.copy(scene)
+    tris = scene.indices.reshape(-1, 3)[::every]
+    sc.indices = np.ascontiguousarray(tris.reshape(-1))
+    return sc
+
+
+def cpu_frame_estimate(scene, every, tiles, tile_begin=0, threads=None):
+    """Times the oracle (the reference path restated, all host threads) on a
+    bounded sample and extrapolates to one full frame:
+      t_vs    vertex stage over all vertices (no primitives)
+      t_geo   vertex + geometry stage on every `every`-th triangle
+      t_ras   rasterisation of that sample over `tiles` of the frame's tiles
+    frame = t_vs + every * (t_geo - t_vs) + every * t_ras * n_tiles / tiles
+    (the reference's geometry cost and its per-tile cost are linear in the
+    primitive count: every tile visits every primitive)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    threads = threads or os.cpu_count()
+    empty = subsample_scene(scene, 1)
+    empty.indices = np.zeros(0, dtype=np.uint32)
+    t0 = time.perf_counter()
+    oracle.render(empty, n_threads=threads, tile_end=0)
+    t_vs = time.perf_counter() - t0
+    sc = subsample_scene(scene, every)
+    t0 = time.perf_counter()
+    _, st, _ = oracle.render(sc, n_threads=threads, tile_end=0)
+    t_geo = time.perf_counter() - t0
+    n_tiles = int(st["tiles"])
+    tiles = min(tiles, n_tiles)
+    tb = tile_begin % max(1, n_tiles - tiles + 1)
+    t0 = time.perf_counter()
+    oracle.render(sc, n_threads=threads, tile_begin=tb, tile_end=tb + tiles)
+    t_all = time.perf_counter() - t0
+    t_ras = max(0.0, t_all - t_geo)
+    frame = t_vs + every * max(0.0, t_geo - t_vs) + every * t_ras * n_tiles / tiles
+    sample = ("every %d-th of %d triangles through vertex+clip GS, rasterised over %d of %d tiles, "
+              "extrapolated linearly to the frame; %.1f s of CPU wall time" % (
+                  every, scene.n_tris, tiles, n_tiles, t_vs + t_geo + t_all))
+    return frame, sample, threads
+
+
+# ------------------------------------------------------------------ ours
+def run_ours(args, rank, world, local):
+    import torch
+    import softrender as sr
+    from softrender import scenes
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    scene = scenes.grid_sphere_scene()
+    n_tris = scene.n_tris
+    pl, mesh, tex = sr.prepare_scene(scene)
+    stream = torch.cuda.Stream(device=dev)
+    pl.set_stream(stream.cuda_stream)
+    clear = list(scene.clear_bytes())
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+
+    def frame():
+        pl.clear(clear)
+        sr.submit_scene(pl, mesh, tex, scene)
+
+    for _ in range(max(3, args.warmup)):
+        frame()
+        st = pl.sync()
+        if st != 0:
+            raise RuntimeError("warm-up draw failed: status %d" % st)
+    stats = pl.stats()
+    launches_per_step = stats["kernel_launches"] + 2          # + colour and depth clear fills
+
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    uuid = str(getattr(torch.cuda.get_device_properties(local), "uuid", "") or "")
+    clocks = ClockSampler(uuid)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_wall = time.perf_counter()
+    with torch.cuda.stream(stream):
+        for e0, e1 in evs:
+            flush.zero_()                      # L2 flush, outside the timed events
+            e0.record(stream)
+            frame()
+            e1.record(stream)
+    st = pl.sync()
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    if st != 0:
+        raise RuntimeError("timed draws failed: status %d" % st)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    ms = float(np.mean(step_ms))
+    if world > 1:
+        t = torch.tensor([ms], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    stats = pl.stats()
+
+    # per-stage device times (a separate profiled pass, same work)
+    pl.set_profiling(True)
+    stage = {}
+    for _ in range(5):
+        flush.zero_()
+        frame()
+        pl.sync()
+        for k, v in pl.stats()["stage_ms"].items():
+            stage.setdefault(k, []).append(v)
+    pl.set_profiling(False)
+    stage = {k: float(np.median(v)) for k, v in stage.items()}
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        keep = []
+
+        def pinned(a):
+            t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+            keep.append(t)
+            return t.numpy()
+        h_planes = [pinned(p) for p in scene.planes]
+        h_idx = pinned(scene.indices)
+        h_tex = pinned(scene.texture)
+        h_color = pinned(np.zeros((scene.height, scene.width), dtype=np.uint32))
+        h_depth = pinned(np.zeros((scene.height, scene.width), dtype=np.float32))
+        import ctypes as C
+        from softrender._lib import lib
+        h2d = sum(p.nbytes for p in h_planes) + h_idx.nbytes + h_tex.nbytes
+        d2h = h_color.nbytes + h_depth.nbytes
+        e2e_steps = max(3, min(args.steps, 10))
+        times = []
+        for i in range(e2e_steps + 2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            mesh.update(h_planes, h_idx, stream.cuda_stream)
+            tex.update(h_tex, stream.cuda_stream)
+            frame()
+            rc = lib().sr_framebuffer_read(pl.handle, h_color.ctypes.data, h_depth.ctypes.data, None)
+            dt = time.perf_counter() - t0
+            if rc != 0:
+                raise RuntimeError("e2e read failed: %d" % rc)
+            if i >= 2:
+                times.append(dt)
+        e2e_ms = float(np.mean(times)) * 1e3
+        e2e = {"value": round(n_tris / (e2e_ms * 1e-3) / 1e6 * world, 3), "unit": "Mtris/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4)}
+
+    pl.destroy()
+    return dict(ms=ms, step_ms=step_ms, stats=stats, stage=stage, clocks=clk, e2e=e2e, scene=scene,
+                launches=launches_per_step * args.steps, wall_s=t_wall)
+
+
+# -------------------------------------------------------------- reporting
+def config_block(world):
+    return {"workload": WORKLOAD, "triangles": 1048576, "vertices": 525825, "resolution": "3840x2160",
+            "framebuffer": "RGBA8 + f32 depth", "geometry_shader": "clip_primitives",
+            "shader": "textured_blinn_phong (1024x1024 RGBA8, bilinear, clamp)", "semantic_tile": "128x128",
+            "step": "clear + vertex + clip GS + setup/binning + raster (one frame)",
+            "l2": "flushed by a 256 MiB write between timed steps",
+            "parallelism": "single GPU" if world == 1 else "replicas x%d (no collective)" % world}
+
+
+def raster_bytes(scene):
+    """Algorithmic bytes of the raster kernel: colour + depth planes read and
+    written once, texture read once."""
+    return 2 * scene.width * scene.height * 8 + scene.texture.nbytes
+
+
+def traffic_from_profiles():
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f).get("raster_kernel_dram_bytes_per_launch")
+    except Exception:
+        return None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import torch
+    if world > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    r = run_ours(args, rank, world, local)
+    scene = r["scene"]
+    n_tris = scene.n_tris
+    peak, peak_kind = measured_peaks()
+    ms = r["ms"]
+    value = n_tris * world / (ms * 1e-3) / 1e6
+    frags = r["stats"]["fragments"]
+    line = None
+    if rank == 0:
+        rb = raster_bytes(scene)
+        r_ms = r["stage"].get("raster", float("nan"))
+        ach = rb / (r_ms * 1e-3) / 1e9
+        fb = scene.algorithmic_bytes()
+        line = {
+            "metric": METRIC, "value": round(value, 3), "unit": "Mtris/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 4),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded displaced grid-sphere, procedural texture)",
+            "config": config_block(world),
+            "gfrag_per_s": round(frags * world / (ms * 1e-3) / 1e9, 4),
+            "fragments_per_frame": int(frags),
+            "triangles_generated_per_frame": int(r["stats"]["triangles_generated"]),
+            "triangles_rasterised_per_frame": int(r["stats"]["triangles_raster"]),
+            "roofline": {"bound": "hbm", "kernel": "raster_opaque_kernel<textured_blinn_phong, RGBA8>",
+                         "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
+                         "frac": round(ach / peak, 4), "traffic": traffic_from_profiles(),
+                         "algorithmic_bytes": int(rb), "kernel_ms": round(r_ms, 4),
+                         "peak_source": peak_kind},
+            "frame_roofline": {"algorithmic_bytes": int(fb), "achieved": round(fb / (ms * 1e-3) / 1e9, 2),
+                               "unit": "GB/s", "frac": round(fb / (ms * 1e-3) / 1e9 / peak, 4)},
+            "stage_ms": {k: round(v, 4) for k, v in r["stage"].items()},
+            "e2e": r["e2e"],
+            "gpu_launches": int(r["launches"]),
+            "clocks": r["clocks"],
+        }
+        if not args.no_cpu_baseline:
+            frame_s, sample, threads = cpu_frame_estimate(scene, every=4, tiles=48)
+            line["cpu_baseline"] = {"value": round(n_tris / frame_s / 1e6, 5), "unit": "Mtris/s",
+                                    "cores": threads, "kind": "port", "sample": sample}
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.destroy_process_group()
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+def run_reference(args, rank, world):
+    """The reference's CPU path (restated in oracle/, as the Rust crate cannot
+    be built here) on the host cores, same workload and metric."""
+    if rank != 0:
+        return
+    from softrender import scenes
+    scene = scenes.grid_sphere_scene()
+    n_tris = scene.n_tris
+    for i in range(args.warmup):
+        cpu_frame_estimate(scene, every=64, tiles=2, tile_begin=i)
+    frames, sample, threads = [], "", os.cpu_count()
+    for i in range(args.steps):
+        f, sample, threads = cpu_frame_estimate(scene, every=16, tiles=32, tile_begin=32 * i)
+        frames.append(f)
+    frame_s = float(np.mean(frames))
+    value = n_tris / frame_s / 1e6
+    line = {
+        "metric": METRIC, "value": round(value, 5), "unit": "Mtris/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(frame_s * 1e3, 2),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded displaced grid-sphere, procedural texture)",
+        "config": config_block(1), "impl": "reference",
+        "cpu_baseline": {"value": round(value, 5), "unit": "Mtris/s", "cores": threads, "kind": "port",
+                         "sample": "per step: " + sample},
+        "e2e": {"value": round(value, 5), "unit": "Mtris/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

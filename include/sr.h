@@ -159,6 +159,11 @@ typedef struct sr_stats {
                                      counted once per pixel and primitive          */
     uint32_t nan_bbox;            /* primitives skipped for an all-NaN bbox        */
     uint32_t overflow;            /* nonzero if a fixed-capacity buffer overflowed */
+    uint32_t kernel_launches;     /* kernels the draw launched                     */
+    uint32_t profiled;            /* 1 if stage_ms holds timings                   */
+    float stage_ms[6];            /* with sr_pipeline_set_profiling: device time of
+                                     vertex, geometry, setup+binning, raster,
+                                     stencil, total                               */
 } sr_stats;
 
 /* -------------------------------------------------------------- pipeline */
@@ -177,6 +182,10 @@ SR_API int sr_pipeline_set_stencil(sr_pipeline* p, int test, int op, int wrap);
  * (cudaStream_t as void*) that render calls are ordered on; NULL = legacy default. */
 SR_API int sr_pipeline_set_stream(sr_pipeline* p, void* stream);
 SR_API int sr_pipeline_destroy(sr_pipeline* p);
+/* Records CUDA events between the stages of every draw (no counterpart in the
+ * reference, which has no profiling hooks); sr_get_stats then reports
+ * stage_ms for the most recent draw. */
+SR_API int sr_pipeline_set_profiling(sr_pipeline* p, int enable);
 
 /* Framebuffer::clear (src/framebuffer/mod.rs:36, renderbuffer/mod.rs:125-133):
  * colour <- *color (float[4] for RGBA32F, uint8[4] for RGBA8), depth <- f32::MIN,
@@ -198,12 +207,23 @@ SR_API int sr_framebuffer_device_ptrs(sr_pipeline* p, void** color, float** dept
  * Host buffers are copied before return; the mesh is immutable afterwards. */
 SR_API int sr_mesh_upload(const float* const* planes, uint32_t n_planes, uint32_t n_verts,
                           const uint32_t* indices, uint64_t n_indices, sr_mesh** out);
+/* Replaces the contents of an uploaded mesh with new host data of the same
+ * shape (plane count, vertex count, index count), without reallocating;
+ * copies are ordered on `stream` (cudaStream_t as void*, NULL: synchronous).
+ * Host buffers should be pinned for asynchronous copies.  Indices are not
+ * scanned on the host here: primitives with an index >= n_verts are skipped
+ * on the device and the next sr_sync returns SR_EINVAL. */
+SR_API int sr_mesh_update(sr_mesh* m, const float* const* planes, uint32_t n_planes, uint32_t n_verts,
+                          const uint32_t* indices, uint64_t n_indices, void* stream);
 SR_API int sr_mesh_free(sr_mesh* m);
 /* Device bytes held by a mesh (for HBM budgeting). */
 SR_API uint64_t sr_mesh_bytes(const sr_mesh* m);
 
 /* An RGBA8 texture (r in the low byte) read by the textured shaders. */
 SR_API int sr_texture_upload(const uint32_t* rgba8, uint32_t width, uint32_t height, sr_texture** out);
+/* Replaces the texels of an uploaded texture of the same size, ordered on
+ * `stream` (NULL: synchronous). */
+SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, uint32_t width, uint32_t height, void* stream);
 SR_API int sr_texture_free(sr_texture* t);
 
 /* Shader registry: device functions compiled into the library, looked up by

@@ -18,6 +18,9 @@
  *   - `as u8`: truncate toward zero, saturate to [0,255], NaN -> 0
  * f32::powf is libm's in the reference; here it is sr_powf below (double-float
  * log2 + exp2, own implementation from the series stated in its comment).
+ * Explicit fused multiply-adds (sr_fma) appear only inside these library
+ * functions (pow, the byte -> unit conversion), which are defined here, not
+ * restated from the reference.
  *
  * Matrices are 16 floats, row-major: m[row*4 + col].
  */
@@ -148,8 +151,18 @@ SR_HD float sr_powi(float x, int n) {
 }
 
 /* ---------------------------------------------- double-float building blocks
- * Error-free transformations without FMA: Knuth's TwoSum, Dekker's FastTwoSum,
- * Veltkamp splitting (splitter 2^12+1 for binary32) and Dekker's TwoProduct.  */
+ * Error-free transformations: Knuth's TwoSum, Dekker's FastTwoSum, and the
+ * exact product error e = fma(a, b, -a*b).  Explicit fused multiply-adds are
+ * single correctly rounded operations on every IEEE-754 target (CUDA fma.rn,
+ * C99 fmaf), so host and device results are identical; they are used only
+ * inside these library functions, never in the restated shader expressions. */
+SR_HD float sr_fma(float a, float b, float c) {
+#if defined(__CUDA_ARCH__)
+    return __fmaf_rn(a, b, c);
+#else
+    return fmaf(a, b, c);
+#endif
+}
 SR_HD void sr_two_sum(float a, float b, float* s, float* e) {
     float ss = a + b;
     float bb = ss - a;
@@ -161,18 +174,9 @@ SR_HD void sr_fast_two_sum(float a, float b, float* s, float* e) {  /* |a| >= |b
     *e = b - (ss - a);
     *s = ss;
 }
-SR_HD void sr_split(float a, float* hi, float* lo) {
-    float c = 4097.0f * a;
-    float h = c - (c - a);
-    *hi = h;
-    *lo = a - h;
-}
 SR_HD void sr_two_prod(float a, float b, float* p, float* e) {
     float pp = a * b;
-    float ah, al, bh, bl;
-    sr_split(a, &ah, &al);
-    sr_split(b, &bh, &bl);
-    *e = (((ah * bh - pp) + ah * bl) + al * bh) + al * bl;
+    *e = sr_fma(a, b, -pp);
     *p = pp;
 }
 
@@ -207,11 +211,11 @@ SR_HD void sr_log2_df(float x, float* lhi, float* llo) {
     float sl = r / dh;
     float s2 = sh * sh;
     float poly = 0.1538461538461538f;                 /* 2/13 */
-    poly = 0.1818181818181818f + s2 * poly;           /* 2/11 */
-    poly = 0.2222222222222222f + s2 * poly;           /* 2/9  */
-    poly = 0.2857142857142857f + s2 * poly;           /* 2/7  */
-    poly = 0.4f + s2 * poly;                          /* 2/5  */
-    poly = 0.6666666666666666f + s2 * poly;           /* 2/3  */
+    poly = sr_fma(s2, poly, 0.1818181818181818f);     /* 2/11 */
+    poly = sr_fma(s2, poly, 0.2222222222222222f);     /* 2/9  */
+    poly = sr_fma(s2, poly, 0.2857142857142857f);     /* 2/7  */
+    poly = sr_fma(s2, poly, 0.4f);                    /* 2/5  */
+    poly = sr_fma(s2, poly, 0.6666666666666666f);     /* 2/3  */
     float tail = (sh * s2) * poly;
     float ln_h, ln_l;
     sr_fast_two_sum(2.0f * sh, 2.0f * sl + tail, &ln_h, &ln_l);
@@ -244,12 +248,12 @@ SR_HD float sr_exp2_df(float th, float tl) {
     sr_two_prod(f, LN2_HI, &rh, &rl);
     rl = rl + f * LN2_LO;
     float p = 2.4801587301587302e-05f;                /* 1/8! */
-    p = 1.9841269841269841e-04f + rh * p;             /* 1/7! */
-    p = 1.3888888888888889e-03f + rh * p;             /* 1/6! */
-    p = 8.3333333333333332e-03f + rh * p;             /* 1/5! */
-    p = 4.1666666666666664e-02f + rh * p;             /* 1/4! */
-    p = 1.6666666666666666e-01f + rh * p;             /* 1/3! */
-    p = 0.5f + rh * p;                                /* 1/2! */
+    p = sr_fma(rh, p, 1.9841269841269841e-04f);       /* 1/7! */
+    p = sr_fma(rh, p, 1.3888888888888889e-03f);       /* 1/6! */
+    p = sr_fma(rh, p, 8.3333333333333332e-03f);       /* 1/5! */
+    p = sr_fma(rh, p, 4.1666666666666664e-02f);       /* 1/4! */
+    p = sr_fma(rh, p, 1.6666666666666666e-01f);       /* 1/3! */
+    p = sr_fma(rh, p, 0.5f);                          /* 1/2! */
     p = (rh * rh) * p;
     float res = 1.0f + (rh + (rl + p));
     int ni = (int)n;
@@ -324,10 +328,21 @@ SR_HD uint32_t sr_to_rgba8(sr_v4 c) {
     return sr_pack_rgba8(sr_f32_to_u8(c.x * 255.0f), sr_f32_to_u8(c.y * 255.0f),
                          sr_f32_to_u8(c.z * 255.0f), sr_f32_to_u8(c.w * 255.0f));
 }
+/* c as f32 / 255.0 for a byte c: the correctly rounded quotient, computed as
+ * q = c * (1/255) refined once with the exact residual c - 255 q (fused);
+ * equal to the IEEE division for all 256 values (checked exhaustively by the
+ * tests). */
+SR_HD float sr_u8_unit(uint32_t c) {
+    const float r = 1.0f / 255.0f;
+    float x = (float)c;
+    float q = x * r;
+    float e = sr_fma(-q, 255.0f, x);
+    return sr_fma(e, r, q);
+}
 /* RGBA8 -> f32 as in from_image_texel (full_example/src/texture.rs:38-45): c as f32 / 255.0 */
 SR_HD sr_v4 sr_from_rgba8(uint32_t p) {
-    return sr_make_v4((float)(p & 0xffu) / 255.0f, (float)((p >> 8) & 0xffu) / 255.0f,
-                      (float)((p >> 16) & 0xffu) / 255.0f, (float)(p >> 24) / 255.0f);
+    return sr_make_v4(sr_u8_unit(p & 0xffu), sr_u8_unit((p >> 8) & 0xffu),
+                      sr_u8_unit((p >> 16) & 0xffu), sr_u8_unit(p >> 24));
 }
 /* Over operator on RGBA8: channels to f32 (c/255), over, back with `as u8`. */
 SR_HD uint32_t sr_blend_over_rgba8(uint32_t src, uint32_t dst) {

@@ -65,8 +65,12 @@ def lib():
         L.or_clip_triangle.argtypes = [C.POINTER(C.c_float)] * 3 + [C.c_uint32, C.POINTER(C.c_float),
                                                                     C.c_uint32]
         L.or_clip_triangle.restype = C.c_uint32
+        L.or_raster_tris.argtypes = [C.POINTER(OrDraw), C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint64,
+                                     C.POINTER(C.c_uint64)]
         L.or_powf.argtypes = [C.c_float, C.c_float]
         L.or_powf.restype = C.c_float
+        L.or_u8_unit.argtypes = [C.c_uint32]
+        L.or_u8_unit.restype = C.c_float
         L.or_coordinate_into_index.argtypes = [C.c_uint32, C.c_uint32, C.c_uint32]
         L.or_coordinate_into_index.restype = C.c_uint64
         L.or_coordinate_from_index.argtypes = [C.c_uint64, C.c_uint32, C.POINTER(C.c_uint32),
@@ -111,16 +115,13 @@ def framebuffer_for(scene):
     return fb
 
 
-def render(scene, fb=None, n_threads=1, tile_begin=0, tile_end=0xFFFFFFFF):
-    """Renders `scene` (softrender.scenes.Scene) into fb (a new cleared one if
-    None); returns (fb, stats dict, status)."""
-    if fb is None:
-        fb = framebuffer_for(scene)
-    keep = []
+def _draw(scene, keep):
     planes = [np.ascontiguousarray(p, dtype=np.float32) for p in scene.planes]
     keep += planes
     parr = (C.POINTER(C.c_float) * len(planes))(*[p.ctypes.data_as(C.POINTER(C.c_float)) for p in planes])
+    keep.append(parr)
     idx = np.ascontiguousarray(scene.indices, dtype=np.uint32)
+    keep.append(idx)
     d = OrDraw()
     d.planes = parr
     d.n_planes = len(planes)
@@ -146,6 +147,28 @@ def render(scene, fb=None, n_threads=1, tile_begin=0, tile_end=0xFFFFFFFF):
         d.tex_h, d.tex_w = tex.shape
     d.tex_filter, d.tex_edge = scene.tex_filter, scene.tex_edge
     d.uniforms = C.addressof(scene.uniforms)
+    return d
+
+
+def raster_tris(scene):
+    """(n, 3, 4) float32 screen positions of the triangles the fragment stage
+    rasterises for `scene` (after vertex and geometry stages)."""
+    keep = []
+    d = _draw(scene, keep)
+    n = C.c_uint64()
+    lib().or_raster_tris(C.byref(d), scene.width, scene.height, None, 0, C.byref(n))
+    out = np.empty((max(1, n.value), 3, 4), dtype=np.float32)
+    lib().or_raster_tris(C.byref(d), scene.width, scene.height, out.ctypes.data, n.value, C.byref(n))
+    return out[:n.value]
+
+
+def render(scene, fb=None, n_threads=1, tile_begin=0, tile_end=0xFFFFFFFF):
+    """Renders `scene` (softrender.scenes.Scene) into fb (a new cleared one if
+    None); returns (fb, stats dict, status)."""
+    if fb is None:
+        fb = framebuffer_for(scene)
+    keep = []
+    d = _draw(scene, keep)
     st = OrStats()
     cfb = fb._c()
     status = lib().or_render(C.byref(d), C.byref(cfb), n_threads, tile_begin, tile_end, C.byref(st))
@@ -178,6 +201,10 @@ def clip_triangle(a, b, c, nk=0):
     out = (C.c_float * (stride * 3 * 40))()
     n = lib().or_clip_triangle(A_, B_, C_, nk, out, 120)
     return np.array(out[:n * stride], dtype=np.float32).reshape(n, stride)
+
+
+def u8_unit(c):
+    return np.float32(lib().or_u8_unit(int(c)))
 
 
 def powf(x, y):

@@ -629,6 +629,7 @@ uint32_t or_clip_triangle(const float* a, const float* b, const float* c, uint32
 }
 
 float or_powf(float x, float y) { return sr_powf(x, y); }
+float or_u8_unit(uint32_t c) { return sr_u8_unit(c); }
 
 /* Coordinate::into_index / from_index (src/geometry/coordinate.rs:44-61) */
 uint64_t or_coordinate_into_index(uint32_t x, uint32_t y, uint32_t width) {
@@ -640,8 +641,24 @@ void or_coordinate_from_index(uint64_t index, uint32_t width, uint32_t* x, uint3
     *y = (uint32_t)((index - xx) / width);
 }
 
+int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, uint32_t tile_end,
+                   or_stats* stats, float* tris_out, uint64_t tris_cap, uint64_t* n_tris_out);
+
 int or_render(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, uint32_t tile_end,
               or_stats* stats) {
+    return or_render_impl(d, fb, n_threads, tile_begin, tile_end, stats, nullptr, 0, nullptr);
+}
+
+int or_raster_tris(const or_draw* d, uint32_t width, uint32_t height, float* out, uint64_t cap, uint64_t* n) {
+    or_fb fb;
+    std::memset(&fb, 0, sizeof(fb));
+    fb.width = width;
+    fb.height = height;
+    return or_render_impl(d, &fb, 1, 0, 0, nullptr, out, cap, n);
+}
+
+int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, uint32_t tile_end,
+                   or_stats* stats, float* tris_out, uint64_t tris_cap, uint64_t* n_tris_out) {
     Ctx c;
     c.d = d;
     c.U = d->uniforms;
@@ -718,6 +735,25 @@ int or_render(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, u
         norm_all(gen_tris);
         norm_all(gen_lines);
         norm_all(gen_points);
+    }
+
+    if (tris_out || n_tris_out) {
+        /* screen positions of the triangles the fragment stage rasterises */
+        uint64_t k = 0;
+        auto put = [&](const CV& a, const CV& b, const CV& c2) {
+            if (k < tris_cap) {
+                const CV* v[3] = {&a, &b, &c2};
+                for (int j = 0; j < 3; ++j)
+                    for (int q = 0; q < 4; ++q) tris_out[k * 12 + j * 4 + q] = v[j]->p[q];
+            }
+            ++k;
+        };
+        if (pn == 3 && indexed)
+            for (uint64_t i = 0; i < d->n_indices; i += 3)
+                put(verts[d->indices[i]], verts[d->indices[i + 1]], verts[d->indices[i + 2]]);
+        for (size_t i = 0; i + 2 < gen_tris.size(); i += 3) put(gen_tris[i], gen_tris[i + 1], gen_tris[i + 2]);
+        if (n_tris_out) *n_tris_out = k;
+        return 0;
     }
 
     /* fragment stage (fragment.rs:168-319) */

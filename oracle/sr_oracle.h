@@ -68,6 +68,11 @@ typedef struct or_stats {
 int or_render(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, uint32_t tile_end,
               or_stats* stats);
 
+/* Screen-space positions (x, y, z, 1/w per vertex, 12 floats per triangle)
+ * of the triangles the fragment stage rasterises, after the vertex and
+ * geometry stages; *n receives the count (out may hold fewer). */
+int or_raster_tris(const or_draw* d, uint32_t width, uint32_t height, float* out, uint64_t cap, uint64_t* n);
+
 /* Framebuffer::clear: colour <- color, depth <- f32::MIN, stencil <- 0 */
 void or_clear(or_fb* fb, const void* color);
 
@@ -78,6 +83,7 @@ void or_normalize(const float clip[4], const float viewport[6], float out[4]);
 uint32_t or_clip_triangle(const float* a, const float* b, const float* c, uint32_t nk,
                           float* out, uint32_t cap);
 float or_powf(float x, float y);
+float or_u8_unit(uint32_t c);
 uint64_t or_coordinate_into_index(uint32_t x, uint32_t y, uint32_t width);
 void or_coordinate_from_index(uint64_t index, uint32_t width, uint32_t* x, uint32_t* y);
 void or_derive_uniforms(sr_uniforms* u);

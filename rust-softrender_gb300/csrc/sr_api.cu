@@ -8,6 +8,7 @@
 // buffers and replays the draws from the first poisoned one, so the
 // framebuffer always ends up exactly as if capacities had been large enough.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -77,7 +78,10 @@ struct sr_pipeline {
     DevBuf<uint32_t> refs;
     DevBuf<float4> setup;
     DevBuf<uint2> binrect;
-    DevBuf<uint32_t> bin_counts, bin_off, bin_cursor, bin_tmp, entries;
+    DevBuf<uint32_t> bin_counts, bin_off, bin_cursor, bin_tmp, entries, unsafe_list;
+    DevBuf<unsigned long long> area, gkeys;
+    DevBuf<uint32_t> big_list;
+    DevBuf<uint32_t> bitmap;
     DevBuf<int> st_diff, st_lines;
     DevBuf<unsigned long long> st_glob;
     // capacities (elements) requested for the generated geometry
@@ -85,6 +89,11 @@ struct sr_pipeline {
     std::vector<PendingDraw> pending;
     sr_stats last_stats;
     bool stats_valid = false;
+    bool force_unsafe = false;   // SR_FORCE_UNSAFE=1: every primitive takes the exact unsafe path
+    bool profiling = false;
+    cudaEvent_t ev[6] = {};
+    uint32_t last_launches = 0;
+    bool last_profiled = false;
 };
 
 namespace {
@@ -198,6 +207,8 @@ extern "C" SR_API int sr_pipeline_create(const sr_fb_desc* fb, const void* unifo
         return e == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA;
     }
     p->stream = p->own_stream;
+    const char* fu = std::getenv("SR_FORCE_UNSAFE");
+    p->force_unsafe = fu && fu[0] == '1';
     DeviceFlags z;
     std::memset(&z, 0, sizeof(z));
     z.poison_draw = 0xffffffffu;
@@ -223,8 +234,10 @@ extern "C" SR_API int sr_pipeline_destroy(sr_pipeline* p) {
     p->clip4.release(); p->scr4.release(); p->vary.release();
     p->clip_counts.release(); p->clip_offsets.release(); p->clip_tmp.release(); p->refs.release();
     p->setup.release(); p->binrect.release();
-    p->bin_counts.release(); p->bin_off.release(); p->bin_cursor.release(); p->bin_tmp.release(); p->entries.release();
+    p->bin_counts.release(); p->bin_off.release(); p->bin_cursor.release(); p->bin_tmp.release(); p->entries.release(); p->unsafe_list.release();
     p->st_diff.release(); p->st_lines.release(); p->st_glob.release();
+    p->area.release(); p->big_list.release(); p->gkeys.release(); p->bitmap.release();
+    for (auto& e : p->ev) if (e) cudaEventDestroy(e);
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
     delete p;
     return SR_OK;
@@ -234,6 +247,14 @@ extern "C" SR_API int sr_pipeline_set_uniforms(sr_pipeline* p, const void* unifo
     if (!p || !uniforms || usz != sizeof(sr_uniforms)) return SR_EINVAL;
     std::memcpy(&p->U, uniforms, sizeof(sr_uniforms));
     sr_uniforms_derive(&p->U);
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_pipeline_set_profiling(sr_pipeline* p, int enable) {
+    if (!p) return SR_EINVAL;
+    if (enable && !p->ev[0])
+        for (auto& e : p->ev) SR_CK(cudaEventCreate(&e));
+    p->profiling = enable != 0;
     return SR_OK;
 }
 
@@ -343,6 +364,18 @@ extern "C" SR_API int sr_mesh_upload(const float* const* planes, uint32_t n_plan
     return SR_OK;
 }
 
+extern "C" SR_API int sr_mesh_update(sr_mesh* m, const float* const* planes, uint32_t n_planes, uint32_t n_verts,
+                                     const uint32_t* indices, uint64_t n_indices, void* stream) {
+    if (!m || n_planes != m->n_planes || n_verts != m->n_verts || n_indices != m->n_indices) return SR_EINVAL;
+    if ((n_planes && !planes) || (n_indices && !indices)) return SR_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    for (uint32_t j = 0; j < n_planes; ++j)
+        SR_CK(cudaMemcpyAsync(m->planes + (size_t)j * m->n_pad, planes[j], (size_t)n_verts * 4, cudaMemcpyHostToDevice, st));
+    if (n_indices) SR_CK(cudaMemcpyAsync(m->indices, indices, n_indices * 4, cudaMemcpyHostToDevice, st));
+    if (!stream) SR_CK(cudaStreamSynchronize(st));
+    return SR_OK;
+}
+
 extern "C" SR_API int sr_mesh_free(sr_mesh* m) {
     if (!m) return SR_EINVAL;
     if (m->planes) cudaFree(m->planes);
@@ -369,6 +402,14 @@ extern "C" SR_API int sr_texture_upload(const uint32_t* rgba8, uint32_t w, uint3
         return e == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA;
     }
     *out = t;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, uint32_t w, uint32_t h, void* stream) {
+    if (!t || !rgba8 || w != t->w || h != t->h) return SR_EINVAL;
+    cudaStream_t st = (cudaStream_t)stream;
+    SR_CK(cudaMemcpyAsync(t->data, rgba8, (size_t)w * h * 4, cudaMemcpyHostToDevice, st));
+    if (!stream) SR_CK(cudaStreamSynchronize(st));
     return SR_OK;
 }
 
@@ -403,6 +444,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
     P.has_stencil = p->stencil != nullptr;
     P.color_format = p->fb.color_format;
     P.draw_id = draw_id;
+    P.force_unsafe = p->force_unsafe ? 1u : 0u;
     if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; }
     P.tex_filter = d->tex_filter; P.tex_edge = d->tex_edge;
     // stencil mode (src/stencil.rs; a missing attachment behaves as `()`)
@@ -436,6 +478,8 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
     // per-draw statistics start from zero
     SR_CK(cudaMemsetAsync(reinterpret_cast<char*>(p->flags) + FLAGS_STATS_OFFSET, 0,
                           sizeof(DeviceFlags) - FLAGS_STATS_OFFSET, st));
+    p->last_launches = 0;
+    p->last_profiled = false;
     if (nothing) return SR_OK;
 
     // ---- capacities
@@ -464,8 +508,21 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
     if ((rc = p->setup.ensure(4 * n_raster_cap)) || (rc = p->binrect.ensure(n_raster_cap)) ||
         (rc = p->bin_counts.ensure(n_bins)) || (rc = p->bin_off.ensure((size_t)n_bins + 1)) ||
         (rc = p->bin_cursor.ensure(n_bins)) || (rc = p->bin_tmp.ensure(scan_blocks(n_bins) + 2)) ||
-        (rc = p->entries.ensure(p->entry_cap)))
+        (rc = p->entries.ensure(p->entry_cap)) || (rc = p->unsafe_list.ensure(n_raster_cap)))
         return rc;
+    if (!ordered) {
+        const size_t npx = (size_t)W * H;
+        const size_t nblk = (size_t)((W + 31) / 32) * ((H + 31) / 32);
+        const bool fresh = p->gkeys.cap < npx || p->bitmap.cap < (nblk + 31) / 32;
+        if ((rc = p->area.ensure(n_raster_cap + 1)) || (rc = p->big_list.ensure(n_raster_cap + 1)) ||
+            (rc = p->gkeys.ensure(npx)) ||
+            (rc = p->bitmap.ensure((nblk + 31) / 32)))
+            return rc;
+        if (fresh) {   // zero once; the resolve pass leaves them zero
+            SR_CK(cudaMemsetAsync(p->gkeys.p, 0, p->gkeys.cap * 8, st));
+            SR_CK(cudaMemsetAsync(p->bitmap.p, 0, p->bitmap.cap * 4, st));
+        }
+    }
     StencilCountArgs S{nullptr, nullptr, nullptr};
     if (P.stencil_active && !P.mode_b) {
         size_t nd = (size_t)(W + 1) * (H + 1);
@@ -478,22 +535,42 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
     }
     VertexStore vs{p->clip4.p, p->scr4.p, p->vary.p, (uint32_t)vslots};
 
-    // ---- vertex stage
+    // ---- stages, with optional events between them
+    cudaEvent_t* ev = p->profiling ? p->ev : nullptr;
+    if (ev) cudaEventRecord(ev[0], st);
     launch_vertex(P, pd.U, m, vs, !indexed, st);
-    // ---- geometry stage
+    uint32_t launches = 1;
+    if (ev) cudaEventRecord(ev[1], st);
     const uint32_t* vidx = m->indices;
     if (!indexed) {
         launch_clip(P, m, vs, p->clip_counts.p, p->clip_offsets.p, p->clip_tmp.p, p->refs.p, p->flags, st);
         vidx = p->refs.p;
+        launches += 5;
     }
-    // ---- setup + binning (+ stencil event counts)
+    if (ev) cudaEventRecord(ev[2], st);
     launch_setup_bin(P, vidx, vs, p->setup.p, reinterpret_cast<uint32_t*>(p->binrect.p), p->bin_counts.p, p->bin_off.p,
-                     p->bin_cursor.p, p->entries.p, p->bin_tmp.p, S, p->flags, st);
-    // ---- raster
+                     p->bin_cursor.p, p->entries.p, p->bin_tmp.p, p->unsafe_list.p, ordered ? nullptr : p->area.p, S,
+                     p->flags, st);
+    launches += !ordered ? 1 : (P.mode_b ? 6 : 8);
+    if (ev) cudaEventRecord(ev[3], st);
     const uint32_t* tex = d->texture ? d->texture->data : nullptr;
-    launch_raster_any(ordered, P, pd.U, p->setup.p, p->bin_off.p, p->entries.p, vidx, p->vary.p, tex, p->color,
-                      p->depth, p->stencil, gate, p->flags, st);
-    if (P.stencil_active && !P.mode_b) launch_stencil_apply(P, S, p->stencil, p->flags, st);
+    if (ordered) {
+        launch_ordered(P, pd.U, p->setup.p, p->bin_off.p, p->entries.p, vidx, p->vary.p, tex, p->color, p->depth,
+                       p->stencil, gate, p->flags, st);
+        launches += 1;
+    } else {
+        OpaqueArgs A{p->setup.p, p->area.p, p->big_list.p, p->gkeys.p, p->bitmap.p, p->unsafe_list.p,
+                     vidx, p->vary.p, tex, p->color, p->depth, p->stencil, gate, p->flags};
+        launches += (uint32_t)launch_opaque(P, pd.U, A, st);
+    }
+    if (ev) cudaEventRecord(ev[4], st);
+    if (P.stencil_active && !P.mode_b) {
+        launch_stencil_apply(P, S, p->stencil, p->flags, st);
+        launches += 5;
+    }
+    if (ev) cudaEventRecord(ev[5], st);
+    p->last_launches = launches;
+    p->last_profiled = ev != nullptr;
     SR_CK(cudaGetLastError());
     return SR_OK;
 }
@@ -547,7 +624,14 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
             p->last_stats.overflow = f.overflow_bits;
             const sr_mesh* m = p->pending.back().d.mesh;
             p->last_stats.triangles_in = m ? m->n_indices / 3 : 0;
+            p->last_stats.kernel_launches = p->last_launches;
+            if (p->last_profiled) {
+                p->last_stats.profiled = 1;
+                for (int k = 0; k < 5; ++k) cudaEventElapsedTime(&p->last_stats.stage_ms[k], p->ev[k], p->ev[k + 1]);
+                cudaEventElapsedTime(&p->last_stats.stage_ms[5], p->ev[0], p->ev[5]);
+            }
             if (f.nan_total) status = SR_ENAN;
+            if (f.bad_index) status = SR_EINVAL;
             break;
         }
         // grow what overflowed and replay from the first poisoned draw

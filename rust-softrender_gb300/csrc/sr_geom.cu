@@ -157,13 +157,21 @@ __device__ __forceinline__ bool out_tri_degenerate(const Poly& P, int k) {
     return same_vertex(P, i0, i1) || same_vertex(P, i1, i2) || same_vertex(P, i0, i2);
 }
 
-__global__ void __launch_bounds__(256) clip_count_kernel(uint32_t n_in, uint32_t keep_degenerate,
+__global__ void __launch_bounds__(256) clip_count_kernel(uint32_t n_in, uint32_t n_verts, uint32_t keep_degenerate,
                                                          const uint32_t* __restrict__ idx,
                                                          const float4* __restrict__ clip4,
                                                          unsigned long long* __restrict__ counts,
                                                          DeviceFlags* flags) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long gen = 0;
+    if (t < n_in) {
+        uint32_t i0 = __ldg(idx + 3 * t), i1 = __ldg(idx + 3 * t + 1), i2 = __ldg(idx + 3 * t + 2);
+        if (i0 >= n_verts || i1 >= n_verts || i2 >= n_verts) {
+            counts[t] = 0;
+            atomicOr(&flags->bad_index, 1u);
+            t = n_in;   // contributes nothing
+        }
+    }
     if (t < n_in) {
         uint32_t mk[3];
 #pragma unroll
@@ -192,7 +200,8 @@ __global__ void __launch_bounds__(256) clip_count_kernel(uint32_t n_in, uint32_t
 // then ClipVertex::normalize of finish().
 __device__ __forceinline__ float lerp1(float t, float x1, float x2) { return (1.0f - t) * x1 + t * x2; }
 
-__global__ void __launch_bounds__(256) clip_emit_kernel(uint32_t n_in, uint32_t keep_degenerate, uint32_t draw_id,
+__global__ void __launch_bounds__(256) clip_emit_kernel(uint32_t n_in, uint32_t n_verts, uint32_t keep_degenerate,
+                                                        uint32_t draw_id,
                                                         VpMatrix vpm,
                                                         uint32_t gen_base, uint32_t gen_tri_cap,
                                                         uint32_t gen_vert_cap,
@@ -219,8 +228,10 @@ __global__ void __launch_bounds__(256) clip_emit_kernel(uint32_t n_in, uint32_t 
     float4 c[3];
     uint32_t mk[3];
 #pragma unroll
+    for (int j = 0; j < 3; ++j) vi[j] = __ldg(idx + 3 * t + j);
+    if (vi[0] >= n_verts || vi[1] >= n_verts || vi[2] >= n_verts) return;   // flagged in the count pass
+#pragma unroll
     for (int j = 0; j < 3; ++j) {
-        vi[j] = __ldg(idx + 3 * t + j);
         c[j] = __ldg(clip4 + vi[j]);
         mk[j] = inside_mask(c[j]);
     }
@@ -282,10 +293,10 @@ void launch_clip(const DrawParams& P, const sr_mesh* m, VertexStore vs, unsigned
                  DeviceFlags* flags, cudaStream_t st) {
     uint32_t n = P.n_in;
     dim3 block(256), grid((n + 255) / 256 ? (n + 255) / 256 : 1);
-    clip_count_kernel<<<grid, block, 0, st>>>(n, P.keep_degenerate, m->indices, vs.clip4, counts, flags);
+    clip_count_kernel<<<grid, block, 0, st>>>(n, P.n_verts, P.keep_degenerate, m->indices, vs.clip4, counts, flags);
     exclusive_scan<unsigned long long>(counts, n, offsets, scan_tmp, st);
     VpMatrix vpm = viewport_matrix(P.vp);
-    clip_emit_kernel<<<grid, block, 0, st>>>(n, P.keep_degenerate, P.draw_id, vpm, P.gen_base, P.gen_tri_cap, P.gen_vert_cap,
+    clip_emit_kernel<<<grid, block, 0, st>>>(n, P.n_verts, P.keep_degenerate, P.draw_id, vpm, P.gen_base, P.gen_tri_cap, P.gen_vert_cap,
                                              m->indices, vs.clip4, vs.scr4, vs.vary, offsets, refs, flags);
 }
 

@@ -44,6 +44,8 @@ struct DeviceFlags {
     unsigned int overflow_bits;   // OVF_* bits
     unsigned int poison_draw;     // id of the first draw that overflowed (atomicMin)
     unsigned int nan_total;       // primitives met with an all-NaN bbox since the last sync
+    unsigned int bad_index;       // a mesh index >= vertex count was met (primitive skipped)
+    unsigned int pad0;
     unsigned long long need_gen_tris;
     unsigned long long need_gen_verts;
     unsigned long long need_entries;
@@ -55,10 +57,12 @@ struct DeviceFlags {
     unsigned long long fragments;
     unsigned long long n_gen_tris;     // raster triangles produced by the geometry stage
     unsigned long long n_gen_verts;
+    unsigned long long n_unsafe_list;  // primitives on the unsafe list (extension pass)
+    unsigned long long n_big;          // primitives on the large-bbox list (opaque path)
     unsigned int nan_bbox;
     unsigned int pad;
 };
-constexpr size_t FLAGS_STATS_OFFSET = 40;
+constexpr size_t FLAGS_STATS_OFFSET = 48;
 static_assert(offsetof(DeviceFlags, triangles_generated) == FLAGS_STATS_OFFSET, "DeviceFlags layout");
 
 enum { OVF_GEN_TRIS = 1, OVF_GEN_VERTS = 2, OVF_ENTRIES = 4, OVF_SORT = 8 };
@@ -85,6 +89,7 @@ struct DrawParams {
     uint32_t mode_b;              // exhaustive raster (stencil events gate fragments)
     uint32_t stencil_active;      // stencil plane changes during this draw
     uint32_t draw_id;             // sequence number of the draw since the last sync
+    uint32_t force_unsafe;        // test hook: treat every primitive as unsafe
 };
 
 // Setup record of a raster triangle (64 bytes):
@@ -166,6 +171,38 @@ __device__ __forceinline__ bool clamp_axis(int i0, int i1, uint32_t p, uint32_t 
     return i0 <= pi && pi <= i1;
 }
 
+// Sound segment test of the extension pass (see sr_setup.cu): true when one of
+// the reference's u, v, w is certainly negative on the whole clamped segment
+// [x0, x1] x [y0, y1] (one of the two ranges is a single coordinate).
+__device__ __forceinline__ bool segment_cleared(float4 r0, float4 r1, uint32_t x0, uint32_t y0, uint32_t x1,
+                                                uint32_t y1) {
+    const float g = 5.0e-7f;
+    const float eps = 6.0e-8f;
+    const float det = r1.z;
+    const float s = det > 0.0f ? 1.0f : -1.0f;
+    float nu[2], nv[2], Su[2], Sv[2];
+    uint32_t xs[2] = {x0, x1}, ys[2] = {y0, y1};
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+        float dx = ((float)xs[e] + 0.5f) - r1.x;
+        float dy = ((float)ys[e] + 0.5f) - r1.y;
+        nu[e] = r0.x * dx + r0.y * dy;
+        nv[e] = r0.z * dx + r0.w * dy;
+        Su[e] = fabsf(r0.x) * fabsf(dx) + fabsf(r0.y) * fabsf(dy);
+        Sv[e] = fabsf(r0.z) * fabsf(dx) + fabsf(r0.w) * fabsf(dy);
+    }
+    float sum = fmaxf(Su[0], Su[1]), svm = fmaxf(Sv[0], Sv[1]);
+    float tiny = fabsf(det) * 1.0e-30f;
+    bool cu = (s * nu[0] + g * sum + tiny < 0.0f) && (s * nu[1] + g * sum + tiny < 0.0f);
+    if (cu) return true;
+    bool cv = (s * nv[0] + g * svm + tiny < 0.0f) && (s * nv[1] + g * svm + tiny < 0.0f);
+    if (cv) return true;
+    float mag = fabsf(det) + fmaxf(fabsf(nu[0]), fabsf(nu[1])) + fmaxf(fabsf(nv[0]), fabsf(nv[1]));
+    float mw = 2.0f * g * (sum + svm) + 16.0f * eps * mag;
+    bool cw = (s * (det - nu[0] - nv[0]) + mw < 0.0f) && (s * (det - nu[1] - nv[1]) + mw < 0.0f);
+    return cw;
+}
+
 }  // namespace sr
 
 // Opaque handles of the C ABI
@@ -202,13 +239,33 @@ void launch_clip(const DrawParams& P, const sr_mesh* m, VertexStore vs, unsigned
                  DeviceFlags* flags, cudaStream_t st);
 void launch_setup_bin(const DrawParams& P, const uint32_t* vidx, VertexStore vs, float4* setup,
                       uint32_t* binrect, uint32_t* bin_counts, uint32_t* bin_off, uint32_t* bin_cursor,
-                      uint32_t* entries, uint32_t* scan_tmp, const StencilCountArgs& S,
-                      DeviceFlags* flags, cudaStream_t st);
-void launch_raster_any(bool ordered, const DrawParams& P, const sr_uniforms& U, const float4* setup,
-                       const uint32_t* bin_off, const uint32_t* entries, const uint32_t* vidx,
-                       const float* vary, const uint32_t* tex, void* color, float* depth,
-                       uint8_t* stencil, uint32_t gate, DeviceFlags* flags, cudaStream_t st);
+                      uint32_t* entries, uint32_t* scan_tmp, uint32_t* unsafe_list,
+                      unsigned long long* area, const StencilCountArgs& S, DeviceFlags* flags, cudaStream_t st);
+
 void launch_stencil_apply(const DrawParams& P, const StencilCountArgs& S, uint8_t* stencil,
                           DeviceFlags* flags, cudaStream_t st);
+
+struct OpaqueArgs {
+    const float4* setup;
+    unsigned long long* area;        // per raster primitive: bbox pixels in the frame (setup output)
+    uint32_t* big_list;              // primitives with more than RG_BIG bbox pixels
+    unsigned long long* gkeys;       // W x H winner keys, zero between draws
+    uint32_t* bitmap;                // touched 32x32 blocks, zero between draws
+    const uint32_t* unsafe_list;
+    const uint32_t* vidx;
+    const float* vary;
+    const uint32_t* tex;
+    void* color;
+    float* depth;
+    const uint8_t* stencil;
+    uint32_t gate;
+    DeviceFlags* flags;
+};
+// Opaque draws (sr_opaque.cu); returns the number of kernels launched.
+int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A, cudaStream_t st);
+// Blending / stencil-gated draws over sorted bins (sr_raster.cu).
+void launch_ordered(const DrawParams& P, const sr_uniforms& U, const float4* setup, const uint32_t* bin_off,
+                    const uint32_t* entries, const uint32_t* vidx, const float* vary, const uint32_t* tex, void* color,
+                    float* depth, uint8_t* stencil, uint32_t gate, DeviceFlags* flags, cudaStream_t st);
 
 }  // namespace sr

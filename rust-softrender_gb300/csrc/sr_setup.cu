@@ -37,19 +37,17 @@ __device__ __forceinline__ void tri_slots(uint32_t t, const uint32_t* __restrict
 }
 
 // Conservative bound of the pixel centres whose computed coverage
-// !(u<0 || v<0 || w<0) can hold (see file comment).  Returns true and leaves
-// eb = bbox when no pixel centre outside the integer bbox can be covered.
+// !(u<0 || v<0 || w<0) can hold (see file comment): true when no pixel centre
+// outside the integer bbox [ix0, ix1] x [iy0, iy1] can be covered.
 __device__ bool inflated_region(float x1, float y1, float x2, float y2, float x3, float y3, float det,
-                                uint32_t W, uint32_t H, int ix0, int iy0, int ix1, int iy1, int eb[4]) {
-    eb[0] = 0; eb[1] = 0; eb[2] = (int)W - 1; eb[3] = (int)H - 1;
+                                uint32_t W, uint32_t H, int ix0, int iy0, int ix1, int iy1) {
     const float BIG = 1.0e6f;
     if (!(fabsf(x1) < BIG && fabsf(x2) < BIG && fabsf(x3) < BIG && fabsf(y1) < BIG && fabsf(y2) < BIG &&
           fabsf(y3) < BIG))
         return false;
     float a = y2 - y3, b = x3 - x2, c = y3 - y1, d = x1 - x3;
-    float ex = (float)W, ey = (float)H;
-    float Rx = fmaxf(fabsf(0.5f - x3), fabsf(ex - x3));
-    float Ry = fmaxf(fabsf(0.5f - y3), fabsf(ey - y3));
+    float Rx = fmaxf(fabsf(0.5f - x3), fabsf((float)W - x3));
+    float Ry = fmaxf(fabsf(0.5f - y3), fabsf((float)H - y3));
     // g >= 2 * gamma_4 (gamma_4 = 4u/(1-4u), u = 2^-24): absolute rounding of
     // the two-product numerators and the determinant, with slack for the
     // float evaluation of these bounds themselves
@@ -65,22 +63,20 @@ __device__ bool inflated_region(float x1, float y1, float x2, float y2, float x3
     float tv = (g * Sv + 1.0e-30f) / Dlo;
     float tw = 2.0f * (g * SD / Dlo + (g * (Su + Sv)) / Dlo + 16.0f * eps);
     if (!(tu < 1.0f && tv < 1.0f && tw < 1.0f)) return false;
+    // vertices of {l_u >= -tu, l_v >= -tv, l_w >= -tw}
     float v1x = x1 + tv * (x1 - x2) + tw * (x1 - x3), v1y = y1 + tv * (y1 - y2) + tw * (y1 - y3);
     float v2x = x2 + tu * (x2 - x1) + tw * (x2 - x3), v2y = y2 + tu * (y2 - y1) + tw * (y2 - y3);
     float v3x = x3 + tu * (x3 - x1) + tv * (x3 - x2), v3y = y3 + tu * (y3 - y1) + tv * (y3 - y2);
     float slack = 1.0e-3f + 4.0e-6f * (fabsf(x1) + fabsf(x2) + fabsf(x3) + fabsf(y1) + fabsf(y2) + fabsf(y3));
     float fx0 = fminf(fminf(v1x, v2x), v3x) - slack, fx1 = fmaxf(fmaxf(v1x, v2x), v3x) + slack;
     float fy0 = fminf(fminf(v1y, v2y), v3y) - slack, fy1 = fmaxf(fmaxf(v1y, v2y), v3y) + slack;
-    if (fx0 > (float)ix0 - 0.5f && fx1 < (float)ix1 + 1.5f && fy0 > (float)iy0 - 0.5f && fy1 < (float)iy1 + 1.5f) {
-        eb[0] = ix0; eb[1] = iy0; eb[2] = ix1; eb[3] = iy1;
-        return true;
-    }
-    // pixel centres px+0.5 in [fx0, fx1] -> px in [floor(fx0-0.5), floor(fx1-0.5)]
-    eb[0] = min(ix0, floor_sat(fx0 - 0.5f, -1, (int)W));
-    eb[1] = min(iy0, floor_sat(fy0 - 0.5f, -1, (int)H));
-    eb[2] = max(ix1, floor_sat(fx1 - 0.5f, -1, (int)W));
-    eb[3] = max(iy1, floor_sat(fy1 - 0.5f, -1, (int)H));
-    return false;
+    // a side only constrains where the frame has pixel centres beyond it
+    // (ix0 etc. are clamped to [-1, W] / [-1, H])
+    bool ok_l = ix0 <= 0 || fx0 > (float)ix0 - 0.5f;
+    bool ok_r = ix1 >= (int)W - 1 || fx1 < (float)ix1 + 1.5f;
+    bool ok_t = iy0 <= 0 || fy0 > (float)iy0 - 0.5f;
+    bool ok_b = iy1 >= (int)H - 1 || fy1 < (float)iy1 + 1.5f;
+    return ok_l && ok_r && ok_t && ok_b;
 }
 
 __device__ __forceinline__ void stencil_count_tri(const DrawParams& P, const StencilCountArgs& S, int ix0,
@@ -128,9 +124,16 @@ __device__ __forceinline__ void stencil_count_tri(const DrawParams& P, const Ste
 __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_host, const uint32_t* __restrict__ vidx,
                                                     const float4* __restrict__ scr4, float4* __restrict__ setup,
                                                     uint2* __restrict__ binrect, uint32_t* __restrict__ bin_counts,
-                                                    StencilCountArgs S, DeviceFlags* flags) {
+                                                    uint32_t* __restrict__ unsafe_list,
+                                                    unsigned long long* __restrict__ area, StencilCountArgs S,
+                                                    DeviceFlags* flags) {
     if (flags->poison) return;
     uint32_t n = n_host ? n_host : (uint32_t)flags->n_gen_tris;
+    if (area) {   // opaque path: bbox pixel counts instead of bins (zero past the last primitive)
+        const uint32_t t0 = blockIdx.x * blockDim.x + threadIdx.x;
+        const uint32_t n_launch = n_host ? n_host : P.gen_tri_cap;
+        if (t0 >= n && t0 < n_launch) area[t0] = 0;
+    }
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const int lane = threadIdx.x & 31;
     uint32_t single_bin = 0xfffffffeu;   // bin of a one-bin primitive (warp aggregation key)
@@ -140,6 +143,8 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
     if (t < n) {
         uint32_t ia, ib, ic;
         tri_slots(t, vidx, ia, ib, ic);
+        bool bad = n_host && (ia >= P.n_verts || ib >= P.n_verts || ic >= P.n_verts);
+        if (bad) { atomicOr(&flags->bad_index, 1u); ia = ib = ic = 0; }
         float4 s0 = __ldg(scr4 + ia), s1 = __ldg(scr4 + ib), s2 = __ldg(scr4 + ic);
         float x1 = s0.x, y1 = s0.y, x2 = s1.x, y2 = s1.y, x3 = s2.x, y3 = s2.y;
         bool culled = false;
@@ -149,7 +154,9 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
             uint32_t winding = neg ? 1u : 2u;
             culled = winding == P.cull;
         }
+        culled = culled || bad;
         uint2 rect = make_uint2(RECT_EMPTY, RECT_EMPTY);
+        if (area) area[t] = 0;
         // every primitive gets a record flag word (mode B walks all of them)
         setup[4 * (size_t)t + 2] = make_float4(0.0f, 0.0f, __uint_as_float(0u), 0.0f);
         if (!culled) {
@@ -165,15 +172,10 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
                 if (P.stencil_active && !P.mode_b) stencil_count_tri(P, S, ix0, iy0, ix1, iy1);
                 bool no_frag = det == 0.0f || isnan(det) || (s0.z >= 0.0f && s1.z >= 0.0f && s2.z >= 0.0f);
                 if (!no_frag || P.mode_b) {
-                    int eb[4];
-                    bool safe = false;
-                    if (P.mode_b) {
-                        eb[0] = 0; eb[1] = 0; eb[2] = W - 1; eb[3] = H - 1;
-                    } else {
-                        safe = inflated_region(x1, y1, x2, y2, x3, y3, det, P.W, P.H, ix0, iy0, ix1, iy1, eb);
-                    }
-                    int qx0 = max(eb[0], 0), qy0 = max(eb[1], 0), qx1 = min(eb[2], W - 1), qy1 = min(eb[3], H - 1);
-                    if (qx0 <= qx1 && qy0 <= qy1) {
+                    bool safe = !P.mode_b && !P.force_unsafe && inflated_region(x1, y1, x2, y2, x3, y3, det, P.W, P.H, ix0, iy0, ix1, iy1);
+                    int qx0 = max(ix0, 0), qy0 = max(iy0, 0), qx1 = min(ix1, W - 1), qy1 = min(iy1, H - 1);
+                    bool b_in = qx0 <= qx1 && qy0 <= qy1;
+                    if (b_in || !safe) {
                         float4* r = setup + 4 * (size_t)t;
                         r[0] = make_float4(y2 - y3, x3 - x2, y3 - y1, x1 - x3);
                         r[1] = make_float4(x3, y3, det, s0.z);
@@ -183,12 +185,24 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
                                            __int_as_float(iy1));
                         n_raster = 1;
                         n_unsafe = safe ? 0 : 1;
-                        if (!P.mode_b) {
-                            rx0 = (uint32_t)qx0 >> P.bin_w_log2; rx1 = (uint32_t)qx1 >> P.bin_w_log2;
-                            ry0 = (uint32_t)qy0 >> P.bin_h_log2; ry1 = (uint32_t)qy1 >> P.bin_h_log2;
-                            rect = make_uint2(rx0 | (ry0 << 16), rx1 | (ry1 << 16));
-                            n_entries = (unsigned long long)(rx1 - rx0 + 1) * (ry1 - ry0 + 1);
-                            if (rx0 == rx1 && ry0 == ry1) single_bin = ry0 * P.bins_x + rx0;
+                        if (area) {
+                            area[t] = b_in ? (unsigned long long)(qx1 - qx0 + 1) * (unsigned long long)(qy1 - qy0 + 1) : 0ull;
+                            if (!safe) {
+                                unsigned long long k = atomicAdd(&flags->n_unsafe_list, 1ull);
+                                unsafe_list[k] = t;
+                            }
+                        } else if (!P.mode_b) {
+                            if (b_in) {
+                                rx0 = (uint32_t)qx0 >> P.bin_w_log2; rx1 = (uint32_t)qx1 >> P.bin_w_log2;
+                                ry0 = (uint32_t)qy0 >> P.bin_h_log2; ry1 = (uint32_t)qy1 >> P.bin_h_log2;
+                                rect = make_uint2(rx0 | (ry0 << 16), rx1 | (ry1 << 16));
+                                n_entries = (unsigned long long)(rx1 - rx0 + 1) * (ry1 - ry0 + 1);
+                                if (rx0 == rx1 && ry0 == ry1) single_bin = ry0 * P.bins_x + rx0;
+                            }
+                            if (!safe) {
+                                unsigned long long k = atomicAdd(&flags->n_unsafe_list, 1ull);
+                                unsafe_list[k] = t;
+                            }
                         }
                     }
                 }
@@ -256,6 +270,93 @@ __global__ void __launch_bounds__(256) bin_fill_kernel(DrawParams P, uint32_t n_
     }
 }
 
+
+// ------------------------------------------------------- extension pass
+// An unsafe primitive can produce fragments outside its bbox, but only at
+// the pixels where the reference evaluates it there: the projection of its
+// bbox onto each semantic tile it does not overlap (a column segment, a row
+// segment or a corner pixel on that tile's edge).  For each such segment a
+// sound sign test clears the whole segment when one of u, v, w is certainly
+// negative on it; remaining pixels are evaluated exactly (the reference's
+// expressions), and the primitive is added to the bin of every pixel that
+// yields a fragment, unless that bin already lists it.
+//
+// Sign test: the reference's numerator n_u(P) differs from the exact edge
+// function N_u(P) by at most gamma_4 * S_u(P), S_u = |y2-y3||x-x3| + |x3-x2||y-y3|
+// (convex on the segment, so its maximum is at an end point).  N_u is affine,
+// so s*n_u(end) + 2 gamma_4 max S_u < 0 at both ends (s = sign of the computed
+// det) makes u < 0 on the whole segment; v likewise.  For w = (1-u)-v the
+// quantity det - N_u - N_v is affine and w < 0 follows when it is negative
+// beyond the numerator errors plus 8 eps |det| (the roundings of the two
+// quotients and two subtractions while u, v lie in [0, 2]; outside that range
+// u < 0, v < 0 or w < 0 holds anyway).
+__device__ __forceinline__ uint32_t clampu(int v, uint32_t lo, uint32_t hi) {
+    return v < (int)lo ? lo : (v > (int)hi ? hi : (uint32_t)v);
+}
+
+template <bool FILL>
+__global__ void __launch_bounds__(256) ext_kernel(DrawParams P, const uint32_t* __restrict__ unsafe_list,
+                                                  const float4* __restrict__ setup, const uint2* __restrict__ binrect,
+                                                  uint32_t* __restrict__ bin_counts, const uint32_t* __restrict__ bin_off,
+                                                  uint32_t* __restrict__ cursor, uint32_t* __restrict__ entries,
+                                                  uint64_t entry_cap, DeviceFlags* flags) {
+    if (flags->poison) return;
+    const uint32_t nu = (uint32_t)flags->n_unsafe_list;
+    const uint32_t ntiles = P.ncols * P.nrows;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long emitted = 0;
+    for (uint32_t k = warp; k < nu; k += nwarps) {
+        const uint32_t t = unsafe_list[k];
+        const float4* r = setup + 4 * (size_t)t;
+        const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+        const int ix0 = __float_as_int(r3.x), iy0 = __float_as_int(r3.y);
+        const int ix1 = __float_as_int(r3.z), iy1 = __float_as_int(r3.w);
+        const uint2 br = binrect[t];
+        const bool has_rect = br.x != RECT_EMPTY;
+        const uint32_t bx0 = br.x & 0xffffu, by0 = br.x >> 16, bx1 = br.y & 0xffffu, by1 = br.y >> 16;
+        for (uint32_t ti = lane; ti < ntiles; ti += 32) {
+            const uint32_t C = ti % P.ncols, R = ti / P.ncols;
+            const uint32_t lx = C * P.tile_w, hx = min((C + 1) * P.tile_w, P.W - 1);
+            const uint32_t ly = R * P.tile_h, hy = min((R + 1) * P.tile_h, P.H - 1);
+            const bool ox = ix1 >= (int)lx && ix0 <= (int)hx;
+            const bool oy = iy1 >= (int)ly && iy0 <= (int)hy;
+            if (ox && oy) continue;   // bbox meets the tile: those pixels lie in the bbox bins
+            const uint32_t cx0 = clampu(ix0, lx, hx), cx1 = clampu(ix1, lx, hx);
+            const uint32_t cy0 = clampu(iy0, ly, hy), cy1 = clampu(iy1, ly, hy);
+            if (segment_cleared(r0, r1, cx0, cy0, cx1, cy1)) continue;
+            uint32_t last_b = 0xffffffffu;
+            for (uint32_t py = cy0; py <= cy1; ++py) {
+                for (uint32_t px = cx0; px <= cx1; ++px) {
+                    float x = (float)px + 0.5f, y = (float)py + 0.5f;
+                    float dx = x - r1.x, dy = y - r1.y;
+                    float u = (r0.x * dx + r0.y * dy) / r1.z;
+                    float v = (r0.z * dx + r0.w * dy) / r1.z;
+                    float w = 1.0f - u - v;
+                    if (u < 0.0f || v < 0.0f || w < 0.0f) continue;
+                    float z = (r1.w * u + r2.x * v) + r2.y * w;
+                    if (!(z < 0.0f)) continue;
+                    const uint32_t bxx = px >> P.bin_w_log2, byy = py >> P.bin_h_log2;
+                    if (has_rect && bxx >= bx0 && bxx <= bx1 && byy >= by0 && byy <= by1) continue;
+                    const uint32_t b = byy * P.bins_x + bxx;
+                    if (b == last_b) continue;
+                    last_b = b;
+                    if (FILL) {
+                        uint32_t pos = atomicAdd(cursor + b, 1u);
+                        uint64_t at = (uint64_t)bin_off[b] + pos;
+                        if (at < entry_cap) entries[at] = t;
+                    } else {
+                        atomicAdd(bin_counts + b, 1u);
+                        ++emitted;
+                    }
+                }
+            }
+        }
+    }
+    if (!FILL && emitted) atomicAdd(&flags->entries, emitted);
+}
+
 __global__ void check_entries_kernel(uint32_t n_bins, const uint32_t* bin_off, uint64_t entry_cap, uint32_t draw_id,
                                      DeviceFlags* flags) {
     if (flags->poison) return;
@@ -269,19 +370,32 @@ __global__ void check_entries_kernel(uint32_t n_bins, const uint32_t* bin_off, u
 
 void launch_setup_bin(const DrawParams& P, const uint32_t* vidx, VertexStore vs, float4* setup, uint32_t* binrect,
                       uint32_t* bin_counts, uint32_t* bin_off, uint32_t* bin_cursor, uint32_t* entries,
-                      uint32_t* scan_tmp, const StencilCountArgs& S, DeviceFlags* flags, cudaStream_t st) {
+                      uint32_t* scan_tmp, uint32_t* unsafe_list, unsigned long long* area, const StencilCountArgs& S,
+                      DeviceFlags* flags, cudaStream_t st) {
     uint32_t n_bins = P.bins_x * P.bins_y;
     uint32_t n_host = P.n_raster_host;
     uint32_t n_launch = n_host ? n_host : P.gen_tri_cap;
+    dim3 block(256), grid((n_launch + 255) / 256 ? (n_launch + 255) / 256 : 1);
+    if (area) {   // opaque path: no bins
+        setup_kernel<<<grid, block, 0, st>>>(P, n_host, vidx, vs.scr4, setup, reinterpret_cast<uint2*>(binrect),
+                                             bin_counts, unsafe_list, area, S, flags);
+        return;
+    }
     cudaMemsetAsync(bin_counts, 0, (size_t)n_bins * 4, st);
     cudaMemsetAsync(bin_cursor, 0, (size_t)n_bins * 4, st);
-    dim3 block(256), grid((n_launch + 255) / 256 ? (n_launch + 255) / 256 : 1);
     setup_kernel<<<grid, block, 0, st>>>(P, n_host, vidx, vs.scr4, setup, reinterpret_cast<uint2*>(binrect),
-                                         bin_counts, S, flags);
+                                         bin_counts, unsafe_list, nullptr, S, flags);
+    const uint2* br = reinterpret_cast<const uint2*>(binrect);
+    const dim3 ext_grid(4 * 152);
+    if (!P.mode_b)
+        ext_kernel<false><<<ext_grid, block, 0, st>>>(P, unsafe_list, setup, br, bin_counts, bin_off, bin_cursor,
+                                                      entries, P.entry_cap, flags);
     exclusive_scan<uint32_t>(bin_counts, n_bins, bin_off, scan_tmp, st);
     check_entries_kernel<<<1, 1, 0, st>>>(n_bins, bin_off, P.entry_cap, P.draw_id, flags);
-    bin_fill_kernel<<<grid, block, 0, st>>>(P, n_host, reinterpret_cast<const uint2*>(binrect), bin_off, bin_cursor,
-                                            entries, P.entry_cap, flags);
+    bin_fill_kernel<<<grid, block, 0, st>>>(P, n_host, br, bin_off, bin_cursor, entries, P.entry_cap, flags);
+    if (!P.mode_b)
+        ext_kernel<true><<<ext_grid, block, 0, st>>>(P, unsafe_list, setup, br, bin_counts, bin_off, bin_cursor,
+                                                     entries, P.entry_cap, flags);
 }
 
 }  // namespace sr

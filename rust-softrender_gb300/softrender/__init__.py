@@ -80,6 +80,15 @@ class Mesh:
         self.n_verts = n
         self.n_indices = int(idx.size)
 
+    def update(self, planes, indices, stream_ptr=None):
+        """Copies new host data of the same shape into the device mesh."""
+        planes = [np.ascontiguousarray(p, dtype=np.float32) for p in planes]
+        idx = np.ascontiguousarray(indices, dtype=np.uint32)
+        arr = (C.c_void_p * max(1, len(planes)))(*[p.ctypes.data for p in planes])
+        check(lib().sr_mesh_update(self.handle, arr, len(planes), planes[0].shape[0] if planes else 0,
+                                   idx.ctypes.data if idx.size else None, idx.size,
+                                   C.c_void_p(stream_ptr) if stream_ptr else None), "sr_mesh_update")
+
     @property
     def nbytes(self):
         return int(lib().sr_mesh_bytes(self.handle))
@@ -103,6 +112,11 @@ class Texture:
         check(lib().sr_texture_upload(t.ctypes.data, t.shape[1], t.shape[0], C.byref(h)), "sr_texture_upload")
         self.handle = h
         self.width, self.height = t.shape[1], t.shape[0]
+
+    def update(self, rgba8, stream_ptr=None):
+        t = np.ascontiguousarray(rgba8, dtype=np.uint32)
+        check(lib().sr_texture_update(self.handle, t.ctypes.data, t.shape[1], t.shape[0],
+                                      C.c_void_p(stream_ptr) if stream_ptr else None), "sr_texture_update")
 
     def free(self):
         if self.handle:
@@ -186,10 +200,15 @@ class Pipeline:
     def sync(self):
         return lib().sr_sync(self.handle)
 
+    def set_profiling(self, enable=True):
+        check(lib().sr_pipeline_set_profiling(self.handle, 1 if enable else 0), "sr_pipeline_set_profiling")
+
     def stats(self):
         s = A.SrStats()
         check(lib().sr_get_stats(self.handle, C.byref(s)), "sr_get_stats")
-        return {f: getattr(s, f) for f, _ in A.SrStats._fields_}
+        out = {f: getattr(s, f) for f, _ in A.SrStats._fields_ if f != "stage_ms"}
+        out["stage_ms"] = dict(zip(A.STAGE_NAMES, list(s.stage_ms))) if s.profiled else {}
+        return out
 
     def render_mesh(self, primitive, mesh, stencil=None):
         """Pipeline::render_mesh (mod.rs:146-155) -> VertexShader."""

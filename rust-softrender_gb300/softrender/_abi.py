@@ -73,4 +73,7 @@ class SrStats(C.Structure):
         ("triangles_raster", C.c_uint64), ("unsafe_triangles", C.c_uint64),
         ("bin_entries", C.c_uint64), ("fragments", C.c_uint64),
         ("nan_bbox", C.c_uint32), ("overflow", C.c_uint32),
+        ("kernel_launches", C.c_uint32), ("profiled", C.c_uint32), ("stage_ms", C.c_float * 6),
     ]
+
+STAGE_NAMES = ("vertex", "geometry", "setup_bin", "raster", "stencil", "total")

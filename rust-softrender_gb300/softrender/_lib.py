@@ -18,6 +18,7 @@ SIGNATURES = {
     "sr_pipeline_set_stencil": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int]),
     "sr_pipeline_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sr_pipeline_destroy": (C.c_int, [C.c_void_p]),
+    "sr_pipeline_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "sr_framebuffer_clear": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sr_framebuffer_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sr_framebuffer_write": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
@@ -25,9 +26,12 @@ SIGNATURES = {
                                              C.POINTER(C.c_void_p)]),
     "sr_mesh_upload": (C.c_int, [C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_void_p, C.c_uint64,
                                  C.POINTER(C.c_void_p)]),
+    "sr_mesh_update": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_uint32, C.c_uint32, C.c_void_p,
+                                 C.c_uint64, C.c_void_p]),
     "sr_mesh_free": (C.c_int, [C.c_void_p]),
     "sr_mesh_bytes": (C.c_uint64, [C.c_void_p]),
     "sr_texture_upload": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_void_p)]),
+    "sr_texture_update": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
     "sr_texture_free": (C.c_int, [C.c_void_p]),
     "sr_shader_lookup": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int)]),
     "sr_draw_init": (None, [C.POINTER(A.SrDraw)]),

@@ -391,6 +391,38 @@ def stress_scene(n_tiny=16777216, n_large=4096, size=2048, seed=6, seed_large=7,
     return sc
 
 
+def sliver_scene(n=4000, size=256, seed=9, **kw):
+    """Nearly collinear triangles (perpendicular offsets 1e-7..1e-2 px, lengths
+    up to half the frame) in clip space with w = 1: their computed barycentric
+    coordinates are dominated by rounding, which exercises the exact handling
+    of coverage outside the bounding box."""
+    rng = np.random.default_rng(seed)
+    W = H = size
+    p0 = rng.uniform(-0.1 * size, 1.1 * size, (n, 2))
+    ang = rng.uniform(0.0, 2.0 * math.pi, n)
+    length = np.exp(rng.uniform(math.log(0.5), math.log(0.5 * size), n))
+    d = np.stack([np.cos(ang), np.sin(ang)], 1)
+    nrm = np.stack([-d[:, 1], d[:, 0]], 1)
+    off = np.exp(rng.uniform(math.log(1e-7), math.log(1e-2), n)) * rng.choice([-1.0, 1.0], n)
+    t2 = rng.uniform(0.05, 0.95, n)
+    v0 = p0
+    v1 = p0 + d * length[:, None]
+    v2 = p0 + d * (length * t2)[:, None] + nrm * off[:, None]
+    tri = np.stack([v0, v1, v2], 1)
+    z = rng.uniform(-0.9, 0.9, (n, 3))
+    x, y, zz = _clip_from_screen(tri[:, :, 0].reshape(-1), tri[:, :, 1].reshape(-1), z.reshape(-1), W, H)
+    col = rng.integers(0, 256, (3 * n, 3))
+    packed = _pack_rgba8(col[:, 0], col[:, 1], col[:, 2], np.full(3 * n, 255))
+    planes = [np.ascontiguousarray(x, dtype=np.float32), np.ascontiguousarray(y, dtype=np.float32),
+              np.ascontiguousarray(zz, dtype=np.float32), packed.view(np.float32).copy()]
+    sc = Scene(planes=planes, indices=np.arange(3 * n, dtype=np.uint32), width=W, height=H,
+               color_format=A.SR_COLOR_RGBA8, vs="clip_rgba8", fs="vertex_color", tile=(32, 32),
+               name="slivers_%d_%d" % (n, size))
+    for k, val in kw.items():
+        setattr(sc, k, val)
+    return sc
+
+
 def random_camera(rng, dist_lo=2.0, dist_hi=6.0):
     d = rng.uniform(dist_lo, dist_hi)
     th = rng.uniform(0.2, math.pi - 0.2)

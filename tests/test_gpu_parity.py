@@ -121,3 +121,60 @@ def test_blend_over_f32(built_lib, oracle_mod):
     sc.color_format = A.SR_COLOR_RGBA32F
     sc.stencil = False
     check(sc, oracle_mod)
+
+
+# ------------------------------------------------- rounding-dominated slivers
+@pytest.mark.parametrize("blend", ["replace", "over"])
+def test_slivers(built_lib, oracle_mod, blend):
+    """Nearly collinear primitives whose coverage outside the bbox is decided
+    by rounding: the unsafe classification and extension pass must reproduce
+    the reference's tile-edge fragments exactly."""
+    sc = scenes.sliver_scene(n=3000, size=256, blend=blend)
+    stats, _ = check(sc, oracle_mod)
+    assert stats["unsafe_triangles"] > 0
+
+
+def test_slivers_stencil(built_lib, oracle_mod):
+    sc = scenes.sliver_scene(n=1500, size=160, stencil=True, stencil_test=A.SR_STENCIL_ALWAYS,
+                             stencil_op=A.SR_STENCIL_INCREMENT, stencil_wrap=0, tile=(24, 40))
+    check(sc, oracle_mod)
+
+
+@pytest.fixture
+def force_unsafe():
+    import os
+    os.environ["SR_FORCE_UNSAFE"] = "1"
+    yield
+    del os.environ["SR_FORCE_UNSAFE"]
+
+
+@pytest.mark.parametrize("make", [
+    lambda: scenes.sliver_scene(n=800, size=200, seed=3),
+    lambda: scenes.icosphere_scene(180, 140, tile=(32, 24), subdiv=3),
+    lambda: scenes.stress_scene(n_tiny=800, n_large=12, size=128, tile=(24, 40)),
+    lambda: scenes.grid_sphere_scene(width=256, height=144, n_lat=16, n_lon=32, tex_size=32, tile=(40, 32)),
+])
+def test_forced_unsafe_path(built_lib, oracle_mod, force_unsafe, make):
+    """Every primitive through the unsafe path: bbox bins plus the exact
+    evaluation of its clamped tile-edge targets (extension pass)."""
+    stats, _ = check(make(), oracle_mod)
+    assert stats["unsafe_triangles"] == stats["triangles_raster"] > 0
+
+
+@pytest.mark.parametrize("size,n", [(64, 20000), (96, 60000)])
+def test_dense_overlap(built_lib, oracle_mod, size, n):
+    """Thousands of primitives per pixel block: many concurrent 64-bit atomicMax
+    reductions on the same pixels must still select the reference's winner."""
+    sc = scenes.stress_scene(n_tiny=n, n_large=3, size=size, blend="replace", tile=(20, 24))
+    sc.stencil = False
+    stats, _ = check(sc, oracle_mod)
+    assert stats["fragments"] > n // 4
+
+
+def test_dense_bins_depth_ties(built_lib, oracle_mod):
+    """Equal depths everywhere: the last primitive in submission order wins."""
+    sc = scenes.stress_scene(n_tiny=30000, n_large=0, size=64, blend="replace", tile=(16, 16))
+    sc.stencil = False
+    z = sc.planes[2]
+    z[:] = np.float32(0.25)
+    check(sc, oracle_mod)
