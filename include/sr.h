@@ -244,6 +244,53 @@ SR_API int sr_sync(sr_pipeline* p);
 /* Counters of the most recent sr_render (valid after sr_sync). */
 SR_API int sr_get_stats(sr_pipeline* p, sr_stats* out);
 
+/* ---------------------------------------------------- allocation-free draw
+ * sr_render_static has no counterpart in the reference.  It is for callers
+ * that cannot let a library allocate device memory: an application whose own
+ * allocator owns the GPU's memory, a real-time loop that cannot afford
+ * cudaMalloc/cudaFree (and the device synchronisation they imply) inside a
+ * frame, or a plugin given nothing but device pointers.  It draws one opaque
+ * (blend "replace"), indexed triangle mesh with no geometry shader
+ * (gs_mode SR_GS_NONE, as the sr_render chain run_to_fragment) and no stencil
+ * attachment, producing the framebuffer sr_render produces for the same draw,
+ * and it calls no cudaMalloc, cudaFree or other allocating routine.
+ *
+ * Inputs and outputs are caller-owned DEVICE pointers:
+ *   planes   n_planes attribute planes, plane j at planes + j * plane_stride
+ *            (plane_stride a multiple of 4, >= n_verts; planes 16-byte aligned)
+ *   indices  3 * n_triangles vertex indices; a triangle with an index >=
+ *            n_verts draws nothing (this call does not wait for the GPU, so,
+ *            unlike sr_sync, it cannot report that)
+ *   texture  tex_w * tex_h RGBA8 texels (textured_blinn_phong only, else NULL)
+ *   color    width * height pixels of fb->color_format (16-byte aligned for
+ *            RGBA32F); depth: width * height f32 when fb->depth.  They are
+ *            drawn into as they are: clearing them is the caller's job.
+ * d->mesh and d->texture must be NULL; uniforms are an sr_uniforms.  Work is
+ * enqueued on `stream` (NULL: the legacy default stream); the call returns
+ * without waiting.
+ *
+ * Limits: width * height <= SR_STATIC_MAX_PIXELS, n_triangles <=
+ * SR_STATIC_MAX_TRIANGLES, n_verts <= SR_STATIC_MAX_VERTICES; larger draws
+ * return SR_EOVERFLOW without doing anything (use sr_render for them).  The
+ * scratch is one fixed array of about 17.5 MiB in the library's device image,
+ * held by every GPU that loads the library until the process exits.  Each
+ * call clears the parts of it that must start at zero.
+ *
+ * All calls on a device share that one array: two calls whose work overlaps
+ * on the GPU (different streams, or different host threads, without an
+ * ordering between them) race and corrupt each other's output.  Order them
+ * on one stream or with events.  The first call on each device looks up the
+ * array's device address (cudaGetSymbolAddress, with that device current);
+ * make that first call before any stream capture begins. */
+#define SR_STATIC_MAX_PIXELS    (1u << 20)
+#define SR_STATIC_MAX_TRIANGLES (1u << 16)
+#define SR_STATIC_MAX_VERTICES  (1u << 16)
+SR_API int sr_render_static(const sr_draw* d, const void* uniforms, size_t uniforms_size,
+                            const float* planes, uint32_t n_planes, uint32_t plane_stride, uint32_t n_verts,
+                            const uint32_t* indices, uint32_t n_triangles,
+                            const uint32_t* texture, uint32_t tex_w, uint32_t tex_h,
+                            const sr_fb_desc* fb, void* color, float* depth, void* stream);
+
 /* Human-readable name of a status code. */
 SR_API const char* sr_status_string(int status);
 /* Library version, e.g. "softrender-gb300 0.1.0 sm_103a". */

@@ -13,6 +13,8 @@ SR_COLOR_NONE, SR_COLOR_RGBA32F, SR_COLOR_RGBA8 = 0, 1, 2
 SR_PRIM_POINT, SR_PRIM_LINE, SR_PRIM_TRIANGLE = 1, 2, 3
 # sr_gs_mode
 SR_GS_NONE, SR_GS_CLIP, SR_GS_NAMED = 0, 1, 2
+# limits of sr_render_static (its fixed scratch)
+SR_STATIC_MAX_PIXELS, SR_STATIC_MAX_TRIANGLES, SR_STATIC_MAX_VERTICES = 1 << 20, 1 << 16, 1 << 16
 # sr_cull
 SR_CULL_NONE, SR_CULL_CLOCKWISE, SR_CULL_COUNTER_CLOCKWISE = 0, 1, 2
 # sr_stencil_test

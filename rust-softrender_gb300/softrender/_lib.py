@@ -38,6 +38,9 @@ SIGNATURES = {
     "sr_render": (C.c_int, [C.c_void_p, C.POINTER(A.SrDraw)]),
     "sr_sync": (C.c_int, [C.c_void_p]),
     "sr_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.SrStats)]),
+    "sr_render_static": (C.c_int, [C.POINTER(A.SrDraw), C.c_void_p, C.c_size_t, C.c_void_p, C.c_uint32, C.c_uint32,
+                                   C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32,
+                                   C.POINTER(A.SrFbDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
     "sr_status_string": (C.c_char_p, [C.c_int]),
     "sr_version": (C.c_char_p, []),
 }
