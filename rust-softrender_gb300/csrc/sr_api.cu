@@ -7,6 +7,7 @@
 // kernel of that draw and of later draws skips.  sr_sync() then grows the
 // buffers and replays the draws from the first poisoned one, so the
 // framebuffer always ends up exactly as if capacities had been large enough.
+#include <algorithm>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -118,13 +119,17 @@ const ShaderName kShaders[] = {
     {"over", SR_STAGE_BLEND, BLEND_OVER},
 };
 
-__global__ void fill_u32_kernel(uint32_t* p, size_t n, uint32_t v) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = v;
-}
-__global__ void fill_f4_kernel(float4* p, size_t n, float4 v) {
-    size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) p[i] = v;
+// Clears a colour plane (cn 32-bit words, pattern cv repeating every 4 words)
+// and a depth plane (dn words of dv) with 16-byte stores in one launch.
+__global__ void clear_planes_kernel(uint32_t* __restrict__ c, size_t cn, uint4 cv, uint32_t* __restrict__ d, size_t dn,
+                                    uint32_t dv) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    const size_t c4 = cn / 4, d4 = dn / 4;
+    const uint4 dv4 = make_uint4(dv, dv, dv, dv);
+    for (size_t j = i; j < c4; j += stride) reinterpret_cast<uint4*>(c)[j] = cv;
+    for (size_t j = i; j < d4; j += stride) reinterpret_cast<uint4*>(d)[j] = dv4;
+    if (i < cn - 4 * c4) c[4 * c4 + i] = (&cv.x)[i & 3];
+    if (i < dn - 4 * d4) d[4 * d4 + i] = dv;
 }
 
 int fs_min_varyings(int fs) {
@@ -276,22 +281,26 @@ extern "C" SR_API int sr_pipeline_set_stream(sr_pipeline* p, void* stream) {
 extern "C" SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color) {
     if (!p || !color) return SR_EINVAL;
     size_t n = (size_t)p->fb.width * p->fb.height;
-    dim3 b(256), g((unsigned)((n + 255) / 256));
+    uint4 cv = make_uint4(0, 0, 0, 0);
+    size_t cn = 0;
     if (p->fb.color_format == SR_COLOR_RGBA32F) {
-        float4 c;
-        std::memcpy(&c, color, 16);
-        fill_f4_kernel<<<g, b, 0, p->stream>>>(reinterpret_cast<float4*>(p->color), n, c);
+        std::memcpy(&cv, color, 16);
+        cn = 4 * n;
     } else if (p->fb.color_format == SR_COLOR_RGBA8) {
         uint32_t c;
         std::memcpy(&c, color, 4);
-        fill_u32_kernel<<<g, b, 0, p->stream>>>(reinterpret_cast<uint32_t*>(p->color), n, c);
+        cv = make_uint4(c, c, c, c);
+        cn = n;
     }
-    if (p->depth) {
-        float far_ = -3.40282347e+38f;  // f32::MIN (attachments/depth.rs:31)
-        uint32_t fb;
-        std::memcpy(&fb, &far_, 4);
-        fill_u32_kernel<<<g, b, 0, p->stream>>>(reinterpret_cast<uint32_t*>(p->depth), n, fb);
-    }
+    const float far_ = -3.40282347e+38f;  // f32::MIN (attachments/depth.rs:31)
+    uint32_t dv;
+    std::memcpy(&dv, &far_, 4);
+    const size_t dn = p->depth ? n : 0;
+    const size_t work = std::max(cn, dn) / 4 + 4;
+    const unsigned grid = (unsigned)std::min<size_t>((work + 255) / 256, 152 * 16);
+    if (cn || dn)
+        clear_planes_kernel<<<grid, 256, 0, p->stream>>>(reinterpret_cast<uint32_t*>(p->color), cn, cv,
+                                                         reinterpret_cast<uint32_t*>(p->depth), dn, dv);
     if (p->stencil) SR_CK(cudaMemsetAsync(p->stencil, 0, n, p->stream));
     SR_CK(cudaGetLastError());
     return SR_OK;

@@ -40,11 +40,20 @@ __device__ __forceinline__ void mark_touched(uint32_t* bitmap, uint32_t blocks_x
     if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);   // a stale read only costs an extra atomic
 }
 
-// Tile span of a coordinate: first tile index and 1 or 2 tiles (seam).
-__device__ __forceinline__ int kp_of(const DrawParams& P, uint32_t px, uint32_t py) {
-    TileSpan cs = tiles_of(px, P.tile_w, P.ncols, P.W - 1);
-    TileSpan rs = tiles_of(py, P.tile_h, P.nrows, P.H - 1);
-    return cs.count * rs.count;
+// ceil(2^32 / t): floor(p / t) == __umulhi(p, m) for p, t < 2^16
+__device__ __forceinline__ uint32_t div_magic(uint32_t t) { return (uint32_t)((0x100000000ull + t - 1) / t); }
+// number of semantic tiles along one axis containing coordinate p (1 or 2)
+__device__ __forceinline__ int seam_count(uint32_t p, uint32_t t, uint32_t m, uint32_t last) {
+    return (p > 0 && p < last && __umulhi(p, m) * t == p) ? 2 : 1;
+}
+// mark the 32x32 blocks of a clamped bbox as touched
+__device__ __forceinline__ void mark_rect(uint32_t* bitmap, uint32_t blocks_x, uint32_t x0, uint32_t y0, uint32_t x1,
+                                          uint32_t y1) {
+    for (uint32_t by = y0 >> TOUCH_LOG2; by <= (y1 >> TOUCH_LOG2); ++by)
+        for (uint32_t bx = x0 >> TOUCH_LOG2; bx <= (x1 >> TOUCH_LOG2); ++bx) {
+            const uint32_t b = by * blocks_x + bx, bit = 1u << (b & 31);
+            if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);
+        }
 }
 
 // Exact test of one (primitive, pixel) item; emits the fragment key.
@@ -52,7 +61,7 @@ __device__ __forceinline__ void rg_fragment(const DrawParams& P, float4 r0, floa
                                             uint32_t px, uint32_t py, uint32_t N,
                                             unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap,
                                             const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
-                                            unsigned long long& frags) {
+                                            uint32_t mx, uint32_t my, unsigned long long& frags) {
     const float x = (float)px + 0.5f, y = (float)py + 0.5f;
     const float dx = x - r1.x, dy = y - r1.y;
     const float nu = r0.x * dx + r0.y * dy;
@@ -66,19 +75,20 @@ __device__ __forceinline__ void rg_fragment(const DrawParams& P, float4 r0, floa
     if (!(z < 0.0f)) return;
     const size_t gi = (size_t)py * P.W + px;
     if (gate_with_stencil && !stencil_test(P.stencil_test, __ldg(stencil + gi), P.sref)) return;
-    const int kp = kp_of(P, px, py);
+    const int kp = seam_count(px, P.tile_w, mx, P.W - 1) * seam_count(py, P.tile_h, my, P.H - 1);
     ++frags;
     const uint32_t zk = P.has_depth ? zkey(z) : 0u;
     atomicMax(gkeys + gi, ((unsigned long long)zk << 32) | (unsigned long long)((uint32_t)(kp - 1) * N + t + 1u));
-    mark_touched(bitmap, (P.W + 31) >> 5, px, py);
 }
 
 constexpr uint32_t RG_BIG = 2048;   // bbox pixels above which a primitive goes to the block-cooperative pass
 
-// Each warp takes 32 consecutive primitives; their bbox pixels are flattened
-// into items spread over the lanes (warp prefix sum of the pixel counts and a
-// 5-step shuffle search for each lane's owner), so adjacent lanes test
-// adjacent pixels.  Records are staged in shared memory per warp.
+// Each warp takes G consecutive primitives (G a power of two <= 32, chosen by
+// the host so that small meshes still spread over every SM); their bbox pixels
+// are flattened into items spread over the lanes (warp prefix sum of the pixel
+// counts and a log2(G)-step shuffle search for each lane's owner), so adjacent
+// lanes test adjacent pixels.  Records are staged in shared memory per warp.
+template <uint32_t G>
 __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
     DrawParams P, const float4* __restrict__ setup, const unsigned long long* __restrict__ area,
     unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap, const uint8_t* __restrict__ stencil,
@@ -93,10 +103,12 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long frags = 0;
-    for (uint32_t t0 = warp * 32; t0 < N; t0 += nwarps * 32) {
+    const uint32_t mx = div_magic(P.tile_w), my = div_magic(P.tile_h);
+    const uint32_t blocks_x = (P.W + 31) >> 5;
+    for (uint32_t t0 = warp * G; t0 < N; t0 += nwarps * G) {
         const uint32_t t = t0 + lane;
         uint32_t a = 0;
-        if (t < N) {
+        if (lane < G && t < N) {
             const unsigned long long at = area[t];
             if (at > RG_BIG) {
                 big_list[atomicAdd(&flags->n_big, 1ull)] = t;
@@ -110,7 +122,9 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
                 const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
                 const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
                 const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)P.W - 1);
+                const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1);
                 const uint32_t w = x1 - x0 + 1;
+                mark_rect(bitmap, blocks_x, x0, y0, x1, y1);
                 sxy[wl][lane] = x0 | (y0 << 16);
                 sw[wl][lane] = w;
                 smag[wl][lane] = ((1ull << 32) + w - 1) / w;
@@ -124,10 +138,10 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
             const uint32_t q = base + lane;
             uint32_t lo = 0;
 #pragma unroll
-            for (uint32_t step = 16; step >= 1; step >>= 1) {
+            for (uint32_t step = G >> 1; step >= 1; step >>= 1) {
                 const uint32_t c = lo + step;
                 const uint32_t v = __shfl_sync(0xffffffffu, ex, c & 31u);
-                if (c < 32 && v <= q) lo = c;
+                if (c < G && v <= q) lo = c;
             }
             const uint32_t exo = __shfl_sync(0xffffffffu, ex, lo);
             if (q < total) {
@@ -137,7 +151,7 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
                 const uint32_t xy = sxy[wl][lo];
                 rg_fragment(P, srec[wl][lo][0], srec[wl][lo][1], srec[wl][lo][2], t0 + lo,
                             (xy & 0xffffu) + (local - row * w), (xy >> 16) + row, N, gkeys, bitmap, stencil,
-                            gate_with_stencil, frags);
+                            gate_with_stencil, mx, my, frags);
             }
         }
         __syncwarp();
@@ -155,6 +169,8 @@ __global__ void __launch_bounds__(RG_THREADS) raster_big_kernel(
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
     const uint32_t nb = (uint32_t)flags->n_big;
     unsigned long long frags = 0;
+    const uint32_t mx = div_magic(P.tile_w), my = div_magic(P.tile_h);
+    const uint32_t blocks_x = (P.W + 31) >> 5;
     for (uint32_t k = blockIdx.x; k < nb; k += gridDim.x) {
         const uint32_t t = big_list[k];
         const float4* r = setup + 4 * (size_t)t;
@@ -164,9 +180,18 @@ __global__ void __launch_bounds__(RG_THREADS) raster_big_kernel(
         const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)P.W - 1);
         const uint32_t w = x1 - x0 + 1;
         const unsigned long long at = area[t];
+        {
+            const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1);
+            const uint32_t bx0 = x0 >> TOUCH_LOG2, by0 = y0 >> TOUCH_LOG2;
+            const uint32_t nbx = (x1 >> TOUCH_LOG2) - bx0 + 1, nby = (y1 >> TOUCH_LOG2) - by0 + 1;
+            for (uint32_t j = threadIdx.x; j < nbx * nby; j += RG_THREADS) {
+                const uint32_t b = (by0 + j / nbx) * blocks_x + bx0 + j % nbx, bit = 1u << (b & 31);
+                if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);
+            }
+        }
         for (unsigned long long j = threadIdx.x; j < at; j += RG_THREADS) {
             const uint32_t row = (uint32_t)(j / w), col = (uint32_t)(j - (unsigned long long)row * w);
-            rg_fragment(P, r0, r1, r2, t, x0 + col, y0 + row, N, gkeys, bitmap, stencil, gate_with_stencil, frags);
+            rg_fragment(P, r0, r1, r2, t, x0 + col, y0 + row, N, gkeys, bitmap, stencil, gate_with_stencil, mx, my, frags);
         }
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
@@ -315,8 +340,23 @@ static void launch_resolve_fs(const DrawParams& P, const sr_uniforms& U, const O
 
 // launches: raster_small, raster_big, ext_direct, resolve
 int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A, cudaStream_t st) {
-    raster_small_kernel<<<152 * 8, RG_THREADS, 0, st>>>(P, A.setup, A.area, A.gkeys, A.bitmap, A.stencil, A.gate,
-                                                         A.big_list, A.flags);
+    // primitives per warp: 32, halved while that would leave fewer warps than
+    // the GPU holds (152 SMs x 48 resident warps); clipped draws estimate the
+    // primitive count by the input count
+    const uint32_t n_est = P.n_raster_host ? P.n_raster_host : P.n_in;
+    uint32_t G = 32;
+    while (G > 1 && n_est / G < 152u * 48u) G >>= 1;
+#define SR_RS(g) raster_small_kernel<g><<<152 * 8, RG_THREADS, 0, st>>>(P, A.setup, A.area, A.gkeys, A.bitmap, \
+                                                                      A.stencil, A.gate, A.big_list, A.flags)
+    switch (G) {
+    case 1: SR_RS(1); break;
+    case 2: SR_RS(2); break;
+    case 4: SR_RS(4); break;
+    case 8: SR_RS(8); break;
+    case 16: SR_RS(16); break;
+    default: SR_RS(32); break;
+    }
+#undef SR_RS
     raster_big_kernel<<<152 * 2, RG_THREADS, 0, st>>>(P, A.setup, A.area, A.gkeys, A.bitmap, A.stencil, A.gate,
                                                        A.big_list, A.flags);
     ext_direct_kernel<<<152 * 4, 256, 0, st>>>(P, A.unsafe_list, A.setup, A.gkeys, A.bitmap, A.stencil, A.gate, A.flags);
