@@ -275,12 +275,21 @@ def raster_bytes(scene):
     return 2 * scene.width * scene.height * 8 + scene.texture.nbytes
 
 
+TRAFFIC_FILE = os.path.join(ROOT, "profiles", "raster_stage_gridsphere_1M_3840x2160.md")
+
+
 def traffic_from_profiles():
+    """dram__bytes_read.sum + dram__bytes_write.sum of the raster stage's kernels
+    for one frame of this workload, from the committed ncu summary (the line
+    `raster stage DRAM bytes per launch: N`)."""
     try:
-        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
-            return json.load(f).get("raster_kernel_dram_bytes_per_launch")
-    except Exception:
+        with open(TRAFFIC_FILE) as f:
+            for ln in f:
+                if ln.startswith("raster stage DRAM bytes per launch:"):
+                    return int(ln.split(":")[1].strip().split()[0].replace(",", ""))
+    except (OSError, ValueError):
         return None
+    return None
 
 
 def main():
@@ -324,7 +333,9 @@ def main():
             "fragments_per_frame": int(frags),
             "triangles_generated_per_frame": int(r["stats"]["triangles_generated"]),
             "triangles_rasterised_per_frame": int(r["stats"]["triangles_raster"]),
-            "roofline": {"bound": "hbm", "kernel": "raster_opaque_kernel<textured_blinn_phong, RGBA8>",
+            "roofline": {"bound": "hbm",
+                         "kernel": "opaque raster stage: raster_small_kernel<32> + raster_big_kernel + "
+                                   "ext_direct_kernel + resolve_kernel<textured_blinn_phong,RGBA8>",
                          "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
                          "frac": round(ach / peak, 4), "traffic": traffic_from_profiles(),
                          "algorithmic_bytes": int(rb), "kernel_ms": round(r_ms, 4),
