@@ -244,6 +244,51 @@ SR_API int sr_sync(sr_pipeline* p);
 /* Counters of the most recent sr_render (valid after sr_sync). */
 SR_API int sr_get_stats(sr_pipeline* p, sr_stats* out);
 
+/* ------------------------------------------------------------ batched draws
+ * Many independent draws of uneven sizes rendered together: one launch per
+ * stage (clear, vertex, setup, raster, resolve) pulls (draw, item) work items
+ * from the whole batch, and the launch sequence is replayed as a CUDA graph.
+ * Equivalent to sr_render(items[i].target, &items[i].draw) for every i (each
+ * target's framebuffer ends up bit-identical).  The reference renders one
+ * mesh per Pipeline::render_mesh call (src/pipeline/mod.rs:146-155); batching
+ * has no counterpart there (src/lib.rs:43-44 notes that many small meshes are
+ * slow).
+ *
+ * Eligible draws: triangles, gs_mode SR_GS_NONE (run_to_fragment), blend
+ * "replace", no stencil writes (no stencil attachment, or test Always with op
+ * Keep); every target distinct and synced (no draws pending since its last
+ * sr_sync).  Others return SR_EINVAL / SR_EBUSY without rendering anything.
+ * Uniforms come from each target (sr_pipeline_set_uniforms). */
+typedef struct sr_batch sr_batch;
+typedef struct sr_batch_item {
+    sr_pipeline* target;        /* framebuffer and uniforms of this draw             */
+    sr_draw draw;               /* as for sr_render                                  */
+    uint32_t clear;             /* nonzero: clear the target first (depth f32::MIN)  */
+    uint8_t clear_color[16];    /* clear colour in the target's format (RGBA32F: 4
+                                   floats; RGBA8: 4 bytes, r first)                  */
+} sr_batch_item;
+SR_API int sr_batch_create(sr_batch** out);
+SR_API int sr_batch_destroy(sr_batch* b);
+/* Stream the batch runs on (NULL: the batch's own stream). */
+SR_API int sr_batch_set_stream(sr_batch* b, void* stream);
+/* use_graphs: replay the launch sequence as a CUDA graph (default 1);
+ * autotune: measure the launch configurations once per batch size class and
+ * keep the fastest (default 1). */
+SR_API int sr_batch_set_options(sr_batch* b, int use_graphs, int autotune);
+/* Forces a launch configuration (primitives per warp 1..32, power of two;
+ * large-primitive threshold in bbox pixels; raster CTAs per SM 1..8); all
+ * zero returns to the tuned / default choice.  Results do not depend on it. */
+SR_API int sr_batch_set_config(sr_batch* b, uint32_t prims_per_warp, uint32_t big_threshold, uint32_t ctas_per_sm);
+SR_API int sr_batch_get_config(sr_batch* b, uint32_t* prims_per_warp, uint32_t* big_threshold, uint32_t* ctas_per_sm);
+/* Enqueues the batch (returns after enqueue; waits first for this batch
+ * object's previous batch, whose host table it reuses). */
+SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, uint32_t n);
+/* Waits for the last batch; SR_ENAN / SR_EINVAL (an index >= the vertex
+ * count dropped its triangle) as sr_sync reports them. */
+SR_API int sr_batch_sync(sr_batch* b);
+/* Summed counters of the last batch (valid after sr_batch_sync). */
+SR_API int sr_batch_get_stats(sr_batch* b, sr_stats* out);
+
 /* ---------------------------------------------------- allocation-free draw
  * sr_render_static has no counterpart in the reference.  It is for callers
  * that cannot let a library allocate device memory: an application whose own

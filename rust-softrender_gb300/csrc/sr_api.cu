@@ -19,83 +19,7 @@
 
 using namespace sr;
 
-#define SR_CK(x)                                   \
-    do {                                           \
-        cudaError_t e_ = (x);                      \
-        if (e_ != cudaSuccess) {                   \
-            last_cuda_error() = e_;                \
-            return e_ == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA; \
-        }                                          \
-    } while (0)
-
-static cudaError_t& last_cuda_error() {
-    static thread_local cudaError_t e = cudaSuccess;
-    return e;
-}
-
-namespace {
-
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t cap = 0;  // elements
-    int ensure(size_t n) {
-        if (n <= cap) return SR_OK;
-        if (p) cudaFree(p);
-        p = nullptr;
-        cap = 0;
-        size_t want = n + n / 4 + 64;
-        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
-        if (e != cudaSuccess) { last_cuda_error() = e; p = nullptr; return SR_ENOMEM; }
-        cap = want;
-        return SR_OK;
-    }
-    void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
-};
-
-struct PendingDraw {
-    sr_draw d;
-    sr_uniforms U;
-    uint32_t stencil_test, stencil_op, stencil_wrap;
-};
-
-}  // namespace
-
-struct sr_pipeline {
-    sr_fb_desc fb;
-    void* color = nullptr;
-    float* depth = nullptr;
-    uint8_t* stencil = nullptr;
-    sr_uniforms U;
-    uint32_t stencil_test = SR_STENCIL_ALWAYS, stencil_op = SR_STENCIL_KEEP, stencil_wrap = 1;
-    cudaStream_t own_stream = nullptr;
-    cudaStream_t stream = nullptr;
-    DeviceFlags* flags = nullptr;     // device
-    DeviceFlags* hflags = nullptr;    // pinned host mirror
-    // workspace
-    DevBuf<float4> clip4, scr4;
-    DevBuf<float> vary;
-    DevBuf<unsigned long long> clip_counts, clip_offsets, clip_tmp;
-    DevBuf<uint32_t> refs;
-    DevBuf<float4> setup;
-    DevBuf<uint2> binrect;
-    DevBuf<uint32_t> bin_counts, bin_off, bin_cursor, bin_tmp, entries, unsafe_list;
-    DevBuf<unsigned long long> area, gkeys;
-    DevBuf<uint32_t> big_list;
-    DevBuf<uint32_t> bitmap;
-    DevBuf<int> st_diff, st_lines;
-    DevBuf<unsigned long long> st_glob;
-    // capacities (elements) requested for the generated geometry
-    uint64_t gen_tri_cap = 0, gen_vert_cap = 0, entry_cap = 0;
-    std::vector<PendingDraw> pending;
-    sr_stats last_stats;
-    bool stats_valid = false;
-    bool force_unsafe = false;   // SR_FORCE_UNSAFE=1: every primitive takes the exact unsafe path
-    bool profiling = false;
-    cudaEvent_t ev[6] = {};
-    uint32_t last_launches = 0;
-    bool last_profiled = false;
-};
+#include "sr_host.h"
 
 namespace {
 

@@ -1,0 +1,825 @@
+// sr_batch.cu — batched rendering: many independent opaque draws (each into
+// its own pipeline's framebuffer, meshes and resolutions of uneven sizes)
+// rendered by one launch per stage instead of one set of launches per draw.
+//
+// Every stage is a persistent kernel (a fixed grid sized to the GPU) that
+// pulls work items from the flattened (instance, item) space: vertex quads,
+// primitives, 32x32 resolve blocks and clear chunks.  An item's instance is
+// found by binary search over per-instance exclusive prefix sums.  Per-draw
+// results are identical to sr_render's: the per-primitive, per-pixel and
+// per-block device code is the same (sr_vertex.cuh, sr_setup.cuh,
+// sr_opaque.cuh), only the indexing differs; each instance keeps its own
+// primitive numbering, key buffer and touched-block bitmap (its pipeline's).
+//
+// The launch sequence reads every size from a device-resident table, so one
+// CUDA graph serves every batch with the same table capacity and launch
+// configuration; the host fills a pinned table per batch and replays.  The
+// launch configuration (primitives per warp, large-primitive threshold,
+// raster CTAs per SM) is picked per batch size class by measuring the
+// candidates once (results do not depend on it: the opaque reduction is
+// order independent).
+#include <algorithm>
+#include <cstdlib>
+#include <map>
+#include <unordered_set>
+#include <vector>
+
+#include "sr_host.h"
+#include "sr_opaque.cuh"
+#include "sr_scan.cuh"
+#include "sr_setup.cuh"
+#include "sr_vertex.cuh"
+
+namespace sr {
+
+// One draw of a batch (device table entry).
+struct BInst {
+    DrawParams P;                 // as sr_render derives it; P.n_raster_host = triangle count
+    VpMatrix vpm;                 // viewport matrix of ClipVertex::normalize
+    const float* planes;
+    const uint32_t* indices;
+    const uint32_t* tex;
+    void* color;
+    float* depth;
+    unsigned long long* gkeys;    // the target pipeline's per-pixel key buffer
+    uint32_t* bitmap;             // the target pipeline's touched-block bitmap
+    uint32_t n_pad;               // plane stride of the mesh
+    uint32_t vbase, tbase;        // first batch vertex slot / first batch primitive
+    uint32_t clear;               // clear colour and depth before drawing
+    uint4 clear_color;            // colour clear pattern (one pixel of RGBA32F, four of RGBA8)
+    uint32_t mx, my;              // division magics of the semantic tile size
+};
+
+// Device table layout for a capacity of NB draws (all offsets 256-aligned).
+struct BTables {
+    const uint32_t* n;            // number of draws in this batch
+    const BInst* inst;
+    const sr_uniforms* U;
+    const uint32_t* qbase;        // exclusive prefix of vertex quads        (NB + 1)
+    const uint32_t* tbase;        // exclusive prefix of primitives          (NB + 1)
+    const uint32_t* bbase;        // exclusive prefix of 32x32 resolve blocks (NB + 1)
+    const uint32_t* cbase;        // exclusive prefix of clear chunks        (NB + 1)
+};
+
+constexpr uint32_t CLEAR_CHUNK = 8192;   // pixels per clear work item
+
+// Largest i in [0, n) with base[i] <= j (base[0] = 0, j < base[n]).
+__device__ __forceinline__ uint32_t owner_of(const uint32_t* __restrict__ base, uint32_t n, uint32_t j) {
+    uint32_t lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi + 1) >> 1;
+        if (__ldg(base + mid) <= j) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+// ---------------------------------------------------------------- clear
+__global__ void __launch_bounds__(256) batch_clear_kernel(BTables T) {
+    const uint32_t n = *T.n;
+    const uint32_t total = __ldg(T.cbase + n);
+    for (uint32_t j = blockIdx.x; j < total; j += gridDim.x) {
+        const uint32_t i = owner_of(T.cbase, n, j);
+        const BInst& I = T.inst[i];
+        const size_t npx = (size_t)I.P.W * I.P.H;
+        const size_t p0 = (size_t)(j - __ldg(T.cbase + i)) * CLEAR_CHUNK;
+        const size_t p1 = min(npx, p0 + CLEAR_CHUNK);
+        const uint4 cv = I.clear_color;
+        const float far_ = -3.40282347e+38f;   // f32::MIN (attachments/depth.rs:31)
+        const uint32_t dv = __float_as_uint(far_);
+        for (size_t p = p0 + 4 * (size_t)threadIdx.x; p < p1; p += 4 * (size_t)blockDim.x) {
+            const bool full = p + 4 <= p1;
+            if (I.P.color_format == SR_COLOR_RGBA32F) {
+                uint4* c = reinterpret_cast<uint4*>(I.color) + p;
+                for (uint32_t k = 0; k < 4 && p + k < p1; ++k) c[k] = cv;
+            } else if (I.P.color_format == SR_COLOR_RGBA8) {
+                uint32_t* c = reinterpret_cast<uint32_t*>(I.color) + p;
+                if (full) *reinterpret_cast<uint4*>(c) = cv;
+                else for (uint32_t k = 0; p + k < p1; ++k) c[k] = cv.x;
+            }
+            if (I.P.has_depth) {
+                float* d = I.depth + p;
+                if (full) *reinterpret_cast<uint4*>(d) = make_uint4(dv, dv, dv, dv);
+                else for (uint32_t k = 0; p + k < p1; ++k) d[k] = far_;
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- vertex
+__global__ void __launch_bounds__(128) batch_vertex_kernel(BTables T, float4* __restrict__ scr4,
+                                                           float* __restrict__ vary) {
+    const uint32_t n = *T.n;
+    const uint32_t total = __ldg(T.qbase + n);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
+        const uint32_t i = owner_of(T.qbase, n, j);
+        const BInst& I = T.inst[i];
+        const uint32_t q = j - __ldg(T.qbase + i);
+        float4* s4 = scr4 + I.vbase;
+        float* vy = vary + (size_t)I.vbase * VSTRIDE;
+        switch (I.P.vs) {
+        case VS_MVP_POS_NRM: vertex_quad<VS_MVP_POS_NRM>(q, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
+        case VS_MVP_POS_NRM_UV: vertex_quad<VS_MVP_POS_NRM_UV>(q, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
+        case VS_CLIP_COLOR: vertex_quad<VS_CLIP_COLOR>(q, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
+        default: vertex_quad<VS_CLIP_RGBA8>(q, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- setup
+// The opaque branch of setup_kernel (sr_setup.cu) per batch primitive g:
+// cull, det, bbox, safety class, record, bbox pixel count, unsafe list.
+__global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float4* __restrict__ scr4,
+                                                          float4* __restrict__ setup,
+                                                          unsigned long long* __restrict__ area,
+                                                          uint32_t* __restrict__ unsafe_list, DeviceFlags* flags) {
+    const uint32_t n = *T.n;
+    const uint32_t total = __ldg(T.tbase + n);
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t lane = threadIdx.x & 31;
+    // every thread runs the same number of iterations (warp reductions below)
+    const uint32_t rounds = (total + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t g = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        unsigned long long n_raster = 0, n_unsafe = 0;
+        uint32_t nan_cnt = 0;
+        if (g < total) {
+            const uint32_t i = owner_of(T.tbase, n, g);
+            const BInst& I = T.inst[i];
+            const DrawParams& P = I.P;
+            const uint32_t t = g - I.tbase;
+            uint32_t ia, ib, ic;
+            tri_slots(t, I.indices, ia, ib, ic);
+            const bool bad = ia >= P.n_verts || ib >= P.n_verts || ic >= P.n_verts;
+            if (bad) { atomicOr(&flags->bad_index, 1u); ia = ib = ic = 0; }
+            const float4* sv = scr4 + I.vbase;
+            const float4 s0 = __ldg(sv + ia), s1 = __ldg(sv + ib), s2 = __ldg(sv + ic);
+            const float x1 = s0.x, y1 = s0.y, x2 = s1.x, y2 = s1.y, x3 = s2.x, y3 = s2.y;
+            bool culled = false;
+            if (P.cull) {
+                const float ar = x1 * y2 + x2 * y3 + x3 * y1 - x2 * y1 - x3 * y2 - x1 * y3;
+                const bool neg = !isnan(ar) && signbit(ar);
+                culled = (neg ? 1u : 2u) == P.cull;
+            }
+            culled = culled || bad;
+            area[g] = 0;
+            setup[4 * (size_t)g + 2] = make_float4(0.0f, 0.0f, __uint_as_float(0u), 0.0f);
+            if (!culled) {
+                const float det = (y2 - y3) * (x1 - x3) + (x3 - x2) * (y1 - y3);
+                const float mnx = sr_min(sr_min(x1, x2), x3), mny = sr_min(sr_min(y1, y2), y3);
+                const float mxx = sr_max(sr_max(x1, x2), x3), mxy = sr_max(sr_max(y1, y2), y3);
+                if (isnan(mnx) || isnan(mny)) {
+                    nan_cnt = 1;
+                } else {
+                    const int W = (int)P.W, H = (int)P.H;
+                    const int ix0 = floor_sat(mnx, -1, W), ix1 = floor_sat(mxx, -1, W);
+                    const int iy0 = floor_sat(mny, -1, H), iy1 = floor_sat(mxy, -1, H);
+                    const bool no_frag = det == 0.0f || isnan(det) || (s0.z >= 0.0f && s1.z >= 0.0f && s2.z >= 0.0f);
+                    if (!no_frag) {
+                        const bool safe = !P.force_unsafe &&
+                                          inflated_region(x1, y1, x2, y2, x3, y3, det, P.W, P.H, ix0, iy0, ix1, iy1);
+                        const int qx0 = max(ix0, 0), qy0 = max(iy0, 0), qx1 = min(ix1, W - 1), qy1 = min(iy1, H - 1);
+                        const bool b_in = qx0 <= qx1 && qy0 <= qy1;
+                        if (b_in || !safe) {
+                            float4* rr = setup + 4 * (size_t)g;
+                            rr[0] = make_float4(y2 - y3, x3 - x2, y3 - y1, x1 - x3);
+                            rr[1] = make_float4(x3, y3, det, s0.z);
+                            rr[2] = make_float4(s1.z, s2.z, __uint_as_float(REC_RASTER | (safe ? 0u : REC_UNSAFE)), 0.0f);
+                            rr[3] = make_float4(__int_as_float(ix0), __int_as_float(iy0), __int_as_float(ix1),
+                                                __int_as_float(iy1));
+                            n_raster = 1;
+                            n_unsafe = safe ? 0 : 1;
+                            area[g] = b_in ? (unsigned long long)(qx1 - qx0 + 1) * (unsigned long long)(qy1 - qy0 + 1)
+                                           : 0ull;
+                            if (!safe) unsafe_list[atomicAdd(&flags->n_unsafe_list, 1ull)] = g;
+                        }
+                    }
+                }
+            }
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            n_raster += __shfl_down_sync(0xffffffffu, n_raster, o);
+            n_unsafe += __shfl_down_sync(0xffffffffu, n_unsafe, o);
+            nan_cnt += __shfl_down_sync(0xffffffffu, nan_cnt, o);
+        }
+        if (lane == 0) {
+            if (n_raster) atomicAdd(&flags->triangles_raster, n_raster);
+            if (n_unsafe) atomicAdd(&flags->unsafe, n_unsafe);
+            if (nan_cnt) { atomicAdd(&flags->nan_bbox, nan_cnt); atomicAdd(&flags->nan_total, nan_cnt); }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- raster
+// raster_small_kernel (sr_opaque.cu) over batch primitives: each warp takes G
+// consecutive batch primitives, which may belong to different draws; every
+// staged primitive carries its draw index.
+template <uint32_t G>
+__global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, const float4* __restrict__ setup,
+                                                                 const unsigned long long* __restrict__ area,
+                                                                 uint32_t big_threshold,
+                                                                 uint32_t* __restrict__ big_list, DeviceFlags* flags) {
+    __shared__ float4 srec[8][32][3];
+    __shared__ uint32_t sxy[8][32];
+    __shared__ uint32_t sw[8][32];
+    __shared__ uint32_t sid[8][32];                  // draw index
+    __shared__ uint32_t stl[8][32];                  // primitive index within the draw
+    __shared__ unsigned long long smag[8][32];
+    const uint32_t n = *T.n;
+    const uint32_t total = __ldg(T.tbase + n);
+    const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long frags = 0;
+    for (uint32_t t0 = warp * G; t0 < total; t0 += nwarps * G) {
+        const uint32_t g = t0 + lane;
+        uint32_t a = 0;
+        if (lane < G && g < total) {
+            const unsigned long long at = area[g];
+            if (at > big_threshold) {
+                big_list[atomicAdd(&flags->n_big, 1ull)] = g;
+            } else if (at) {
+                a = (uint32_t)at;
+                const uint32_t i = owner_of(T.tbase, n, g);
+                const BInst& I = T.inst[i];
+                const float4* r = setup + 4 * (size_t)g;
+                srec[wl][lane][0] = __ldg(r);
+                srec[wl][lane][1] = __ldg(r + 1);
+                srec[wl][lane][2] = __ldg(r + 2);
+                const float4 r3 = __ldg(r + 3);
+                const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
+                const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
+                const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)I.P.W - 1);
+                const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)I.P.H - 1);
+                const uint32_t w = x1 - x0 + 1;
+                mark_rect(I.bitmap, (I.P.W + 31) >> 5, x0, y0, x1, y1);
+                sxy[wl][lane] = x0 | (y0 << 16);
+                sw[wl][lane] = w;
+                sid[wl][lane] = i;
+                stl[wl][lane] = g - I.tbase;
+                smag[wl][lane] = ((1ull << 32) + w - 1) / w;
+            }
+        }
+        __syncwarp();
+        const uint32_t inc = warp_inclusive_scan(a);
+        const uint32_t tot = __shfl_sync(0xffffffffu, inc, 31);
+        const uint32_t ex = inc - a;
+        for (uint32_t base = 0; base < tot; base += 32) {
+            const uint32_t q = base + lane;
+            uint32_t lo = 0;
+#pragma unroll
+            for (uint32_t step = G >> 1; step >= 1; step >>= 1) {
+                const uint32_t c = lo + step;
+                const uint32_t v = __shfl_sync(0xffffffffu, ex, c & 31u);
+                if (c < G && v <= q) lo = c;
+            }
+            const uint32_t exo = __shfl_sync(0xffffffffu, ex, lo);
+            if (q < tot) {
+                const uint32_t local = q - exo;
+                const uint32_t w = sw[wl][lo];
+                const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][lo]) >> 32);  // local / w
+                const uint32_t xy = sxy[wl][lo];
+                const BInst& I = T.inst[sid[wl][lo]];
+                rg_fragment(I.P, srec[wl][lo][0], srec[wl][lo][1], srec[wl][lo][2], stl[wl][lo],
+                            (xy & 0xffffu) + (local - row * w), (xy >> 16) + row, I.P.n_raster_host, I.gkeys,
+                            I.bitmap, nullptr, 0u, I.mx, I.my, frags);
+            }
+        }
+        __syncwarp();
+    }
+    for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
+    if (lane == 0 && frags) atomicAdd(&flags->fragments, frags);
+}
+
+// raster_big_kernel over the batch's large primitives.
+__global__ void __launch_bounds__(256) batch_raster_big_kernel(BTables T, const float4* __restrict__ setup,
+                                                               const unsigned long long* __restrict__ area,
+                                                               const uint32_t* __restrict__ big_list,
+                                                               DeviceFlags* flags) {
+    const uint32_t n = *T.n;
+    const uint32_t nb = (uint32_t)flags->n_big;
+    unsigned long long frags = 0;
+    for (uint32_t k = blockIdx.x; k < nb; k += gridDim.x) {
+        const uint32_t g = big_list[k];
+        const BInst& I = T.inst[owner_of(T.tbase, n, g)];
+        const float4* r = setup + 4 * (size_t)g;
+        const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+        const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
+        const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
+        const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)I.P.W - 1);
+        const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)I.P.H - 1);
+        const uint32_t w = x1 - x0 + 1;
+        const uint32_t blocks_x = (I.P.W + 31) >> 5;
+        {
+            const uint32_t bx0 = x0 >> TOUCH_LOG2, by0 = y0 >> TOUCH_LOG2;
+            const uint32_t nbx = (x1 >> TOUCH_LOG2) - bx0 + 1, nby = (y1 >> TOUCH_LOG2) - by0 + 1;
+            for (uint32_t j = threadIdx.x; j < nbx * nby; j += blockDim.x) {
+                const uint32_t b = (by0 + j / nbx) * blocks_x + bx0 + j % nbx, bit = 1u << (b & 31);
+                if (!(I.bitmap[b >> 5] & bit)) atomicOr(I.bitmap + (b >> 5), bit);
+            }
+        }
+        const unsigned long long at = area[g];
+        const uint32_t t = g - I.tbase;
+        for (unsigned long long j = threadIdx.x; j < at; j += blockDim.x) {
+            const uint32_t row = (uint32_t)(j / w), col = (uint32_t)(j - (unsigned long long)row * w);
+            rg_fragment(I.P, r0, r1, r2, t, x0 + col, y0 + row, I.P.n_raster_host, I.gkeys, I.bitmap, nullptr, 0u,
+                        I.mx, I.my, frags);
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
+    if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&flags->fragments, frags);
+}
+
+// ext_direct_kernel over the batch's unsafe primitives (one warp each).
+__global__ void __launch_bounds__(256) batch_ext_kernel(BTables T, const float4* __restrict__ setup,
+                                                        const uint32_t* __restrict__ unsafe_list, DeviceFlags* flags) {
+    const uint32_t n = *T.n;
+    const uint32_t nu = (uint32_t)flags->n_unsafe_list;
+    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    unsigned long long frags = 0;
+    for (uint32_t k = warp; k < nu; k += nwarps) {
+        const uint32_t g = unsafe_list[k];
+        const BInst& I = T.inst[owner_of(T.tbase, n, g)];
+        ext_prim(I.P, g - I.tbase, I.P.n_raster_host, setup + 4 * (size_t)I.tbase, I.gkeys, I.bitmap, nullptr, 0u,
+                 lane, frags);
+    }
+    for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
+    if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&flags->fragments, frags);
+}
+
+// ---------------------------------------------------------------- resolve
+// resolve_kernel over (draw, touched 32x32 block) items; the fragment shader
+// and colour format are dispatched per draw.
+__global__ void __launch_bounds__(256) batch_resolve_kernel(BTables T, const float4* __restrict__ setup,
+                                                            const float* __restrict__ vary) {
+    const uint32_t n = *T.n;
+    const uint32_t total = __ldg(T.bbase + n);
+    for (uint32_t j = blockIdx.x; j < total; j += gridDim.x) {
+        const uint32_t i = owner_of(T.bbase, n, j);
+        const BInst& I = T.inst[i];
+        const uint32_t b = j - __ldg(T.bbase + i);
+        if (!(I.bitmap[b >> 5] & (1u << (b & 31)))) continue;
+        const float4* su = setup + 4 * (size_t)I.tbase;
+        const float* vy = vary + (size_t)I.vbase * VSTRIDE;
+        const uint32_t N = I.P.n_raster_host;
+#define SR_BR(FS, FMT) resolve_block<FS, FMT>(I.P, T.U[i], b, N, su, I.indices, vy, I.tex, I.color, I.depth, \
+                                              nullptr, 0u, I.gkeys, I.bitmap)
+#define SR_BR_FS(FS)                                                        \
+        if (I.P.color_format == SR_COLOR_RGBA8) SR_BR(FS, SR_COLOR_RGBA8);   \
+        else if (I.P.color_format == SR_COLOR_RGBA32F) SR_BR(FS, SR_COLOR_RGBA32F); \
+        else SR_BR(FS, SR_COLOR_NONE);
+        switch (I.P.fs) {
+        case FS_BLINN_PHONG_DIR: SR_BR_FS(FS_BLINN_PHONG_DIR) break;
+        case FS_TEXTURED_BLINN_PHONG: SR_BR_FS(FS_TEXTURED_BLINN_PHONG) break;
+        case FS_VERTEX_COLOR: SR_BR_FS(FS_VERTEX_COLOR) break;
+        case FS_ACES_LIGHTS: SR_BR_FS(FS_ACES_LIGHTS) break;
+        default: SR_BR_FS(FS_CONSTANT_COLOR) break;
+        }
+#undef SR_BR_FS
+#undef SR_BR
+    }
+}
+
+}  // namespace sr
+
+// ================================================================== host
+using namespace sr;
+
+namespace {
+
+constexpr uint32_t BATCH_SMS = 152;
+
+struct BatchConfig {
+    uint32_t G = 32;          // primitives per warp in the raster pass
+    uint32_t big = RG_BIG;    // bbox pixels above which a primitive gets a whole block
+    uint32_t ctas = 8;        // raster CTAs per SM
+    bool operator==(const BatchConfig& o) const { return G == o.G && big == o.big && ctas == o.ctas; }
+};
+
+struct Layout {
+    size_t off_n, off_inst, off_U, off_q, off_t, off_b, off_c, bytes;
+};
+
+size_t al256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+Layout layout_for(uint32_t NB) {
+    Layout L;
+    L.off_n = 0;
+    L.off_inst = 256;
+    L.off_U = al256(L.off_inst + (size_t)NB * sizeof(BInst));
+    L.off_q = al256(L.off_U + (size_t)NB * sizeof(sr_uniforms));
+    L.off_t = al256(L.off_q + (size_t)(NB + 1) * 4);
+    L.off_b = al256(L.off_t + (size_t)(NB + 1) * 4);
+    L.off_c = al256(L.off_b + (size_t)(NB + 1) * 4);
+    L.bytes = al256(L.off_c + (size_t)(NB + 1) * 4);
+    return L;
+}
+
+uint32_t bucket_of(uint32_t n) {
+    uint32_t b = 16;
+    while (b < n) b <<= 1;
+    return b;
+}
+
+int batch_min_varyings(int fs) {
+    switch (fs) {
+    case FS_TEXTURED_BLINN_PHONG: return 10;
+    case FS_VERTEX_COLOR: return 4;
+    case FS_CONSTANT_COLOR: return 0;
+    default: return 8;
+    }
+}
+
+uint32_t log2_floor(uint64_t x) {
+    uint32_t r = 0;
+    while (x > 1) { x >>= 1; ++r; }
+    return r;
+}
+
+}  // namespace
+
+struct sr_batch {
+    cudaStream_t own_stream = nullptr, stream = nullptr;
+    DevBuf<unsigned char> dtab;
+    unsigned char* htab = nullptr;
+    size_t htab_cap = 0;
+    DevBuf<float4> scr4;
+    DevBuf<float> vary;
+    DevBuf<float4> setup;
+    DevBuf<unsigned long long> area;
+    DevBuf<uint32_t> big_list, unsafe_list;
+    DeviceFlags* flags = nullptr;
+    DeviceFlags* hflags = nullptr;
+    cudaEvent_t done = nullptr, ev0 = nullptr, ev1 = nullptr;
+    bool in_flight = false;
+    bool use_graphs = true, autotune = true;
+    BatchConfig forced{0, 0, 0};
+    std::map<uint64_t, BatchConfig> tuned;
+    struct Graph { uint32_t NB; BatchConfig cfg; uint64_t gen; cudaGraphExec_t exec; };
+    std::vector<Graph> graphs;
+    uint64_t gen = 1;            // bumped whenever a device buffer moves
+    BatchConfig last_cfg;
+    uint64_t last_tris = 0;
+    sr_stats last{};
+    bool stats_valid = false;
+};
+
+namespace {
+
+void drop_graphs(sr_batch* b) {
+    for (auto& g : b->graphs) cudaGraphExecDestroy(g.exec);
+    b->graphs.clear();
+}
+
+template <typename T>
+int grow(sr_batch* b, DevBuf<T>& buf, size_t n) {
+    if (n <= buf.cap) return SR_OK;
+    // a buffer that moves invalidates the recorded graphs; wait for users
+    if (b->in_flight) cudaEventSynchronize(b->done);
+    drop_graphs(b);
+    ++b->gen;
+    return buf.ensure(n);
+}
+
+BTables tables_at(unsigned char* base, const Layout& L) {
+    BTables T;
+    T.n = reinterpret_cast<const uint32_t*>(base + L.off_n);
+    T.inst = reinterpret_cast<const BInst*>(base + L.off_inst);
+    T.U = reinterpret_cast<const sr_uniforms*>(base + L.off_U);
+    T.qbase = reinterpret_cast<const uint32_t*>(base + L.off_q);
+    T.tbase = reinterpret_cast<const uint32_t*>(base + L.off_t);
+    T.bbase = reinterpret_cast<const uint32_t*>(base + L.off_b);
+    T.cbase = reinterpret_cast<const uint32_t*>(base + L.off_c);
+    return T;
+}
+
+// The launch sequence of one batch (also what a graph records).
+void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
+    const Layout L = layout_for(NB);
+    cudaStream_t st = b->stream;
+    const BTables T = tables_at(b->dtab.p, L);
+    cudaMemcpyAsync(b->dtab.p, b->htab, L.bytes, cudaMemcpyHostToDevice, st);
+    cudaMemsetAsync(b->flags, 0, sizeof(DeviceFlags), st);
+    batch_clear_kernel<<<BATCH_SMS * 8, 256, 0, st>>>(T);
+    batch_vertex_kernel<<<BATCH_SMS * 16, 128, 0, st>>>(T, b->scr4.p, b->vary.p);
+    batch_setup_kernel<<<BATCH_SMS * 8, 256, 0, st>>>(T, b->scr4.p, b->setup.p, b->area.p, b->unsafe_list.p, b->flags);
+    const dim3 rg(BATCH_SMS * c.ctas);
+#define SR_BRS(g) batch_raster_small_kernel<g><<<rg, 256, 0, st>>>(T, b->setup.p, b->area.p, c.big, b->big_list.p, b->flags)
+    switch (c.G) {
+    case 1: SR_BRS(1); break;
+    case 2: SR_BRS(2); break;
+    case 4: SR_BRS(4); break;
+    case 8: SR_BRS(8); break;
+    case 16: SR_BRS(16); break;
+    default: SR_BRS(32); break;
+    }
+#undef SR_BRS
+    batch_raster_big_kernel<<<BATCH_SMS * 2, 256, 0, st>>>(T, b->setup.p, b->area.p, b->big_list.p, b->flags);
+    batch_ext_kernel<<<BATCH_SMS * 4, 256, 0, st>>>(T, b->setup.p, b->unsafe_list.p, b->flags);
+    batch_resolve_kernel<<<BATCH_SMS * 8, 256, 0, st>>>(T, b->setup.p, b->vary.p);
+}
+
+int launch_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
+    if (!b->use_graphs) {
+        enqueue_batch(b, NB, c);
+        SR_CK(cudaGetLastError());
+        return SR_OK;
+    }
+    cudaGraphExec_t exec = nullptr;
+    for (auto& g : b->graphs)
+        if (g.NB == NB && g.cfg == c && g.gen == b->gen) exec = g.exec;
+    if (!exec) {
+        cudaGraph_t graph = nullptr;
+        SR_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_batch(b, NB, c);
+        cudaError_t e = cudaStreamEndCapture(b->stream, &graph);
+        if (e != cudaSuccess) { last_cuda_error() = e; return SR_ECUDA; }
+        e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) { last_cuda_error() = e; return SR_ECUDA; }
+        if (b->graphs.size() >= 32) { cudaGraphExecDestroy(b->graphs.front().exec); b->graphs.erase(b->graphs.begin()); }
+        b->graphs.push_back({NB, c, b->gen, exec});
+    }
+    SR_CK(cudaGraphLaunch(exec, b->stream));
+    return SR_OK;
+}
+
+// Measures every candidate configuration on this batch (rendering it is
+// idempotent: same inputs, same winners) and returns the fastest.
+BatchConfig tune(sr_batch* b, uint32_t NB) {
+    static const uint32_t Gs[] = {4, 8, 16, 32};
+    static const uint32_t bigs[] = {512, 2048, 8192};
+    static const uint32_t ctas[] = {4, 8};
+    BatchConfig best;
+    float best_ms = 1e30f;
+    for (uint32_t g : Gs)
+        for (uint32_t bg : bigs)
+            for (uint32_t ct : ctas) {
+                BatchConfig c{g, bg, ct};
+                enqueue_batch(b, NB, c);   // warm
+                cudaEventRecord(b->ev0, b->stream);
+                enqueue_batch(b, NB, c);
+                enqueue_batch(b, NB, c);
+                cudaEventRecord(b->ev1, b->stream);
+                if (cudaEventSynchronize(b->ev1) != cudaSuccess) return best;
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, b->ev0, b->ev1);
+                if (ms < best_ms) { best_ms = ms; best = c; }
+            }
+    return best;
+}
+
+}  // namespace
+
+extern "C" SR_API int sr_batch_create(sr_batch** out) {
+    if (!out) return SR_EINVAL;
+    *out = nullptr;
+    sr_batch* b = new (std::nothrow) sr_batch();
+    if (!b) return SR_ENOMEM;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&b->flags, sizeof(DeviceFlags));
+    if (e == cudaSuccess) e = cudaMallocHost(&b->hflags, sizeof(DeviceFlags));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
+    if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
+    if (e != cudaSuccess) {
+        last_cuda_error() = e;
+        sr_batch_destroy(b);
+        return e == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA;
+    }
+    b->stream = b->own_stream;
+    *out = b;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_batch_destroy(sr_batch* b) {
+    if (!b) return SR_EINVAL;
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    drop_graphs(b);
+    b->dtab.release(); b->scr4.release(); b->vary.release(); b->setup.release();
+    b->area.release(); b->big_list.release(); b->unsafe_list.release();
+    if (b->htab) cudaFreeHost(b->htab);
+    if (b->flags) cudaFree(b->flags);
+    if (b->hflags) cudaFreeHost(b->hflags);
+    if (b->done) cudaEventDestroy(b->done);
+    if (b->ev0) cudaEventDestroy(b->ev0);
+    if (b->ev1) cudaEventDestroy(b->ev1);
+    if (b->own_stream) cudaStreamDestroy(b->own_stream);
+    delete b;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_batch_set_stream(sr_batch* b, void* stream) {
+    if (!b) return SR_EINVAL;
+    if (b->in_flight) cudaEventSynchronize(b->done);
+    b->stream = stream ? (cudaStream_t)stream : b->own_stream;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_batch_set_options(sr_batch* b, int use_graphs, int autotune) {
+    if (!b) return SR_EINVAL;
+    b->use_graphs = use_graphs != 0;
+    b->autotune = autotune != 0;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_batch_set_config(sr_batch* b, uint32_t ppw, uint32_t big, uint32_t ctas) {
+    if (!b) return SR_EINVAL;
+    if (ppw == 0 && big == 0 && ctas == 0) { b->forced = BatchConfig{0, 0, 0}; return SR_OK; }
+    if (ppw == 0 || ppw > 32 || (ppw & (ppw - 1)) || big == 0 || ctas == 0 || ctas > 8) return SR_EINVAL;
+    b->forced = BatchConfig{ppw, big, ctas};
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_batch_get_config(sr_batch* b, uint32_t* ppw, uint32_t* big, uint32_t* ctas) {
+    if (!b || !ppw || !big || !ctas) return SR_EINVAL;
+    *ppw = b->last_cfg.G; *big = b->last_cfg.big; *ctas = b->last_cfg.ctas;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, uint32_t n) {
+    if (!b || (n && !items)) return SR_EINVAL;
+    if (n == 0) return SR_OK;
+    if (n > (1u << 20)) return SR_EINVAL;
+    // ---- validation (nothing is enqueued unless every item is acceptable)
+    std::unordered_set<const sr_pipeline*> seen;
+    uint64_t slots = 0, tris = 0, quads = 0, blocks = 0, chunks = 0, px = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const sr_batch_item& it = items[i];
+        const sr_pipeline* p = it.target;
+        const sr_draw* d = &it.draw;
+        const sr_mesh* m = d->mesh;
+        if (!p || !m) return SR_EINVAL;
+        if (!p->pending.empty()) return SR_EBUSY;
+        if (!seen.insert(p).second) return SR_EINVAL;                       // targets must be distinct
+        if (d->prim != SR_PRIM_TRIANGLE || d->gs_mode != SR_GS_NONE || d->blend != BLEND_REPLACE) return SR_EINVAL;
+        if (m->n_indices % 3 != 0) return SR_EINVAL;                        // mod.rs:148
+        if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT) return SR_EINVAL;
+        if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
+        if (d->cull > SR_CULL_COUNTER_CLOCKWISE) return SR_EINVAL;
+        if (m->n_planes < (uint32_t)vs_planes(d->vs)) return SR_EINVAL;
+        if (vs_nk(d->vs) < batch_min_varyings(d->fs)) return SR_EINVAL;
+        if (d->fs == FS_TEXTURED_BLINN_PHONG && !d->texture) return SR_EINVAL;
+        if (p->stencil && !(p->stencil_test == SR_STENCIL_ALWAYS && p->stencil_op == SR_STENCIL_KEEP)) return SR_EINVAL;
+        const uint64_t npx = (uint64_t)p->fb.width * p->fb.height;
+        slots += m->n_pad;
+        tris += m->n_indices / 3;
+        quads += (m->n_verts + 3) / 4;
+        blocks += (uint64_t)((p->fb.width + 31) / 32) * ((p->fb.height + 31) / 32);
+        if (it.clear) chunks += (npx + CLEAR_CHUNK - 1) / CLEAR_CHUNK;
+        px += npx;
+    }
+    if (slots >= (1ull << 31) || tris >= (1ull << 31) || blocks >= (1ull << 31) || chunks >= (1ull << 31))
+        return SR_EINVAL;
+    // the host table is reused: the previous batch must have consumed it
+    if (b->in_flight) {
+        SR_CK(cudaEventSynchronize(b->done));
+        b->in_flight = false;
+    }
+    const uint32_t NB = bucket_of(n);
+    const Layout L = layout_for(NB);
+    int rc;
+    if (L.bytes > b->htab_cap) {
+        if (b->htab) cudaFreeHost(b->htab);
+        b->htab = nullptr;
+        b->htab_cap = 0;
+        SR_CK(cudaMallocHost(&b->htab, L.bytes));
+        b->htab_cap = L.bytes;
+    }
+    if ((rc = grow(b, b->dtab, L.bytes)) || (rc = grow(b, b->scr4, slots + 4)) ||
+        (rc = grow(b, b->vary, (slots + 4) * VSTRIDE)) || (rc = grow(b, b->setup, 4 * (tris + 1))) ||
+        (rc = grow(b, b->area, tris + 1)) || (rc = grow(b, b->big_list, tris + 1)) ||
+        (rc = grow(b, b->unsafe_list, tris + 1)))
+        return rc;
+    // ---- host table
+    std::memset(b->htab, 0, L.bytes);
+    *reinterpret_cast<uint32_t*>(b->htab + L.off_n) = n;
+    BInst* hi = reinterpret_cast<BInst*>(b->htab + L.off_inst);
+    sr_uniforms* hu = reinterpret_cast<sr_uniforms*>(b->htab + L.off_U);
+    uint32_t* qb = reinterpret_cast<uint32_t*>(b->htab + L.off_q);
+    uint32_t* tb = reinterpret_cast<uint32_t*>(b->htab + L.off_t);
+    uint32_t* bb = reinterpret_cast<uint32_t*>(b->htab + L.off_b);
+    uint32_t* cb = reinterpret_cast<uint32_t*>(b->htab + L.off_c);
+    uint32_t vbase = 0;
+    qb[0] = tb[0] = bb[0] = cb[0] = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const sr_batch_item& it = items[i];
+        sr_pipeline* p = it.target;
+        const sr_draw* d = &it.draw;
+        const sr_mesh* m = d->mesh;
+        const uint32_t W = p->fb.width, H = p->fb.height;
+        const size_t npx = (size_t)W * H;
+        const size_t nblk = (size_t)((W + 31) / 32) * ((H + 31) / 32);
+        // the target's opaque scratch (zero between draws; zeroed when allocated)
+        const bool fresh = p->gkeys.cap < npx || p->bitmap.cap < (nblk + 31) / 32;
+        if ((rc = p->gkeys.ensure(npx)) || (rc = p->bitmap.ensure((nblk + 31) / 32))) return rc;
+        if (fresh) {
+            SR_CK(cudaMemsetAsync(p->gkeys.p, 0, p->gkeys.cap * 8, b->stream));
+            SR_CK(cudaMemsetAsync(p->bitmap.p, 0, p->bitmap.cap * 4, b->stream));
+        }
+        BInst& I = hi[i];
+        DrawParams& P = I.P;
+        P.W = W; P.H = H;
+        P.tile_w = d->tile_w; P.tile_h = d->tile_h;
+        P.ncols = W >= 2 ? (W - 1 + d->tile_w - 1) / d->tile_w : 0;
+        P.nrows = H >= 2 ? (H - 1 + d->tile_h - 1) / d->tile_h : 0;
+        P.n_verts = m->n_verts;
+        P.gen_base = m->n_pad;
+        P.n_in = (uint32_t)(m->n_indices / 3);
+        P.cull = d->cull;
+        P.vs = d->vs; P.fs = d->fs; P.blend = BLEND_REPLACE;
+        std::memcpy(P.vp, &d->viewport, sizeof(P.vp));
+        P.has_depth = p->depth != nullptr;
+        P.has_stencil = 0;
+        P.color_format = p->fb.color_format;
+        P.stencil_test = SR_STENCIL_ALWAYS; P.stencil_op = SR_STENCIL_KEEP; P.stencil_wrap = 1;
+        P.force_unsafe = p->force_unsafe ? 1u : 0u;
+        if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; }
+        P.tex_filter = d->tex_filter; P.tex_edge = d->tex_edge;
+        P.bin_w_log2 = 5; P.bin_h_log2 = 5;
+        P.bins_x = (W + 31) >> 5; P.bins_y = (H + 31) >> 5;
+        // the draw renders nothing when the frame has no semantic tile or a
+        // missing stencil attachment fails the test (as in sr_render)
+        const bool nothing = W < 2 || H < 2 || (!p->stencil && !stencil_test(p->stencil_test, 0, 0));
+        const uint32_t nt = nothing ? 0u : P.n_in;
+        P.n_raster_host = nt;
+        I.vpm = viewport_matrix(P.vp);
+        I.planes = m->planes;
+        I.indices = m->indices;
+        I.tex = d->texture ? d->texture->data : nullptr;
+        I.color = p->color;
+        I.depth = p->depth;
+        I.gkeys = p->gkeys.p;
+        I.bitmap = p->bitmap.p;
+        I.n_pad = m->n_pad;
+        I.vbase = vbase;
+        I.tbase = tb[i];
+        I.clear = it.clear ? 1u : 0u;
+        if (p->fb.color_format == SR_COLOR_RGBA32F) {
+            std::memcpy(&I.clear_color, it.clear_color, 16);
+        } else {
+            uint32_t c;
+            std::memcpy(&c, it.clear_color, 4);
+            I.clear_color = make_uint4(c, c, c, c);
+        }
+        I.mx = (uint32_t)((0x100000000ull + d->tile_w - 1) / d->tile_w);
+        I.my = (uint32_t)((0x100000000ull + d->tile_h - 1) / d->tile_h);
+        hu[i] = p->U;
+        vbase += m->n_pad;
+        qb[i + 1] = qb[i] + (nothing ? 0u : (m->n_verts + 3) / 4);
+        tb[i + 1] = tb[i] + nt;
+        bb[i + 1] = bb[i] + (nothing ? 0u : (uint32_t)nblk);
+        cb[i + 1] = cb[i] + (it.clear ? (uint32_t)((npx + CLEAR_CHUNK - 1) / CLEAR_CHUNK) : 0u);
+    }
+    // ---- configuration: forced, tuned for this size class, or the default
+    BatchConfig cfg;
+    if (b->forced.G) {
+        cfg = b->forced;
+    } else {
+        const uint64_t cls = ((uint64_t)NB << 40) | ((uint64_t)log2_floor(tris + 1) << 20) | log2_floor(px + 1);
+        auto f = b->tuned.find(cls);
+        if (f != b->tuned.end()) {
+            cfg = f->second;
+        } else if (b->autotune) {
+            cfg = tune(b, NB);
+            b->tuned[cls] = cfg;
+        }
+    }
+    if ((rc = launch_batch(b, NB, cfg))) return rc;
+    SR_CK(cudaEventRecord(b->done, b->stream));
+    b->in_flight = true;
+    b->last_cfg = cfg;
+    b->last_tris = tris;
+    b->stats_valid = false;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_batch_sync(sr_batch* b) {
+    if (!b) return SR_EINVAL;
+    SR_CK(cudaStreamSynchronize(b->stream));
+    if (!b->in_flight && b->stats_valid) return SR_OK;
+    b->in_flight = false;
+    SR_CK(cudaMemcpyAsync(b->hflags, b->flags, sizeof(DeviceFlags), cudaMemcpyDeviceToHost, b->stream));
+    SR_CK(cudaStreamSynchronize(b->stream));
+    const DeviceFlags& f = *b->hflags;
+    sr_stats& s = b->last;
+    std::memset(&s, 0, sizeof(s));
+    s.triangles_in = b->last_tris;
+    s.triangles_generated = b->last_tris;
+    s.triangles_raster = f.triangles_raster;
+    s.unsafe_triangles = f.unsafe;
+    s.fragments = f.fragments;
+    s.nan_bbox = f.nan_bbox;
+    s.kernel_launches = 7;
+    b->stats_valid = true;
+    if (f.bad_index) return SR_EINVAL;
+    if (f.nan_total) return SR_ENAN;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_batch_get_stats(sr_batch* b, sr_stats* out) {
+    if (!b || !out) return SR_EINVAL;
+    *out = b->last;
+    return SR_OK;
+}

@@ -1,0 +1,88 @@
+// sr_host.h — host-side internals shared by the C ABI translation units:
+// the pipeline object, grow-only device buffers and CUDA error plumbing.
+#pragma once
+#include <cstring>
+#include <vector>
+
+#include "sr_internal.cuh"
+
+namespace sr {
+
+// Last CUDA runtime error seen by this thread (kept for diagnostics).
+inline cudaError_t& last_cuda_error() {
+    static thread_local cudaError_t e = cudaSuccess;
+    return e;
+}
+
+// Grow-only device buffer (capacity in elements).
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t cap = 0;
+    int ensure(size_t n) {
+        if (n <= cap) return SR_OK;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        size_t want = n + n / 4 + 64;
+        cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+        if (e != cudaSuccess) { last_cuda_error() = e; p = nullptr; return SR_ENOMEM; }
+        cap = want;
+        return SR_OK;
+    }
+    void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
+};
+
+struct PendingDraw {
+    sr_draw d;
+    sr_uniforms U;
+    uint32_t stencil_test, stencil_op, stencil_wrap;
+};
+
+}  // namespace sr
+
+#define SR_CK(x)                                                        \
+    do {                                                                \
+        cudaError_t e_ = (x);                                           \
+        if (e_ != cudaSuccess) {                                        \
+            sr::last_cuda_error() = e_;                                 \
+            return e_ == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA; \
+        }                                                               \
+    } while (0)
+
+// The pipeline object behind the opaque sr_pipeline handle.
+struct sr_pipeline {
+    sr_fb_desc fb;
+    void* color = nullptr;
+    float* depth = nullptr;
+    uint8_t* stencil = nullptr;
+    sr_uniforms U;
+    uint32_t stencil_test = SR_STENCIL_ALWAYS, stencil_op = SR_STENCIL_KEEP, stencil_wrap = 1;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+    sr::DeviceFlags* flags = nullptr;     // device
+    sr::DeviceFlags* hflags = nullptr;    // pinned host mirror
+    // workspace
+    sr::DevBuf<float4> clip4, scr4;
+    sr::DevBuf<float> vary;
+    sr::DevBuf<unsigned long long> clip_counts, clip_offsets, clip_tmp;
+    sr::DevBuf<uint32_t> refs;
+    sr::DevBuf<float4> setup;
+    sr::DevBuf<uint2> binrect;
+    sr::DevBuf<uint32_t> bin_counts, bin_off, bin_cursor, bin_tmp, entries, unsafe_list;
+    sr::DevBuf<unsigned long long> area, gkeys;
+    sr::DevBuf<uint32_t> big_list;
+    sr::DevBuf<uint32_t> bitmap;
+    sr::DevBuf<int> st_diff, st_lines;
+    sr::DevBuf<unsigned long long> st_glob;
+    // capacities (elements) requested for the generated geometry
+    uint64_t gen_tri_cap = 0, gen_vert_cap = 0, entry_cap = 0;
+    std::vector<sr::PendingDraw> pending;
+    sr_stats last_stats;
+    bool stats_valid = false;
+    bool force_unsafe = false;   // SR_FORCE_UNSAFE=1: every primitive takes the exact unsafe path
+    bool profiling = false;
+    cudaEvent_t ev[6] = {};
+    uint32_t last_launches = 0;
+    bool last_profiled = false;
+};

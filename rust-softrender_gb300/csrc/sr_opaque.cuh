@@ -1,0 +1,175 @@
+// sr_opaque.cuh — device code of the opaque raster path shared by the
+// per-draw kernels (sr_opaque.cu) and the batched kernels (sr_batch.cu).
+#pragma once
+#include "sr_internal.cuh"
+#include "sr_shade.cuh"
+
+namespace sr {
+
+constexpr int RG_THREADS = 256;
+constexpr uint32_t TOUCH_LOG2 = 5;               // touched-block bitmap granularity: 32 x 32
+
+__device__ __forceinline__ bool surely_negative(float n, float det) {
+    return (n * det < 0.0f) && fabsf(n) > 1.0e-18f && fabsf(det) < 1.0e18f;
+}
+
+__device__ __forceinline__ void mark_touched(uint32_t* bitmap, uint32_t blocks_x, uint32_t px, uint32_t py) {
+    uint32_t b = (py >> TOUCH_LOG2) * blocks_x + (px >> TOUCH_LOG2);
+    uint32_t bit = 1u << (b & 31);
+    if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);   // a stale read only costs an extra atomic
+}
+
+// ceil(2^32 / t): floor(p / t) == __umulhi(p, m) for p, t < 2^16
+__device__ __forceinline__ uint32_t div_magic(uint32_t t) { return (uint32_t)((0x100000000ull + t - 1) / t); }
+// number of semantic tiles along one axis containing coordinate p (1 or 2)
+__device__ __forceinline__ int seam_count(uint32_t p, uint32_t t, uint32_t m, uint32_t last) {
+    return (p > 0 && p < last && __umulhi(p, m) * t == p) ? 2 : 1;
+}
+// mark the 32x32 blocks of a clamped bbox as touched
+__device__ __forceinline__ void mark_rect(uint32_t* bitmap, uint32_t blocks_x, uint32_t x0, uint32_t y0, uint32_t x1,
+                                          uint32_t y1) {
+    for (uint32_t by = y0 >> TOUCH_LOG2; by <= (y1 >> TOUCH_LOG2); ++by)
+        for (uint32_t bx = x0 >> TOUCH_LOG2; bx <= (x1 >> TOUCH_LOG2); ++bx) {
+            const uint32_t b = by * blocks_x + bx, bit = 1u << (b & 31);
+            if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);
+        }
+}
+
+// Exact test of one (primitive, pixel) item; emits the fragment key.
+__device__ __forceinline__ void rg_fragment(const DrawParams& P, float4 r0, float4 r1, float4 r2, uint32_t t,
+                                            uint32_t px, uint32_t py, uint32_t N,
+                                            unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap,
+                                            const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
+                                            uint32_t mx, uint32_t my, unsigned long long& frags) {
+    const float x = (float)px + 0.5f, y = (float)py + 0.5f;
+    const float dx = x - r1.x, dy = y - r1.y;
+    const float nu = r0.x * dx + r0.y * dy;
+    if (surely_negative(nu, r1.z)) return;
+    const float nv = r0.z * dx + r0.w * dy;
+    if (surely_negative(nv, r1.z)) return;
+    const float u = nu / r1.z, v = nv / r1.z;
+    const float w = 1.0f - u - v;
+    if (u < 0.0f || v < 0.0f || w < 0.0f) return;
+    const float z = (r1.w * u + r2.x * v) + r2.y * w;
+    if (!(z < 0.0f)) return;
+    const size_t gi = (size_t)py * P.W + px;
+    if (gate_with_stencil && !stencil_test(P.stencil_test, __ldg(stencil + gi), P.sref)) return;
+    const int kp = seam_count(px, P.tile_w, mx, P.W - 1) * seam_count(py, P.tile_h, my, P.H - 1);
+    ++frags;
+    const uint32_t zk = P.has_depth ? zkey(z) : 0u;
+    atomicMax(gkeys + gi, ((unsigned long long)zk << 32) | (unsigned long long)((uint32_t)(kp - 1) * N + t + 1u));
+}
+
+constexpr uint32_t RG_BIG = 2048;   // bbox pixels above which a primitive goes to the block-cooperative pass
+
+// Extension fragments of one unsafe primitive t (see ext_direct_kernel): the
+// warp's lanes stride over the semantic tiles.
+__device__ __forceinline__ void ext_prim(const DrawParams& P, uint32_t t, uint32_t N, const float4* __restrict__ setup,
+                                         unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap,
+                                         const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
+                                         uint32_t lane, unsigned long long& frags) {
+    const uint32_t ntiles = P.ncols * P.nrows;
+    const uint32_t blocks_x = (P.W + 31) >> 5;
+    const float4* r = setup + 4 * (size_t)t;
+    const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+    const int ix0 = __float_as_int(r3.x), iy0 = __float_as_int(r3.y);
+    const int ix1 = __float_as_int(r3.z), iy1 = __float_as_int(r3.w);
+    for (uint32_t ti = lane; ti < ntiles; ti += 32) {
+        const uint32_t C = ti % P.ncols, R = ti / P.ncols;
+        const uint32_t lx = C * P.tile_w, hx = min((C + 1) * P.tile_w, P.W - 1);
+        const uint32_t ly = R * P.tile_h, hy = min((R + 1) * P.tile_h, P.H - 1);
+        if (ix1 >= (int)lx && ix0 <= (int)hx && iy1 >= (int)ly && iy0 <= (int)hy) continue;
+        const uint32_t cx0 = ix0 < (int)lx ? lx : (ix0 > (int)hx ? hx : (uint32_t)ix0);
+        const uint32_t cx1 = ix1 < (int)lx ? lx : (ix1 > (int)hx ? hx : (uint32_t)ix1);
+        const uint32_t cy0 = iy0 < (int)ly ? ly : (iy0 > (int)hy ? hy : (uint32_t)iy0);
+        const uint32_t cy1 = iy1 < (int)ly ? ly : (iy1 > (int)hy ? hy : (uint32_t)iy1);
+        if (segment_cleared(r0, r1, cx0, cy0, cx1, cy1)) continue;
+        for (uint32_t py = cy0; py <= cy1; ++py) {
+            for (uint32_t px = cx0; px <= cx1; ++px) {
+                const float x = (float)px + 0.5f, y = (float)py + 0.5f;
+                const float dx = x - r1.x, dy = y - r1.y;
+                const float u = (r0.x * dx + r0.y * dy) / r1.z;
+                const float v = (r0.z * dx + r0.w * dy) / r1.z;
+                const float w = 1.0f - u - v;
+                if (u < 0.0f || v < 0.0f || w < 0.0f) continue;
+                const float z = (r1.w * u + r2.x * v) + r2.y * w;
+                if (!(z < 0.0f)) continue;
+                const size_t gi = (size_t)py * P.W + px;
+                if (gate_with_stencil && !stencil_test(P.stencil_test, __ldg(stencil + gi), P.sref)) continue;
+                // rank of tile (R, C) among the tiles containing the pixel
+                TileSpan cs = tiles_of(px, P.tile_w, P.ncols, P.W - 1);
+                TileSpan rs = tiles_of(py, P.tile_h, P.nrows, P.H - 1);
+                const int rank = (int)(R - rs.first) * cs.count + (int)(C - cs.first);
+                if (rank == cs.count * rs.count - 1) ++frags;
+                const uint32_t zk = P.has_depth ? zkey(z) : 0u;
+                atomicMax(gkeys + gi, ((unsigned long long)zk << 32) |
+                                          (unsigned long long)((uint32_t)rank * N + t + 1u));
+                mark_touched(bitmap, blocks_x, px, py);
+            }
+        }
+    }
+}
+
+// Resolve of one touched 32x32 block b: each pixel's winning key against the
+// depth the draw started from, barycentrics of the winner recomputed, its
+// varyings interpolated and shaded, colour and depth written once; the keys
+// and the block's bitmap bit are reset for the next draw.
+template <int FS, int FMT>
+__device__ __forceinline__ void resolve_block(const DrawParams& P, const sr_uniforms& U, uint32_t b, uint32_t N,
+                                              const float4* __restrict__ setup, const uint32_t* __restrict__ vidx,
+                                              const float* __restrict__ vary, const uint32_t* __restrict__ tex,
+                                              void* __restrict__ color, float* __restrict__ depth,
+                                              const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
+                                              unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap) {
+    const uint32_t blocks_x = (P.W + 31) >> 5;
+    const uint32_t X0 = (b % blocks_x) << 5, Y0 = (b / blocks_x) << 5;
+    const uint32_t bw = min(32u, P.W - X0), bh = min(32u, P.H - Y0);
+    for (uint32_t i = threadIdx.x; i < 1024; i += blockDim.x) {
+        const uint32_t lx = i & 31, ly = i >> 5;
+        if (lx >= bw || ly >= bh) continue;
+        const uint32_t px = X0 + lx, py = Y0 + ly;
+        const size_t gi = (size_t)py * P.W + px;
+        const unsigned long long k = gkeys[gi];
+        if (k == 0) continue;
+        gkeys[gi] = 0;
+        if (P.has_depth) {
+            const float d0 = depth[gi];
+            if (isnan(d0) || (uint32_t)(k >> 32) < zkey(d0)) continue;
+        }
+        if (gate_with_stencil && !stencil_test(P.stencil_test, stencil[gi], P.sref)) continue;
+        const uint32_t t = ((uint32_t)(k & 0xffffffffull) - 1u) % N;
+        const float4* r = setup + 4 * (size_t)t;
+        const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2);
+        const float x = (float)px + 0.5f, y = (float)py + 0.5f;
+        const float dx = x - r1.x, dy = y - r1.y;
+        const float u = (r0.x * dx + r0.y * dy) / r1.z;
+        const float v = (r0.z * dx + r0.w * dy) / r1.z;
+        const float w = 1.0f - u - v;
+        const float z = (r1.w * u + r2.x * v) + r2.y * w;
+        constexpr int NK = FS == FS_TEXTURED_BLINN_PHONG ? 10 : FS == FS_VERTEX_COLOR ? 4 : FS == FS_CONSTANT_COLOR ? 0 : 8;
+        float kv[12];
+        if (NK > 0) {
+            const uint32_t a = __ldg(vidx + 3 * (size_t)t), bq = __ldg(vidx + 3 * (size_t)t + 1),
+                           c = __ldg(vidx + 3 * (size_t)t + 2);
+            const float4* ka = reinterpret_cast<const float4*>(vary + (size_t)a * VSTRIDE);
+            const float4* kb = reinterpret_cast<const float4*>(vary + (size_t)bq * VSTRIDE);
+            const float4* kc = reinterpret_cast<const float4*>(vary + (size_t)c * VSTRIDE);
+#pragma unroll
+            for (int q = 0; q < (NK + 3) / 4; ++q) {
+                const float4 xa = __ldg(ka + q), xb = __ldg(kb + q), xc = __ldg(kc + q);
+                kv[4 * q + 0] = (xa.x * u + xb.x * v) + xc.x * w;
+                kv[4 * q + 1] = (xa.y * u + xb.y * v) + xc.y * w;
+                kv[4 * q + 2] = (xa.z * u + xb.z * v) + xc.z * w;
+                kv[4 * q + 3] = (xa.w * u + xb.w * v) + xc.w * w;
+            }
+        }
+        const sr_v4 col = shade_fs<FS>(U, kv, tex, P);
+        if (FMT == SR_COLOR_RGBA32F) reinterpret_cast<float4*>(color)[gi] = make_float4(col.x, col.y, col.z, col.w);
+        else if (FMT == SR_COLOR_RGBA8) reinterpret_cast<uint32_t*>(color)[gi] = sr_to_rgba8(col);
+        if (P.has_depth) depth[gi] = z;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAnd(bitmap + (b >> 5), ~(1u << (b & 31)));
+}
+
+}  // namespace sr

@@ -362,3 +362,101 @@ def render_scene(scene, initial=None):
     if tex is not None:
         tex.free()
     return color, depth, stencil, stats, status
+
+
+def draw_for_scene(scene, mesh, tex=None):
+    """The sr_draw that submit_scene() hands to sr_render, built directly
+    (for sr_batch_render, which takes the descriptors of many draws)."""
+    d = A.SrDraw()
+    lib().sr_draw_init(C.byref(d))
+    d.mesh = mesh.handle.value if isinstance(mesh.handle, C.c_void_p) else mesh.handle
+    d.prim = scene.prim
+    d.vs = shader_id(scene.vs, A.SR_STAGE_VERTEX)
+    d.gs_mode = scene.gs_mode
+    if scene.gs_mode == A.SR_GS_CLIP:
+        d.gs = shader_id("clip", A.SR_STAGE_GEOMETRY)
+    elif scene.gs_mode == A.SR_GS_NAMED:
+        d.gs = shader_id(scene.gs, A.SR_STAGE_GEOMETRY)
+    d.viewport = A.SrViewport(*scene.viewport)
+    d.cull = scene.cull
+    d.fs = shader_id(scene.fs, A.SR_STAGE_FRAGMENT)
+    d.blend = shader_id(scene.blend, A.SR_STAGE_BLEND)
+    d.aa_lines = 1 if scene.aa_lines else 0
+    d.tile_w, d.tile_h = scene.tile
+    d.stencil_ref = scene.stencil_ref
+    if tex is not None:
+        d.texture = tex.handle.value if isinstance(tex.handle, C.c_void_p) else tex.handle
+    d.tex_filter, d.tex_edge = scene.tex_filter, scene.tex_edge
+    return d
+
+
+class Batch:
+    """Batched opaque draws (sr_batch_*): one launch per stage renders many
+    pipelines' draws; the launch sequence is replayed as a CUDA graph and its
+    launch configuration tuned per batch size class."""
+
+    def __init__(self, use_graphs=True, autotune=True):
+        h = C.c_void_p()
+        check(lib().sr_batch_create(C.byref(h)), "sr_batch_create")
+        self.handle = h
+        self.set_options(use_graphs, autotune)
+        self._keep = None
+
+    def set_options(self, use_graphs=True, autotune=True):
+        check(lib().sr_batch_set_options(self.handle, 1 if use_graphs else 0, 1 if autotune else 0),
+              "sr_batch_set_options")
+
+    def set_stream(self, stream_ptr):
+        check(lib().sr_batch_set_stream(self.handle, C.c_void_p(stream_ptr) if stream_ptr else None),
+              "sr_batch_set_stream")
+
+    def set_config(self, prims_per_warp=0, big_threshold=0, ctas_per_sm=0):
+        check(lib().sr_batch_set_config(self.handle, prims_per_warp, big_threshold, ctas_per_sm),
+              "sr_batch_set_config")
+
+    def config(self):
+        v = [C.c_uint32() for _ in range(3)]
+        check(lib().sr_batch_get_config(self.handle, *[C.byref(x) for x in v]), "sr_batch_get_config")
+        return tuple(x.value for x in v)
+
+    @staticmethod
+    def items(entries):
+        """entries: (pipeline, SrDraw, clear_bytes or None) -> ctypes array."""
+        arr = (A.SrBatchItem * len(entries))()
+        for i, (pl, d, clear) in enumerate(entries):
+            arr[i].target = pl.handle.value if isinstance(pl.handle, C.c_void_p) else pl.handle
+            arr[i].draw = d
+            arr[i].clear = 1 if clear is not None else 0
+            if clear is not None:
+                b = bytes(clear)
+                for k in range(len(b)):
+                    arr[i].clear_color[k] = b[k]
+        return arr
+
+    def render_items(self, arr):
+        """Enqueues a prepared item array (returns the status)."""
+        self._keep = arr
+        return lib().sr_batch_render(self.handle, arr, len(arr))
+
+    def render(self, entries):
+        st = self.render_items(self.items(entries))
+        check(st, "sr_batch_render")
+
+    def sync(self):
+        return lib().sr_batch_sync(self.handle)
+
+    def stats(self):
+        s = A.SrStats()
+        check(lib().sr_batch_get_stats(self.handle, C.byref(s)), "sr_batch_get_stats")
+        return {f: getattr(s, f) for f, _ in A.SrStats._fields_ if f != "stage_ms"}
+
+    def destroy(self):
+        if self.handle:
+            lib().sr_batch_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

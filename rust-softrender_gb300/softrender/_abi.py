@@ -69,6 +69,10 @@ class SrDraw(C.Structure):
     ]
 
 
+class SrBatchItem(C.Structure):
+    _fields_ = [("target", C.c_void_p), ("draw", SrDraw), ("clear", C.c_uint32), ("clear_color", C.c_uint8 * 16)]
+
+
 class SrStats(C.Structure):
     _fields_ = [
         ("triangles_in", C.c_uint64), ("triangles_generated", C.c_uint64),

@@ -38,6 +38,16 @@ SIGNATURES = {
     "sr_render": (C.c_int, [C.c_void_p, C.POINTER(A.SrDraw)]),
     "sr_sync": (C.c_int, [C.c_void_p]),
     "sr_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.SrStats)]),
+    "sr_batch_create": (C.c_int, [C.POINTER(C.c_void_p)]),
+    "sr_batch_destroy": (C.c_int, [C.c_void_p]),
+    "sr_batch_set_stream": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sr_batch_set_options": (C.c_int, [C.c_void_p, C.c_int, C.c_int]),
+    "sr_batch_set_config": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32]),
+    "sr_batch_get_config": (C.c_int, [C.c_void_p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32),
+                                      C.POINTER(C.c_uint32)]),
+    "sr_batch_render": (C.c_int, [C.c_void_p, C.POINTER(A.SrBatchItem), C.c_uint32]),
+    "sr_batch_sync": (C.c_int, [C.c_void_p]),
+    "sr_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.SrStats)]),
     "sr_render_static": (C.c_int, [C.POINTER(A.SrDraw), C.c_void_p, C.c_size_t, C.c_void_p, C.c_uint32, C.c_uint32,
                                    C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32,
                                    C.POINTER(A.SrFbDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
