@@ -227,10 +227,13 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
     const uint32_t n = *T.n;
     const uint32_t total = __ldg(T.tbase + n);
     const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long frags = 0;
-    for (uint32_t t0 = warp * G; t0 < total; t0 += nwarps * G) {
+    for (;;) {
+        // dynamic work queue: a warp takes the next G batch primitives
+        uint32_t t0 = 0;
+        if (lane == 0) t0 = (uint32_t)min(atomicAdd(&flags->work_raster, (unsigned long long)G), 0xffffffffull);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= total) break;
         const uint32_t g = t0 + lane;
         uint32_t a = 0;
         if (lane < G && g < total) {
@@ -352,10 +355,17 @@ __global__ void __launch_bounds__(256) batch_ext_kernel(BTables T, const float4*
 // resolve_kernel over (draw, touched 32x32 block) items; the fragment shader
 // and colour format are dispatched per draw.
 __global__ void __launch_bounds__(256) batch_resolve_kernel(BTables T, const float4* __restrict__ setup,
-                                                            const float* __restrict__ vary) {
+                                                            const float* __restrict__ vary, DeviceFlags* flags) {
+    __shared__ uint32_t s_item;
     const uint32_t n = *T.n;
     const uint32_t total = __ldg(T.bbase + n);
-    for (uint32_t j = blockIdx.x; j < total; j += gridDim.x) {
+    for (;;) {
+        // dynamic work queue: the CTA takes the next (draw, block) item
+        if (threadIdx.x == 0) s_item = (uint32_t)min(atomicAdd(&flags->work_resolve, 1ull), 0xffffffffull);
+        __syncthreads();
+        const uint32_t j = s_item;
+        __syncthreads();
+        if (j >= total) break;
         const uint32_t i = owner_of(T.bbase, n, j);
         const BInst& I = T.inst[i];
         const uint32_t b = j - __ldg(T.bbase + i);
@@ -387,8 +397,6 @@ __global__ void __launch_bounds__(256) batch_resolve_kernel(BTables T, const flo
 using namespace sr;
 
 namespace {
-
-constexpr uint32_t BATCH_SMS = 152;
 
 struct BatchConfig {
     uint32_t G = 32;          // primitives per warp in the raster pass
@@ -501,11 +509,12 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     const BTables T = tables_at(b->dtab.p, L);
     cudaMemcpyAsync(b->dtab.p, b->htab, L.bytes, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(b->flags, 0, sizeof(DeviceFlags), st);
-    batch_clear_kernel<<<BATCH_SMS * 8, 256, 0, st>>>(T);
-    batch_vertex_kernel<<<BATCH_SMS * 16, 128, 0, st>>>(T, b->scr4.p, b->vary.p);
-    batch_setup_kernel<<<BATCH_SMS * 8, 256, 0, st>>>(T, b->scr4.p, b->setup.p, b->area.p, b->unsafe_list.p, b->flags);
-    const dim3 rg(BATCH_SMS * c.ctas);
-#define SR_BRS(g) batch_raster_small_kernel<g><<<rg, 256, 0, st>>>(T, b->setup.p, b->area.p, c.big, b->big_list.p, b->flags)
+    batch_clear_kernel<<<resident_grid(batch_clear_kernel, 256, 8), 256, 0, st>>>(T);
+    batch_vertex_kernel<<<resident_grid(batch_vertex_kernel, 128, 16), 128, 0, st>>>(T, b->scr4.p, b->vary.p);
+    batch_setup_kernel<<<resident_grid(batch_setup_kernel, 256, 8), 256, 0, st>>>(T, b->scr4.p, b->setup.p, b->area.p,
+                                                                                b->unsafe_list.p, b->flags);
+#define SR_BRS(g) batch_raster_small_kernel<g><<<resident_grid(batch_raster_small_kernel<g>, 256, (int)c.ctas), 256, 0, st>>>( \
+        T, b->setup.p, b->area.p, c.big, b->big_list.p, b->flags)
     switch (c.G) {
     case 1: SR_BRS(1); break;
     case 2: SR_BRS(2); break;
@@ -515,9 +524,9 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     default: SR_BRS(32); break;
     }
 #undef SR_BRS
-    batch_raster_big_kernel<<<BATCH_SMS * 2, 256, 0, st>>>(T, b->setup.p, b->area.p, b->big_list.p, b->flags);
-    batch_ext_kernel<<<BATCH_SMS * 4, 256, 0, st>>>(T, b->setup.p, b->unsafe_list.p, b->flags);
-    batch_resolve_kernel<<<BATCH_SMS * 8, 256, 0, st>>>(T, b->setup.p, b->vary.p);
+    batch_raster_big_kernel<<<resident_grid(batch_raster_big_kernel, 256, 2), 256, 0, st>>>(T, b->setup.p, b->area.p, b->big_list.p, b->flags);
+    batch_ext_kernel<<<resident_grid(batch_ext_kernel, 256, 4), 256, 0, st>>>(T, b->setup.p, b->unsafe_list.p, b->flags);
+    batch_resolve_kernel<<<resident_grid(batch_resolve_kernel, 256, 8), 256, 0, st>>>(T, b->setup.p, b->vary.p, b->flags);
 }
 
 int launch_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {

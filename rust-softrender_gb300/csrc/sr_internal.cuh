@@ -61,6 +61,8 @@ struct DeviceFlags {
     unsigned long long n_big;          // primitives on the large-bbox list (opaque path)
     unsigned int nan_bbox;
     unsigned int pad;
+    unsigned long long work_raster;    // next primitive to hand out (dynamic raster work queue)
+    unsigned long long work_resolve;   // next block to hand out (batched resolve)
 };
 constexpr size_t FLAGS_STATS_OFFSET = 48;
 static_assert(offsetof(DeviceFlags, triangles_generated) == FLAGS_STATS_OFFSET, "DeviceFlags layout");
@@ -220,6 +222,26 @@ struct sr_texture {
     uint32_t* data;
     uint32_t w, h;
 };
+
+// ------------------------------------------------------- grid sizing (host)
+// Streaming-multiprocessor count of the current device (cached per device).
+inline int sm_count() {
+    static int n[64] = {0};
+    int d = 0;
+    if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= 64) d = 0;
+    if (!n[d] && (cudaDeviceGetAttribute(&n[d], cudaDevAttrMultiProcessorCount, d) != cudaSuccess || n[d] <= 0))
+        n[d] = 152;
+    return n[d];
+}
+// Grid of a persistent (grid-stride) kernel: as many CTAs as can be resident
+// at once (at most max_per_sm per SM), so no CTA waits for another to exit.
+template <typename K>
+inline unsigned resident_grid(K kernel, int threads, int max_per_sm) {
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kernel, threads, 0) != cudaSuccess || nb <= 0) nb = 1;
+    if (nb > max_per_sm) nb = max_per_sm;
+    return (unsigned)nb * (unsigned)sm_count();
+}
 
 // ---------------------------------------------------------------- launches
 // Kernel launchers implemented in the .cu files (host-callable).

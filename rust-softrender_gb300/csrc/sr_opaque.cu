@@ -45,12 +45,15 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
     if (flags->poison) return;
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
     const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long frags = 0;
     const uint32_t mx = div_magic(P.tile_w), my = div_magic(P.tile_h);
     const uint32_t blocks_x = (P.W + 31) >> 5;
-    for (uint32_t t0 = warp * G; t0 < N; t0 += nwarps * G) {
+    for (;;) {
+        // dynamic work queue: a warp takes the next G primitives
+        uint32_t t0 = 0;
+        if (lane == 0) t0 = (uint32_t)min(atomicAdd(&flags->work_raster, (unsigned long long)G), 0xffffffffull);
+        t0 = __shfl_sync(0xffffffffu, t0, 0);
+        if (t0 >= N) break;
         const uint32_t t = t0 + lane;
         uint32_t a = 0;
         if (lane < G && t < N) {
@@ -203,7 +206,8 @@ int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A
     const uint32_t n_est = P.n_raster_host ? P.n_raster_host : P.n_in;
     uint32_t G = 32;
     while (G > 1 && n_est / G < 152u * 48u) G >>= 1;
-#define SR_RS(g) raster_small_kernel<g><<<152 * 8, RG_THREADS, 0, st>>>(P, A.setup, A.area, A.gkeys, A.bitmap, \
+#define SR_RS(g) raster_small_kernel<g><<<resident_grid(raster_small_kernel<g>, RG_THREADS, 8), RG_THREADS, 0, st>>>( \
+        P, A.setup, A.area, A.gkeys, A.bitmap, \
                                                                       A.stencil, A.gate, A.big_list, A.flags)
     switch (G) {
     case 1: SR_RS(1); break;
@@ -214,9 +218,9 @@ int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A
     default: SR_RS(32); break;
     }
 #undef SR_RS
-    raster_big_kernel<<<152 * 2, RG_THREADS, 0, st>>>(P, A.setup, A.area, A.gkeys, A.bitmap, A.stencil, A.gate,
+    raster_big_kernel<<<resident_grid(raster_big_kernel, RG_THREADS, 2), RG_THREADS, 0, st>>>(P, A.setup, A.area, A.gkeys, A.bitmap, A.stencil, A.gate,
                                                        A.big_list, A.flags);
-    ext_direct_kernel<<<152 * 4, 256, 0, st>>>(P, A.unsafe_list, A.setup, A.gkeys, A.bitmap, A.stencil, A.gate, A.flags);
+    ext_direct_kernel<<<resident_grid(ext_direct_kernel, 256, 4), 256, 0, st>>>(P, A.unsafe_list, A.setup, A.gkeys, A.bitmap, A.stencil, A.gate, A.flags);
     switch (P.fs) {
     case FS_BLINN_PHONG_DIR: launch_resolve_fs<FS_BLINN_PHONG_DIR>(P, U, A, st); break;
     case FS_TEXTURED_BLINN_PHONG: launch_resolve_fs<FS_TEXTURED_BLINN_PHONG>(P, U, A, st); break;
