@@ -73,6 +73,14 @@ __device__ __forceinline__ uint32_t owner_of(const uint32_t* __restrict__ base, 
     return lo;
 }
 
+// Owner of item j when the owner of an item j0 <= j is known to be i0 (the
+// items of a warp are consecutive, so this is usually 0 or 1 step).
+__device__ __forceinline__ uint32_t owner_from(const uint32_t* __restrict__ base, uint32_t n, uint32_t i0, uint32_t j) {
+    uint32_t i = i0;
+    while (i + 1 < n && __ldg(base + i + 1) <= j) ++i;
+    return i;
+}
+
 // ---------------------------------------------------------------- clear
 __global__ void __launch_bounds__(256) batch_clear_kernel(BTables T) {
     const uint32_t n = *T.n;
@@ -218,11 +226,20 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
                                                                  const unsigned long long* __restrict__ area,
                                                                  uint32_t big_threshold,
                                                                  uint32_t* __restrict__ big_list, DeviceFlags* flags) {
+    // per staged primitive: record, bbox origin and width, and the scalars of
+    // its draw's target (so the per-pixel loop reads no global tables)
+    struct Slot {
+        uint32_t wh;        // W | H << 16
+        uint32_t tiles;     // tile_w | tile_h << 16
+        uint32_t mx, my;
+        uint32_t n_depth;   // N | has_depth << 31
+        uint32_t t;         // primitive index within the draw
+        unsigned long long* gkeys;
+    };
     __shared__ float4 srec[8][32][3];
     __shared__ uint32_t sxy[8][32];
     __shared__ uint32_t sw[8][32];
-    __shared__ uint32_t sid[8][32];                  // draw index
-    __shared__ uint32_t stl[8][32];                  // primitive index within the draw
+    __shared__ Slot sslot[8][32];
     __shared__ unsigned long long smag[8][32];
     const uint32_t n = *T.n;
     const uint32_t total = __ldg(T.tbase + n);
@@ -230,10 +247,14 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
     unsigned long long frags = 0;
     for (;;) {
         // dynamic work queue: a warp takes the next G batch primitives
-        uint32_t t0 = 0;
-        if (lane == 0) t0 = (uint32_t)min(atomicAdd(&flags->work_raster, (unsigned long long)G), 0xffffffffull);
+        uint32_t t0 = 0, i0 = 0;
+        if (lane == 0) {
+            t0 = (uint32_t)min(atomicAdd(&flags->work_raster, (unsigned long long)G), 0xffffffffull);
+            if (t0 < total) i0 = owner_of(T.tbase, n, t0);
+        }
         t0 = __shfl_sync(0xffffffffu, t0, 0);
         if (t0 >= total) break;
+        i0 = __shfl_sync(0xffffffffu, i0, 0);
         const uint32_t g = t0 + lane;
         uint32_t a = 0;
         if (lane < G && g < total) {
@@ -242,23 +263,31 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
                 big_list[atomicAdd(&flags->n_big, 1ull)] = g;
             } else if (at) {
                 a = (uint32_t)at;
-                const uint32_t i = owner_of(T.tbase, n, g);
+                const uint32_t i = owner_from(T.tbase, n, i0, g);
                 const BInst& I = T.inst[i];
                 const float4* r = setup + 4 * (size_t)g;
                 srec[wl][lane][0] = __ldg(r);
                 srec[wl][lane][1] = __ldg(r + 1);
                 srec[wl][lane][2] = __ldg(r + 2);
                 const float4 r3 = __ldg(r + 3);
+                const uint32_t W = I.P.W, H = I.P.H;
                 const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
                 const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
-                const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)I.P.W - 1);
-                const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)I.P.H - 1);
+                const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)W - 1);
+                const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)H - 1);
                 const uint32_t w = x1 - x0 + 1;
-                mark_rect(I.bitmap, (I.P.W + 31) >> 5, x0, y0, x1, y1);
+                mark_rect(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1);
                 sxy[wl][lane] = x0 | (y0 << 16);
                 sw[wl][lane] = w;
-                sid[wl][lane] = i;
-                stl[wl][lane] = g - I.tbase;
+                Slot S;
+                S.wh = W | (H << 16);
+                S.tiles = I.P.tile_w | (I.P.tile_h << 16);
+                S.mx = I.mx;
+                S.my = I.my;
+                S.n_depth = I.P.n_raster_host | (I.P.has_depth ? 0x80000000u : 0u);
+                S.t = g - I.tbase;
+                S.gkeys = I.gkeys;
+                sslot[wl][lane] = S;
                 smag[wl][lane] = ((1ull << 32) + w - 1) / w;
             }
         }
@@ -281,10 +310,11 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
                 const uint32_t w = sw[wl][lo];
                 const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][lo]) >> 32);  // local / w
                 const uint32_t xy = sxy[wl][lo];
-                const BInst& I = T.inst[sid[wl][lo]];
-                rg_fragment(I.P, srec[wl][lo][0], srec[wl][lo][1], srec[wl][lo][2], stl[wl][lo],
-                            (xy & 0xffffu) + (local - row * w), (xy >> 16) + row, I.P.n_raster_host, I.gkeys,
-                            I.bitmap, nullptr, 0u, I.mx, I.my, frags);
+                const Slot& S = sslot[wl][lo];
+                frag_emit(S.wh & 0xffffu, S.wh >> 16, S.tiles & 0xffffu, S.tiles >> 16, S.mx, S.my,
+                          (S.n_depth >> 31) != 0, srec[wl][lo][0], srec[wl][lo][1], srec[wl][lo][2], S.t,
+                          (xy & 0xffffu) + (local - row * w), (xy >> 16) + row, S.n_depth & 0x7fffffffu, S.gkeys,
+                          nullptr, 0u, 0u, 0u, frags);
             }
         }
         __syncwarp();
@@ -352,42 +382,30 @@ __global__ void __launch_bounds__(256) batch_ext_kernel(BTables T, const float4*
 }
 
 // ---------------------------------------------------------------- resolve
-// resolve_kernel over (draw, touched 32x32 block) items; the fragment shader
-// and colour format are dispatched per draw.
+// resolve_kernel over (draw, touched 32x32 block) items, one launch per
+// (fragment shader, colour format) pair present in the batch; a launch skips
+// the draws of other pairs.  CTAs take items from a work queue.
+template <int FS, int FMT>
 __global__ void __launch_bounds__(256) batch_resolve_kernel(BTables T, const float4* __restrict__ setup,
-                                                            const float* __restrict__ vary, DeviceFlags* flags) {
+                                                            const float* __restrict__ vary,
+                                                            unsigned long long* __restrict__ queue) {
     __shared__ uint32_t s_item;
     const uint32_t n = *T.n;
     const uint32_t total = __ldg(T.bbase + n);
     for (;;) {
-        // dynamic work queue: the CTA takes the next (draw, block) item
-        if (threadIdx.x == 0) s_item = (uint32_t)min(atomicAdd(&flags->work_resolve, 1ull), 0xffffffffull);
+        if (threadIdx.x == 0) s_item = (uint32_t)min(atomicAdd(queue, 1ull), 0xffffffffull);
         __syncthreads();
         const uint32_t j = s_item;
         __syncthreads();
         if (j >= total) break;
         const uint32_t i = owner_of(T.bbase, n, j);
         const BInst& I = T.inst[i];
+        if (I.P.fs != FS || (int)I.P.color_format != FMT) continue;
         const uint32_t b = j - __ldg(T.bbase + i);
         if (!(I.bitmap[b >> 5] & (1u << (b & 31)))) continue;
-        const float4* su = setup + 4 * (size_t)I.tbase;
-        const float* vy = vary + (size_t)I.vbase * VSTRIDE;
-        const uint32_t N = I.P.n_raster_host;
-#define SR_BR(FS, FMT) resolve_block<FS, FMT>(I.P, T.U[i], b, N, su, I.indices, vy, I.tex, I.color, I.depth, \
-                                              nullptr, 0u, I.gkeys, I.bitmap)
-#define SR_BR_FS(FS)                                                        \
-        if (I.P.color_format == SR_COLOR_RGBA8) SR_BR(FS, SR_COLOR_RGBA8);   \
-        else if (I.P.color_format == SR_COLOR_RGBA32F) SR_BR(FS, SR_COLOR_RGBA32F); \
-        else SR_BR(FS, SR_COLOR_NONE);
-        switch (I.P.fs) {
-        case FS_BLINN_PHONG_DIR: SR_BR_FS(FS_BLINN_PHONG_DIR) break;
-        case FS_TEXTURED_BLINN_PHONG: SR_BR_FS(FS_TEXTURED_BLINN_PHONG) break;
-        case FS_VERTEX_COLOR: SR_BR_FS(FS_VERTEX_COLOR) break;
-        case FS_ACES_LIGHTS: SR_BR_FS(FS_ACES_LIGHTS) break;
-        default: SR_BR_FS(FS_CONSTANT_COLOR) break;
-        }
-#undef SR_BR_FS
-#undef SR_BR
+        resolve_block<FS, FMT>(I.P, T.U[i], b, I.P.n_raster_host, setup + 4 * (size_t)I.tbase, I.indices,
+                               vary + (size_t)I.vbase * VSTRIDE, I.tex, I.color, I.depth, nullptr, 0u, I.gkeys,
+                               I.bitmap);
     }
 }
 
@@ -459,12 +477,14 @@ struct sr_batch {
     DevBuf<uint32_t> big_list, unsafe_list;
     DeviceFlags* flags = nullptr;
     DeviceFlags* hflags = nullptr;
+    unsigned long long* queues = nullptr;   // work-queue counters of the resolve launches
+    uint32_t combos = 0;                    // (fragment shader, colour format) pairs of the current batch
     cudaEvent_t done = nullptr, ev0 = nullptr, ev1 = nullptr;
     bool in_flight = false;
     bool use_graphs = true, autotune = true;
     BatchConfig forced{0, 0, 0};
     std::map<uint64_t, BatchConfig> tuned;
-    struct Graph { uint32_t NB; BatchConfig cfg; uint64_t gen; cudaGraphExec_t exec; };
+    struct Graph { uint32_t NB; BatchConfig cfg; uint64_t gen; uint32_t combos; cudaGraphExec_t exec; };
     std::vector<Graph> graphs;
     uint64_t gen = 1;            // bumped whenever a device buffer moves
     BatchConfig last_cfg;
@@ -526,7 +546,27 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
 #undef SR_BRS
     batch_raster_big_kernel<<<resident_grid(batch_raster_big_kernel, 256, 2), 256, 0, st>>>(T, b->setup.p, b->area.p, b->big_list.p, b->flags);
     batch_ext_kernel<<<resident_grid(batch_ext_kernel, 256, 4), 256, 0, st>>>(T, b->setup.p, b->unsafe_list.p, b->flags);
-    batch_resolve_kernel<<<resident_grid(batch_resolve_kernel, 256, 8), 256, 0, st>>>(T, b->setup.p, b->vary.p, b->flags);
+    cudaMemsetAsync(b->queues, 0, 16 * sizeof(unsigned long long), st);
+    for (int fs = 0; fs < FS_COUNT; ++fs)
+        for (int fmt = 0; fmt < 3; ++fmt) {
+            if (!(b->combos & (1u << (fs * 3 + fmt)))) continue;
+            unsigned long long* q = b->queues + (fs * 3 + fmt);
+#define SR_BRES(FS, FMT) batch_resolve_kernel<FS, FMT><<<resident_grid(batch_resolve_kernel<FS, FMT>, 256, 8), 256, 0, st>>>( \
+                T, b->setup.p, b->vary.p, q)
+#define SR_BRES_FS(FS)                                        \
+            if (fmt == SR_COLOR_RGBA8) SR_BRES(FS, SR_COLOR_RGBA8);   \
+            else if (fmt == SR_COLOR_RGBA32F) SR_BRES(FS, SR_COLOR_RGBA32F); \
+            else SR_BRES(FS, SR_COLOR_NONE);
+            switch (fs) {
+            case FS_BLINN_PHONG_DIR: SR_BRES_FS(FS_BLINN_PHONG_DIR) break;
+            case FS_TEXTURED_BLINN_PHONG: SR_BRES_FS(FS_TEXTURED_BLINN_PHONG) break;
+            case FS_VERTEX_COLOR: SR_BRES_FS(FS_VERTEX_COLOR) break;
+            case FS_ACES_LIGHTS: SR_BRES_FS(FS_ACES_LIGHTS) break;
+            default: SR_BRES_FS(FS_CONSTANT_COLOR) break;
+            }
+#undef SR_BRES_FS
+#undef SR_BRES
+        }
 }
 
 int launch_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
@@ -537,7 +577,7 @@ int launch_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     }
     cudaGraphExec_t exec = nullptr;
     for (auto& g : b->graphs)
-        if (g.NB == NB && g.cfg == c && g.gen == b->gen) exec = g.exec;
+        if (g.NB == NB && g.cfg == c && g.gen == b->gen && g.combos == b->combos) exec = g.exec;
     if (!exec) {
         cudaGraph_t graph = nullptr;
         SR_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -548,7 +588,7 @@ int launch_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) { last_cuda_error() = e; return SR_ECUDA; }
         if (b->graphs.size() >= 32) { cudaGraphExecDestroy(b->graphs.front().exec); b->graphs.erase(b->graphs.begin()); }
-        b->graphs.push_back({NB, c, b->gen, exec});
+        b->graphs.push_back({NB, c, b->gen, b->combos, exec});
     }
     SR_CK(cudaGraphLaunch(exec, b->stream));
     return SR_OK;
@@ -589,6 +629,7 @@ extern "C" SR_API int sr_batch_create(sr_batch** out) {
     cudaError_t e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&b->flags, sizeof(DeviceFlags));
     if (e == cudaSuccess) e = cudaMallocHost(&b->hflags, sizeof(DeviceFlags));
+    if (e == cudaSuccess) e = cudaMalloc(&b->queues, 16 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
@@ -611,6 +652,7 @@ extern "C" SR_API int sr_batch_destroy(sr_batch* b) {
     if (b->htab) cudaFreeHost(b->htab);
     if (b->flags) cudaFree(b->flags);
     if (b->hflags) cudaFreeHost(b->hflags);
+    if (b->queues) cudaFree(b->queues);
     if (b->done) cudaEventDestroy(b->done);
     if (b->ev0) cudaEventDestroy(b->ev0);
     if (b->ev1) cudaEventDestroy(b->ev1);
@@ -711,6 +753,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
     uint32_t* bb = reinterpret_cast<uint32_t*>(b->htab + L.off_b);
     uint32_t* cb = reinterpret_cast<uint32_t*>(b->htab + L.off_c);
     uint32_t vbase = 0;
+    uint32_t combos = 0;
     qb[0] = tb[0] = bb[0] = cb[0] = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const sr_batch_item& it = items[i];
@@ -775,12 +818,14 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         I.mx = (uint32_t)((0x100000000ull + d->tile_w - 1) / d->tile_w);
         I.my = (uint32_t)((0x100000000ull + d->tile_h - 1) / d->tile_h);
         hu[i] = p->U;
+        if (!nothing) combos |= 1u << (d->fs * 3 + (int)p->fb.color_format);
         vbase += m->n_pad;
         qb[i + 1] = qb[i] + (nothing ? 0u : (m->n_verts + 3) / 4);
         tb[i + 1] = tb[i] + nt;
         bb[i + 1] = bb[i] + (nothing ? 0u : (uint32_t)nblk);
         cb[i + 1] = cb[i] + (it.clear ? (uint32_t)((npx + CLEAR_CHUNK - 1) / CLEAR_CHUNK) : 0u);
     }
+    b->combos = combos;
     // ---- configuration: forced, tuned for this size class, or the default
     BatchConfig cfg;
     if (b->forced.G) {
@@ -820,7 +865,7 @@ extern "C" SR_API int sr_batch_sync(sr_batch* b) {
     s.unsafe_triangles = f.unsafe;
     s.fragments = f.fragments;
     s.nan_bbox = f.nan_bbox;
-    s.kernel_launches = 7;
+    s.kernel_launches = 6 + (uint32_t)__builtin_popcount(b->combos);
     b->stats_valid = true;
     if (f.bad_index) return SR_EINVAL;
     if (f.nan_total) return SR_ENAN;

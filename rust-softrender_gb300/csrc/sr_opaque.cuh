@@ -36,11 +36,16 @@ __device__ __forceinline__ void mark_rect(uint32_t* bitmap, uint32_t blocks_x, u
 }
 
 // Exact test of one (primitive, pixel) item; emits the fragment key.
-__device__ __forceinline__ void rg_fragment(const DrawParams& P, float4 r0, float4 r1, float4 r2, uint32_t t,
-                                            uint32_t px, uint32_t py, uint32_t N,
-                                            unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap,
-                                            const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
-                                            uint32_t mx, uint32_t my, unsigned long long& frags) {
+// The exact per-pixel sequence of rasterize_triangle (triangle.rs:104-126) for
+// one (primitive, pixel) item: barycentrics in the reference's op order,
+// inclusive coverage, z < 0, optional stencil gate; emits the 64-bit key.
+// The target is given by its scalars (frame size, semantic tile size with
+// its division magics, depth attachment, stencil gate).
+__device__ __forceinline__ void frag_emit(uint32_t W, uint32_t H, uint32_t tile_w, uint32_t tile_h, uint32_t mx,
+                                          uint32_t my, bool has_depth, float4 r0, float4 r1, float4 r2, uint32_t t,
+                                          uint32_t px, uint32_t py, uint32_t N, unsigned long long* __restrict__ gkeys,
+                                          const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
+                                          uint32_t stencil_test_id, uint32_t sref, unsigned long long& frags) {
     const float x = (float)px + 0.5f, y = (float)py + 0.5f;
     const float dx = x - r1.x, dy = y - r1.y;
     const float nu = r0.x * dx + r0.y * dy;
@@ -52,12 +57,21 @@ __device__ __forceinline__ void rg_fragment(const DrawParams& P, float4 r0, floa
     if (u < 0.0f || v < 0.0f || w < 0.0f) return;
     const float z = (r1.w * u + r2.x * v) + r2.y * w;
     if (!(z < 0.0f)) return;
-    const size_t gi = (size_t)py * P.W + px;
-    if (gate_with_stencil && !stencil_test(P.stencil_test, __ldg(stencil + gi), P.sref)) return;
-    const int kp = seam_count(px, P.tile_w, mx, P.W - 1) * seam_count(py, P.tile_h, my, P.H - 1);
+    const size_t gi = (size_t)py * W + px;
+    if (gate_with_stencil && !stencil_test(stencil_test_id, __ldg(stencil + gi), sref)) return;
+    const int kp = seam_count(px, tile_w, mx, W - 1) * seam_count(py, tile_h, my, H - 1);
     ++frags;
-    const uint32_t zk = P.has_depth ? zkey(z) : 0u;
+    const uint32_t zk = has_depth ? zkey(z) : 0u;
     atomicMax(gkeys + gi, ((unsigned long long)zk << 32) | (unsigned long long)((uint32_t)(kp - 1) * N + t + 1u));
+}
+
+__device__ __forceinline__ void rg_fragment(const DrawParams& P, float4 r0, float4 r1, float4 r2, uint32_t t,
+                                            uint32_t px, uint32_t py, uint32_t N,
+                                            unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap,
+                                            const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
+                                            uint32_t mx, uint32_t my, unsigned long long& frags) {
+    frag_emit(P.W, P.H, P.tile_w, P.tile_h, mx, my, P.has_depth != 0, r0, r1, r2, t, px, py, N, gkeys, stencil,
+              gate_with_stencil, P.stencil_test, P.sref, frags);
 }
 
 constexpr uint32_t RG_BIG = 2048;   // bbox pixels above which a primitive goes to the block-cooperative pass
