@@ -62,6 +62,28 @@ struct BTables {
 };
 
 constexpr uint32_t CLEAR_CHUNK = 8192;   // pixels per clear work item
+constexpr uint32_t BIG_CHUNK = 4096;     // bbox pixels per work item of a large primitive
+// Work-queue counters of a batch (device array of 32 u64):
+//   [fs * 3 + format]  resolve launch of that (fragment shader, colour format)
+constexpr int Q_TOUCHED = 16;            // entries on the touched-block list
+constexpr int Q_BIG = 17;                // large primitives (count << 40 | chunks)
+constexpr int Q_BIGCHUNK = 18;           // next large-primitive chunk to hand out
+constexpr int N_QUEUES = 32;
+
+// Marks the 32x32 blocks of a clamped bbox of draw i as touched; a block
+// whose bit this call sets goes on the touched-block list (once per batch).
+__device__ __forceinline__ void mark_rect_list(uint32_t* bitmap, uint32_t blocks_x, uint32_t x0, uint32_t y0,
+                                               uint32_t x1, uint32_t y1, uint32_t i,
+                                               unsigned long long* __restrict__ tlist,
+                                               unsigned long long* __restrict__ queues) {
+    for (uint32_t by = y0 >> TOUCH_LOG2; by <= (y1 >> TOUCH_LOG2); ++by)
+        for (uint32_t bx = x0 >> TOUCH_LOG2; bx <= (x1 >> TOUCH_LOG2); ++bx) {
+            const uint32_t b = by * blocks_x + bx, bit = 1u << (b & 31);
+            if (bitmap[b >> 5] & bit) continue;
+            if (!(atomicOr(bitmap + (b >> 5), bit) & bit))
+                tlist[atomicAdd(queues + Q_TOUCHED, 1ull)] = ((unsigned long long)i << 32) | b;
+        }
+}
 
 // Largest i in [0, n) with base[i] <= j (base[0] = 0, j < base[n]).
 __device__ __forceinline__ uint32_t owner_of(const uint32_t* __restrict__ base, uint32_t n, uint32_t j) {
@@ -225,7 +247,11 @@ template <uint32_t G>
 __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, const float4* __restrict__ setup,
                                                                  const unsigned long long* __restrict__ area,
                                                                  uint32_t big_threshold,
-                                                                 uint32_t* __restrict__ big_list, DeviceFlags* flags) {
+                                                                 uint32_t* __restrict__ big_list,
+                                                                 uint32_t* __restrict__ big_base,
+                                                                 unsigned long long* __restrict__ tlist,
+                                                                 unsigned long long* __restrict__ queues,
+                                                                 DeviceFlags* flags) {
     // per staged primitive: record, bbox origin and width, and the scalars of
     // its draw's target (so the per-pixel loop reads no global tables)
     struct Slot {
@@ -260,7 +286,11 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
         if (lane < G && g < total) {
             const unsigned long long at = area[g];
             if (at > big_threshold) {
-                big_list[atomicAdd(&flags->n_big, 1ull)] = g;
+                // one packed counter keeps list order and chunk offsets consistent
+                const unsigned long long nch = (at + BIG_CHUNK - 1) / BIG_CHUNK;
+                const unsigned long long old = atomicAdd(queues + Q_BIG, (1ull << 40) | nch);
+                big_list[old >> 40] = g;
+                big_base[old >> 40] = (uint32_t)(old & ((1ull << 40) - 1));
             } else if (at) {
                 a = (uint32_t)at;
                 const uint32_t i = owner_from(T.tbase, n, i0, g);
@@ -276,7 +306,7 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
                 const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)W - 1);
                 const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)H - 1);
                 const uint32_t w = x1 - x0 + 1;
-                mark_rect(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1);
+                mark_rect_list(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1, i, tlist, queues);
                 sxy[wl][lane] = x0 | (y0 << 16);
                 sw[wl][lane] = w;
                 Slot S;
@@ -323,39 +353,65 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
     if (lane == 0 && frags) atomicAdd(&flags->fragments, frags);
 }
 
-// raster_big_kernel over the batch's large primitives.
+// raster_big_kernel over the batch's large primitives, split into chunks of
+// BIG_CHUNK bbox pixels taken from a work queue (a huge primitive spreads
+// over many CTAs).
 __global__ void __launch_bounds__(256) batch_raster_big_kernel(BTables T, const float4* __restrict__ setup,
                                                                const unsigned long long* __restrict__ area,
                                                                const uint32_t* __restrict__ big_list,
+                                                               const uint32_t* __restrict__ big_base,
+                                                               unsigned long long* __restrict__ tlist,
+                                                               unsigned long long* __restrict__ queues,
                                                                DeviceFlags* flags) {
+    __shared__ uint32_t s_item;
     const uint32_t n = *T.n;
-    const uint32_t nb = (uint32_t)flags->n_big;
+    const unsigned long long packed = queues[Q_BIG];
+    const uint32_t nb = (uint32_t)(packed >> 40);
+    const uint32_t total = (uint32_t)min(packed & ((1ull << 40) - 1), 0xffffffffull);
     unsigned long long frags = 0;
-    for (uint32_t k = blockIdx.x; k < nb; k += gridDim.x) {
-        const uint32_t g = big_list[k];
-        const BInst& I = T.inst[owner_of(T.tbase, n, g)];
+    for (;;) {
+        if (threadIdx.x == 0) s_item = (uint32_t)min(atomicAdd(queues + Q_BIGCHUNK, 1ull), 0xffffffffull);
+        __syncthreads();
+        const uint32_t j = s_item;
+        __syncthreads();
+        if (j >= total) break;
+        // the large primitive owning chunk j: largest k with big_base[k] <= j
+        uint32_t lo = 0, hi = nb - 1;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi + 1) >> 1;
+            if (big_base[mid] <= j) lo = mid; else hi = mid - 1;
+        }
+        const uint32_t g = big_list[lo];
+        const uint32_t c = j - big_base[lo];
+        const uint32_t i = owner_of(T.tbase, n, g);
+        const BInst& I = T.inst[i];
         const float4* r = setup + 4 * (size_t)g;
         const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+        const uint32_t W = I.P.W, H = I.P.H;
         const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
         const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
-        const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)I.P.W - 1);
-        const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)I.P.H - 1);
+        const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)W - 1);
+        const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)H - 1);
         const uint32_t w = x1 - x0 + 1;
-        const uint32_t blocks_x = (I.P.W + 31) >> 5;
-        {
+        if (c == 0) {   // the first chunk marks the whole bbox
+            const uint32_t blocks_x = (W + 31) >> 5;
             const uint32_t bx0 = x0 >> TOUCH_LOG2, by0 = y0 >> TOUCH_LOG2;
             const uint32_t nbx = (x1 >> TOUCH_LOG2) - bx0 + 1, nby = (y1 >> TOUCH_LOG2) - by0 + 1;
-            for (uint32_t j = threadIdx.x; j < nbx * nby; j += blockDim.x) {
-                const uint32_t b = (by0 + j / nbx) * blocks_x + bx0 + j % nbx, bit = 1u << (b & 31);
-                if (!(I.bitmap[b >> 5] & bit)) atomicOr(I.bitmap + (b >> 5), bit);
+            for (uint32_t q = threadIdx.x; q < nbx * nby; q += blockDim.x) {
+                const uint32_t bb = (by0 + q / nbx) * blocks_x + bx0 + q % nbx, bit = 1u << (bb & 31);
+                if (I.bitmap[bb >> 5] & bit) continue;
+                if (!(atomicOr(I.bitmap + (bb >> 5), bit) & bit))
+                    tlist[atomicAdd(queues + Q_TOUCHED, 1ull)] = ((unsigned long long)i << 32) | bb;
             }
         }
         const unsigned long long at = area[g];
+        const unsigned long long p0 = (unsigned long long)c * BIG_CHUNK;
+        const unsigned long long p1 = min(at, p0 + BIG_CHUNK);
         const uint32_t t = g - I.tbase;
-        for (unsigned long long j = threadIdx.x; j < at; j += blockDim.x) {
-            const uint32_t row = (uint32_t)(j / w), col = (uint32_t)(j - (unsigned long long)row * w);
-            rg_fragment(I.P, r0, r1, r2, t, x0 + col, y0 + row, I.P.n_raster_host, I.gkeys, I.bitmap, nullptr, 0u,
-                        I.mx, I.my, frags);
+        for (unsigned long long q = p0 + threadIdx.x; q < p1; q += blockDim.x) {
+            const uint32_t row = (uint32_t)(q / w), col = (uint32_t)(q - (unsigned long long)row * w);
+            frag_emit(W, H, I.P.tile_w, I.P.tile_h, I.mx, I.my, I.P.has_depth != 0, r0, r1, r2, t, x0 + col,
+                      y0 + row, I.P.n_raster_host, I.gkeys, nullptr, 0u, 0u, 0u, frags);
         }
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
@@ -364,7 +420,9 @@ __global__ void __launch_bounds__(256) batch_raster_big_kernel(BTables T, const 
 
 // ext_direct_kernel over the batch's unsafe primitives (one warp each).
 __global__ void __launch_bounds__(256) batch_ext_kernel(BTables T, const float4* __restrict__ setup,
-                                                        const uint32_t* __restrict__ unsafe_list, DeviceFlags* flags) {
+                                                        const uint32_t* __restrict__ unsafe_list,
+                                                        unsigned long long* __restrict__ tlist,
+                                                        unsigned long long* __restrict__ queues, DeviceFlags* flags) {
     const uint32_t n = *T.n;
     const uint32_t nu = (uint32_t)flags->n_unsafe_list;
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -373,9 +431,17 @@ __global__ void __launch_bounds__(256) batch_ext_kernel(BTables T, const float4*
     unsigned long long frags = 0;
     for (uint32_t k = warp; k < nu; k += nwarps) {
         const uint32_t g = unsafe_list[k];
-        const BInst& I = T.inst[owner_of(T.tbase, n, g)];
-        ext_prim(I.P, g - I.tbase, I.P.n_raster_host, setup + 4 * (size_t)I.tbase, I.gkeys, I.bitmap, nullptr, 0u,
-                 lane, frags);
+        const uint32_t i = owner_of(T.tbase, n, g);
+        const BInst& I = T.inst[i];
+        uint32_t* bm = I.bitmap;
+        const uint32_t blocks_x = (I.P.W + 31) >> 5;
+        ext_prim_m(I.P, g - I.tbase, I.P.n_raster_host, setup + 4 * (size_t)I.tbase, I.gkeys, nullptr, 0u, lane, frags,
+                   [=](uint32_t px, uint32_t py) {
+                       const uint32_t bb = (py >> TOUCH_LOG2) * blocks_x + (px >> TOUCH_LOG2), bit = 1u << (bb & 31);
+                       if (bm[bb >> 5] & bit) return;
+                       if (!(atomicOr(bm + (bb >> 5), bit) & bit))
+                           tlist[atomicAdd(queues + Q_TOUCHED, 1ull)] = ((unsigned long long)i << 32) | bb;
+                   });
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
     if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&flags->fragments, frags);
@@ -388,21 +454,20 @@ __global__ void __launch_bounds__(256) batch_ext_kernel(BTables T, const float4*
 template <int FS, int FMT>
 __global__ void __launch_bounds__(256) batch_resolve_kernel(BTables T, const float4* __restrict__ setup,
                                                             const float* __restrict__ vary,
-                                                            unsigned long long* __restrict__ queue) {
+                                                            const unsigned long long* __restrict__ tlist,
+                                                            unsigned long long* __restrict__ queues, int qi) {
     __shared__ uint32_t s_item;
-    const uint32_t n = *T.n;
-    const uint32_t total = __ldg(T.bbase + n);
+    const uint32_t total = (uint32_t)min(queues[Q_TOUCHED], 0xffffffffull);
     for (;;) {
-        if (threadIdx.x == 0) s_item = (uint32_t)min(atomicAdd(queue, 1ull), 0xffffffffull);
+        if (threadIdx.x == 0) s_item = (uint32_t)min(atomicAdd(queues + qi, 1ull), 0xffffffffull);
         __syncthreads();
         const uint32_t j = s_item;
         __syncthreads();
         if (j >= total) break;
-        const uint32_t i = owner_of(T.bbase, n, j);
+        const unsigned long long e = tlist[j];
+        const uint32_t i = (uint32_t)(e >> 32), b = (uint32_t)e;
         const BInst& I = T.inst[i];
         if (I.P.fs != FS || (int)I.P.color_format != FMT) continue;
-        const uint32_t b = j - __ldg(T.bbase + i);
-        if (!(I.bitmap[b >> 5] & (1u << (b & 31)))) continue;
         resolve_block<FS, FMT>(I.P, T.U[i], b, I.P.n_raster_host, setup + 4 * (size_t)I.tbase, I.indices,
                                vary + (size_t)I.vbase * VSTRIDE, I.tex, I.color, I.depth, nullptr, 0u, I.gkeys,
                                I.bitmap);
@@ -474,7 +539,8 @@ struct sr_batch {
     DevBuf<float> vary;
     DevBuf<float4> setup;
     DevBuf<unsigned long long> area;
-    DevBuf<uint32_t> big_list, unsafe_list;
+    DevBuf<uint32_t> big_list, big_base, unsafe_list;
+    DevBuf<unsigned long long> tlist;       // touched (draw, block) list
     DeviceFlags* flags = nullptr;
     DeviceFlags* hflags = nullptr;
     unsigned long long* queues = nullptr;   // work-queue counters of the resolve launches
@@ -529,12 +595,13 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     const BTables T = tables_at(b->dtab.p, L);
     cudaMemcpyAsync(b->dtab.p, b->htab, L.bytes, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(b->flags, 0, sizeof(DeviceFlags), st);
+    cudaMemsetAsync(b->queues, 0, N_QUEUES * sizeof(unsigned long long), st);
     batch_clear_kernel<<<resident_grid(batch_clear_kernel, 256, 8), 256, 0, st>>>(T);
     batch_vertex_kernel<<<resident_grid(batch_vertex_kernel, 128, 16), 128, 0, st>>>(T, b->scr4.p, b->vary.p);
     batch_setup_kernel<<<resident_grid(batch_setup_kernel, 256, 8), 256, 0, st>>>(T, b->scr4.p, b->setup.p, b->area.p,
                                                                                 b->unsafe_list.p, b->flags);
 #define SR_BRS(g) batch_raster_small_kernel<g><<<resident_grid(batch_raster_small_kernel<g>, 256, (int)c.ctas), 256, 0, st>>>( \
-        T, b->setup.p, b->area.p, c.big, b->big_list.p, b->flags)
+        T, b->setup.p, b->area.p, c.big, b->big_list.p, b->big_base.p, b->tlist.p, b->queues, b->flags)
     switch (c.G) {
     case 1: SR_BRS(1); break;
     case 2: SR_BRS(2); break;
@@ -544,15 +611,16 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     default: SR_BRS(32); break;
     }
 #undef SR_BRS
-    batch_raster_big_kernel<<<resident_grid(batch_raster_big_kernel, 256, 2), 256, 0, st>>>(T, b->setup.p, b->area.p, b->big_list.p, b->flags);
-    batch_ext_kernel<<<resident_grid(batch_ext_kernel, 256, 4), 256, 0, st>>>(T, b->setup.p, b->unsafe_list.p, b->flags);
-    cudaMemsetAsync(b->queues, 0, 16 * sizeof(unsigned long long), st);
+    batch_raster_big_kernel<<<resident_grid(batch_raster_big_kernel, 256, 8), 256, 0, st>>>(
+        T, b->setup.p, b->area.p, b->big_list.p, b->big_base.p, b->tlist.p, b->queues, b->flags);
+    batch_ext_kernel<<<resident_grid(batch_ext_kernel, 256, 4), 256, 0, st>>>(T, b->setup.p, b->unsafe_list.p,
+                                                                             b->tlist.p, b->queues, b->flags);
     for (int fs = 0; fs < FS_COUNT; ++fs)
         for (int fmt = 0; fmt < 3; ++fmt) {
             if (!(b->combos & (1u << (fs * 3 + fmt)))) continue;
-            unsigned long long* q = b->queues + (fs * 3 + fmt);
+            const int qi = fs * 3 + fmt;
 #define SR_BRES(FS, FMT) batch_resolve_kernel<FS, FMT><<<resident_grid(batch_resolve_kernel<FS, FMT>, 256, 8), 256, 0, st>>>( \
-                T, b->setup.p, b->vary.p, q)
+                T, b->setup.p, b->vary.p, b->tlist.p, b->queues, qi)
 #define SR_BRES_FS(FS)                                        \
             if (fmt == SR_COLOR_RGBA8) SR_BRES(FS, SR_COLOR_RGBA8);   \
             else if (fmt == SR_COLOR_RGBA32F) SR_BRES(FS, SR_COLOR_RGBA32F); \
@@ -629,7 +697,7 @@ extern "C" SR_API int sr_batch_create(sr_batch** out) {
     cudaError_t e = cudaStreamCreateWithFlags(&b->own_stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&b->flags, sizeof(DeviceFlags));
     if (e == cudaSuccess) e = cudaMallocHost(&b->hflags, sizeof(DeviceFlags));
-    if (e == cudaSuccess) e = cudaMalloc(&b->queues, 16 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&b->queues, N_QUEUES * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev0);
     if (e == cudaSuccess) e = cudaEventCreate(&b->ev1);
@@ -648,7 +716,7 @@ extern "C" SR_API int sr_batch_destroy(sr_batch* b) {
     if (b->stream) cudaStreamSynchronize(b->stream);
     drop_graphs(b);
     b->dtab.release(); b->scr4.release(); b->vary.release(); b->setup.release();
-    b->area.release(); b->big_list.release(); b->unsafe_list.release();
+    b->area.release(); b->big_list.release(); b->big_base.release(); b->unsafe_list.release(); b->tlist.release();
     if (b->htab) cudaFreeHost(b->htab);
     if (b->flags) cudaFree(b->flags);
     if (b->hflags) cudaFreeHost(b->hflags);
@@ -741,7 +809,8 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
     if ((rc = grow(b, b->dtab, L.bytes)) || (rc = grow(b, b->scr4, slots + 4)) ||
         (rc = grow(b, b->vary, (slots + 4) * VSTRIDE)) || (rc = grow(b, b->setup, 4 * (tris + 1))) ||
         (rc = grow(b, b->area, tris + 1)) || (rc = grow(b, b->big_list, tris + 1)) ||
-        (rc = grow(b, b->unsafe_list, tris + 1)))
+        (rc = grow(b, b->big_base, tris + 1)) || (rc = grow(b, b->unsafe_list, tris + 1)) ||
+        (rc = grow(b, b->tlist, blocks + 1)))
         return rc;
     // ---- host table
     std::memset(b->htab, 0, L.bytes);
@@ -840,6 +909,8 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
             b->tuned[cls] = cfg;
         }
     }
+    // the large-primitive counter packs the count into 24 bits
+    if (tris >= (1ull << 24)) cfg.big = 0xffffffffu;
     if ((rc = launch_batch(b, NB, cfg))) return rc;
     SR_CK(cudaEventRecord(b->done, b->stream));
     b->in_flight = true;

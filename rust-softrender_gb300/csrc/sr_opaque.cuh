@@ -77,13 +77,14 @@ __device__ __forceinline__ void rg_fragment(const DrawParams& P, float4 r0, floa
 constexpr uint32_t RG_BIG = 2048;   // bbox pixels above which a primitive goes to the block-cooperative pass
 
 // Extension fragments of one unsafe primitive t (see ext_direct_kernel): the
-// warp's lanes stride over the semantic tiles.
-__device__ __forceinline__ void ext_prim(const DrawParams& P, uint32_t t, uint32_t N, const float4* __restrict__ setup,
-                                         unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap,
-                                         const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
-                                         uint32_t lane, unsigned long long& frags) {
+// warp's lanes stride over the semantic tiles.  `mark(px, py)` records the
+// pixel's 32x32 block as touched.
+template <class Mark>
+__device__ __forceinline__ void ext_prim_m(const DrawParams& P, uint32_t t, uint32_t N,
+                                           const float4* __restrict__ setup, unsigned long long* __restrict__ gkeys,
+                                           const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
+                                           uint32_t lane, unsigned long long& frags, Mark mark) {
     const uint32_t ntiles = P.ncols * P.nrows;
-    const uint32_t blocks_x = (P.W + 31) >> 5;
     const float4* r = setup + 4 * (size_t)t;
     const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
     const int ix0 = __float_as_int(r3.x), iy0 = __float_as_int(r3.y);
@@ -118,10 +119,19 @@ __device__ __forceinline__ void ext_prim(const DrawParams& P, uint32_t t, uint32
                 const uint32_t zk = P.has_depth ? zkey(z) : 0u;
                 atomicMax(gkeys + gi, ((unsigned long long)zk << 32) |
                                           (unsigned long long)((uint32_t)rank * N + t + 1u));
-                mark_touched(bitmap, blocks_x, px, py);
+                mark(px, py);
             }
         }
     }
+}
+
+__device__ __forceinline__ void ext_prim(const DrawParams& P, uint32_t t, uint32_t N, const float4* __restrict__ setup,
+                                         unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap,
+                                         const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
+                                         uint32_t lane, unsigned long long& frags) {
+    const uint32_t blocks_x = (P.W + 31) >> 5;
+    ext_prim_m(P, t, N, setup, gkeys, stencil, gate_with_stencil, lane, frags,
+               [=](uint32_t px, uint32_t py) { mark_touched(bitmap, blocks_x, px, py); });
 }
 
 // Resolve of one touched 32x32 block b: each pixel's winning key against the
