@@ -70,20 +70,10 @@ constexpr int Q_BIG = 17;                // large primitives (count << 40 | chun
 constexpr int Q_BIGCHUNK = 18;           // next large-primitive chunk to hand out
 constexpr int N_QUEUES = 32;
 
-// Marks the 32x32 blocks of a clamped bbox of draw i as touched; a block
-// whose bit this call sets goes on the touched-block list (once per batch).
-__device__ __forceinline__ void mark_rect_list(uint32_t* bitmap, uint32_t blocks_x, uint32_t x0, uint32_t y0,
-                                               uint32_t x1, uint32_t y1, uint32_t i,
-                                               unsigned long long* __restrict__ tlist,
-                                               unsigned long long* __restrict__ queues) {
-    for (uint32_t by = y0 >> TOUCH_LOG2; by <= (y1 >> TOUCH_LOG2); ++by)
-        for (uint32_t bx = x0 >> TOUCH_LOG2; bx <= (x1 >> TOUCH_LOG2); ++bx) {
-            const uint32_t b = by * blocks_x + bx, bit = 1u << (b & 31);
-            if (bitmap[b >> 5] & bit) continue;
-            if (!(atomicOr(bitmap + (b >> 5), bit) & bit))
-                tlist[atomicAdd(queues + Q_TOUCHED, 1ull)] = ((unsigned long long)i << 32) | b;
-        }
-}
+// The touched-block list is built after the raster passes (which only set
+// bitmap bits with fire-and-forget atomics): one thread per (draw, block).
+__global__ void __launch_bounds__(256) batch_collect_kernel(BTables T, unsigned long long* __restrict__ tlist,
+                                                            unsigned long long* __restrict__ queues);
 
 // Largest i in [0, n) with base[i] <= j (base[0] = 0, j < base[n]).
 __device__ __forceinline__ uint32_t owner_of(const uint32_t* __restrict__ base, uint32_t n, uint32_t j) {
@@ -306,7 +296,7 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
                 const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)W - 1);
                 const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)H - 1);
                 const uint32_t w = x1 - x0 + 1;
-                mark_rect_list(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1, i, tlist, queues);
+                mark_rect(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1);
                 sxy[wl][lane] = x0 | (y0 << 16);
                 sw[wl][lane] = w;
                 Slot S;
@@ -399,9 +389,7 @@ __global__ void __launch_bounds__(256) batch_raster_big_kernel(BTables T, const 
             const uint32_t nbx = (x1 >> TOUCH_LOG2) - bx0 + 1, nby = (y1 >> TOUCH_LOG2) - by0 + 1;
             for (uint32_t q = threadIdx.x; q < nbx * nby; q += blockDim.x) {
                 const uint32_t bb = (by0 + q / nbx) * blocks_x + bx0 + q % nbx, bit = 1u << (bb & 31);
-                if (I.bitmap[bb >> 5] & bit) continue;
-                if (!(atomicOr(I.bitmap + (bb >> 5), bit) & bit))
-                    tlist[atomicAdd(queues + Q_TOUCHED, 1ull)] = ((unsigned long long)i << 32) | bb;
+                if (!(I.bitmap[bb >> 5] & bit)) atomicOr(I.bitmap + (bb >> 5), bit);
             }
         }
         const unsigned long long at = area[g];
@@ -431,20 +419,39 @@ __global__ void __launch_bounds__(256) batch_ext_kernel(BTables T, const float4*
     unsigned long long frags = 0;
     for (uint32_t k = warp; k < nu; k += nwarps) {
         const uint32_t g = unsafe_list[k];
-        const uint32_t i = owner_of(T.tbase, n, g);
-        const BInst& I = T.inst[i];
-        uint32_t* bm = I.bitmap;
-        const uint32_t blocks_x = (I.P.W + 31) >> 5;
-        ext_prim_m(I.P, g - I.tbase, I.P.n_raster_host, setup + 4 * (size_t)I.tbase, I.gkeys, nullptr, 0u, lane, frags,
-                   [=](uint32_t px, uint32_t py) {
-                       const uint32_t bb = (py >> TOUCH_LOG2) * blocks_x + (px >> TOUCH_LOG2), bit = 1u << (bb & 31);
-                       if (bm[bb >> 5] & bit) return;
-                       if (!(atomicOr(bm + (bb >> 5), bit) & bit))
-                           tlist[atomicAdd(queues + Q_TOUCHED, 1ull)] = ((unsigned long long)i << 32) | bb;
-                   });
+        const BInst& I = T.inst[owner_of(T.tbase, n, g)];
+        ext_prim(I.P, g - I.tbase, I.P.n_raster_host, setup + 4 * (size_t)I.tbase, I.gkeys, I.bitmap, nullptr, 0u,
+                 lane, frags);
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
     if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&flags->fragments, frags);
+}
+
+// ---------------------------------------------------------------- collect
+__global__ void __launch_bounds__(256) batch_collect_kernel(BTables T, unsigned long long* __restrict__ tlist,
+                                                            unsigned long long* __restrict__ queues) {
+    const uint32_t n = *T.n;
+    const uint32_t total = __ldg(T.bbase + n);
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    const uint32_t rounds = (total + stride - 1) / stride;
+    for (uint32_t r = 0; r < rounds; ++r) {
+        const uint32_t j = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        bool set = false;
+        unsigned long long e = 0;
+        if (j < total) {
+            const uint32_t i = owner_of(T.bbase, n, j);
+            const uint32_t b = j - __ldg(T.bbase + i);
+            set = (T.inst[i].bitmap[b >> 5] >> (b & 31)) & 1u;
+            e = ((unsigned long long)i << 32) | b;
+        }
+        const uint32_t m = __ballot_sync(0xffffffffu, set);
+        if (!m) continue;
+        unsigned long long base = 0;
+        if (lane == __ffs(m) - 1) base = atomicAdd(queues + Q_TOUCHED, (unsigned long long)__popc(m));
+        base = __shfl_sync(0xffffffffu, base, __ffs(m) - 1);
+        if (set) tlist[base + __popc(m & ((1u << lane) - 1u))] = e;
+    }
 }
 
 // ---------------------------------------------------------------- resolve
@@ -615,6 +622,7 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
         T, b->setup.p, b->area.p, b->big_list.p, b->big_base.p, b->tlist.p, b->queues, b->flags);
     batch_ext_kernel<<<resident_grid(batch_ext_kernel, 256, 4), 256, 0, st>>>(T, b->setup.p, b->unsafe_list.p,
                                                                              b->tlist.p, b->queues, b->flags);
+    batch_collect_kernel<<<resident_grid(batch_collect_kernel, 256, 8), 256, 0, st>>>(T, b->tlist.p, b->queues);
     for (int fs = 0; fs < FS_COUNT; ++fs)
         for (int fmt = 0; fmt < 3; ++fmt) {
             if (!(b->combos & (1u << (fs * 3 + fmt)))) continue;
@@ -936,7 +944,7 @@ extern "C" SR_API int sr_batch_sync(sr_batch* b) {
     s.unsafe_triangles = f.unsafe;
     s.fragments = f.fragments;
     s.nan_bbox = f.nan_bbox;
-    s.kernel_launches = 6 + (uint32_t)__builtin_popcount(b->combos);
+    s.kernel_launches = 7 + (uint32_t)__builtin_popcount(b->combos);
     b->stats_valid = true;
     if (f.bad_index) return SR_EINVAL;
     if (f.nan_total) return SR_ENAN;

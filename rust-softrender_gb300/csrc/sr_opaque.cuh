@@ -15,8 +15,10 @@ __device__ __forceinline__ bool surely_negative(float n, float det) {
 
 __device__ __forceinline__ void mark_touched(uint32_t* bitmap, uint32_t blocks_x, uint32_t px, uint32_t py) {
     uint32_t b = (py >> TOUCH_LOG2) * blocks_x + (px >> TOUCH_LOG2);
-    uint32_t bit = 1u << (b & 31);
-    if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);   // a stale read only costs an extra atomic
+    const uint32_t bit = 1u << (b & 31);
+    // test first: blocks are shared by many primitives, and an atomic per
+    // primitive on the same word would serialise in L2
+    if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);
 }
 
 // ceil(2^32 / t): floor(p / t) == __umulhi(p, m) for p, t < 2^16
@@ -31,7 +33,7 @@ __device__ __forceinline__ void mark_rect(uint32_t* bitmap, uint32_t blocks_x, u
     for (uint32_t by = y0 >> TOUCH_LOG2; by <= (y1 >> TOUCH_LOG2); ++by)
         for (uint32_t bx = x0 >> TOUCH_LOG2; bx <= (x1 >> TOUCH_LOG2); ++bx) {
             const uint32_t b = by * blocks_x + bx, bit = 1u << (b & 31);
-            if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);
+            if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);   // test first (see mark_touched)
         }
 }
 
