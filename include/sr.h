@@ -289,6 +289,57 @@ SR_API int sr_batch_sync(sr_batch* b);
 /* Summed counters of the last batch (valid after sr_batch_sync). */
 SR_API int sr_batch_get_stats(sr_batch* b, sr_stats* out);
 
+/* ------------------------------------------------------------ serving
+ * A request loop in front of the batched renderer.  Requests (a resident
+ * mesh, a camera, a resolution) are admitted against an HBM budget, folded
+ * into the next batch as soon as a batch slot and memory free up (several
+ * batches run on the GPU at once, each on its own stream), rendered into
+ * pooled device framebuffers that stay resident until the result is read,
+ * and timed from submission to completion.  With `plain` set the same loop
+ * serves each request alone through sr_render + sr_sync (the per-request
+ * pipeline), for comparison.  Every request's result equals rendering it
+ * alone with sr_render.  No counterpart in the reference (whose
+ * Pipeline::render_mesh renders one mesh per call, src/pipeline/mod.rs:146). */
+typedef struct sr_server sr_server;
+typedef struct sr_server_config {
+    uint64_t hbm_budget;        /* bytes the server may hold for framebuffers and
+                                   scratch (0: 64 GiB)                            */
+    uint32_t max_inflight;      /* batches on the GPU at once (0: 3)              */
+    uint32_t max_batch;         /* requests per batch (0: 256)                    */
+    uint32_t plain;             /* nonzero: one request at a time via sr_render   */
+} sr_server_config;
+typedef struct sr_request {
+    sr_draw draw;               /* as for sr_render; eligible as for sr_batch_render */
+    const void* uniforms;       /* the draw's sr_uniforms (copied at submission)  */
+    size_t uniforms_size;
+    uint32_t width, height;     /* framebuffer of the result (colour + f32 depth) */
+    uint32_t color_format;      /* SR_COLOR_RGBA8 or SR_COLOR_RGBA32F             */
+    uint8_t clear_color[16];    /* in the colour format                           */
+} sr_request;
+typedef struct sr_server_stats {
+    uint64_t submitted, completed, batches;
+    double mean_batch;          /* requests per batch                             */
+    double p50_ms, p99_ms, mean_ms, max_ms;   /* submission -> completion         */
+    double throughput_rps;      /* completed requests per second of serving time  */
+    uint64_t peak_bytes;        /* largest admitted footprint                     */
+} sr_server_stats;
+SR_API int sr_server_create(const sr_server_config* cfg, sr_server** out);
+/* Queues a request; returns at once with its ticket.  SR_EBUDGET if the
+ * request alone exceeds the budget, SR_EINVAL if it is not eligible. */
+SR_API int sr_server_submit(sr_server* s, const sr_request* r, uint64_t* ticket);
+/* Waits for a request (SR_ETIMEOUT after timeout_ms). */
+SR_API int sr_server_wait(sr_server* s, uint64_t ticket, uint32_t timeout_ms);
+/* Copies a finished request's colour / depth to host memory (either may be
+ * NULL) and releases its framebuffer. */
+SR_API int sr_server_read(sr_server* s, uint64_t ticket, void* color, float* depth);
+/* Releases a finished request's framebuffer without reading it. */
+SR_API int sr_server_release(sr_server* s, uint64_t ticket);
+/* Waits until every submitted request has finished (SR_ETIMEOUT). */
+SR_API int sr_server_drain(sr_server* s, uint32_t timeout_ms);
+SR_API int sr_server_get_stats(sr_server* s, sr_server_stats* out);
+SR_API int sr_server_reset_stats(sr_server* s);
+SR_API int sr_server_destroy(sr_server* s);
+
 /* ---------------------------------------------------- allocation-free draw
  * sr_render_static has no counterpart in the reference.  It is for callers
  * that cannot let a library allocate device memory: an application whose own

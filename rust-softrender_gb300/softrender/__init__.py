@@ -460,3 +460,69 @@ class Batch:
             self.destroy()
         except Exception:
             pass
+
+
+class Server:
+    """Serving loop (sr_server_*): requests admitted against an HBM budget and
+    continuously batched onto the GPU; `plain=True` serves one request at a
+    time through sr_render (the per-request pipeline)."""
+
+    def __init__(self, hbm_budget=0, max_inflight=0, max_batch=0, plain=False):
+        cfg = A.SrServerConfig(hbm_budget, max_inflight, max_batch, 1 if plain else 0)
+        h = C.c_void_p()
+        check(lib().sr_server_create(C.byref(cfg), C.byref(h)), "sr_server_create")
+        self.handle = h
+
+    @staticmethod
+    def request(draw, uniforms, width, height, color_format, clear_bytes):
+        r = A.SrRequest()
+        r.draw = draw
+        r.uniforms = C.cast(C.pointer(uniforms), C.c_void_p)
+        r.uniforms_size = C.sizeof(A.SrUniforms)
+        r.width, r.height, r.color_format = width, height, color_format
+        b = bytes(clear_bytes)
+        for k in range(len(b)):
+            r.clear_color[k] = b[k]
+        r._keep = uniforms
+        return r
+
+    def submit(self, req):
+        """Queues a prepared SrRequest; returns (status, ticket)."""
+        t = C.c_uint64()
+        st = lib().sr_server_submit(self.handle, C.byref(req), C.byref(t))
+        return st, t.value
+
+    def wait(self, ticket, timeout_ms=60000):
+        return lib().sr_server_wait(self.handle, ticket, timeout_ms)
+
+    def read(self, ticket, width, height, color_format):
+        color = (np.empty((height, width, 4), dtype=np.float32) if color_format == A.SR_COLOR_RGBA32F
+                 else np.empty((height, width), dtype=np.uint32))
+        depth = np.empty((height, width), dtype=np.float32)
+        check(lib().sr_server_read(self.handle, ticket, color.ctypes.data, depth.ctypes.data), "sr_server_read")
+        return color, depth
+
+    def release(self, ticket):
+        return lib().sr_server_release(self.handle, ticket)
+
+    def drain(self, timeout_ms=120000):
+        return lib().sr_server_drain(self.handle, timeout_ms)
+
+    def stats(self):
+        s = A.SrServerStats()
+        check(lib().sr_server_get_stats(self.handle, C.byref(s)), "sr_server_get_stats")
+        return {f: getattr(s, f) for f, _ in A.SrServerStats._fields_}
+
+    def reset_stats(self):
+        check(lib().sr_server_reset_stats(self.handle), "sr_server_reset_stats")
+
+    def destroy(self):
+        if self.handle:
+            lib().sr_server_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass

@@ -73,6 +73,24 @@ class SrBatchItem(C.Structure):
     _fields_ = [("target", C.c_void_p), ("draw", SrDraw), ("clear", C.c_uint32), ("clear_color", C.c_uint8 * 16)]
 
 
+class SrServerConfig(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("max_inflight", C.c_uint32), ("max_batch", C.c_uint32),
+                ("plain", C.c_uint32)]
+
+
+class SrRequest(C.Structure):
+    _fields_ = [("draw", SrDraw), ("uniforms", C.c_void_p), ("uniforms_size", C.c_size_t),
+                ("width", C.c_uint32), ("height", C.c_uint32), ("color_format", C.c_uint32),
+                ("clear_color", C.c_uint8 * 16)]
+
+
+class SrServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("batches", C.c_uint64),
+                ("mean_batch", C.c_double), ("p50_ms", C.c_double), ("p99_ms", C.c_double),
+                ("mean_ms", C.c_double), ("max_ms", C.c_double), ("throughput_rps", C.c_double),
+                ("peak_bytes", C.c_uint64)]
+
+
 class SrStats(C.Structure):
     _fields_ = [
         ("triangles_in", C.c_uint64), ("triangles_generated", C.c_uint64),

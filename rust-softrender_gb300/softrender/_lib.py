@@ -48,6 +48,15 @@ SIGNATURES = {
     "sr_batch_render": (C.c_int, [C.c_void_p, C.POINTER(A.SrBatchItem), C.c_uint32]),
     "sr_batch_sync": (C.c_int, [C.c_void_p]),
     "sr_batch_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.SrStats)]),
+    "sr_server_create": (C.c_int, [C.POINTER(A.SrServerConfig), C.POINTER(C.c_void_p)]),
+    "sr_server_submit": (C.c_int, [C.c_void_p, C.POINTER(A.SrRequest), C.POINTER(C.c_uint64)]),
+    "sr_server_wait": (C.c_int, [C.c_void_p, C.c_uint64, C.c_uint32]),
+    "sr_server_read": (C.c_int, [C.c_void_p, C.c_uint64, C.c_void_p, C.c_void_p]),
+    "sr_server_release": (C.c_int, [C.c_void_p, C.c_uint64]),
+    "sr_server_drain": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "sr_server_get_stats": (C.c_int, [C.c_void_p, C.POINTER(A.SrServerStats)]),
+    "sr_server_reset_stats": (C.c_int, [C.c_void_p]),
+    "sr_server_destroy": (C.c_int, [C.c_void_p]),
     "sr_render_static": (C.c_int, [C.POINTER(A.SrDraw), C.c_void_p, C.c_size_t, C.c_void_p, C.c_uint32, C.c_uint32,
                                    C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_uint32,
                                    C.POINTER(A.SrFbDesc), C.c_void_p, C.c_void_p, C.c_void_p]),
