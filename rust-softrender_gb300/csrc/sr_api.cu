@@ -116,13 +116,25 @@ extern "C" SR_API int sr_pipeline_create(const sr_fb_desc* fb, const void* unifo
     if (fb->width > 32767 || fb->height > 32767) return SR_EINVAL;
     if (fb->color_format > SR_COLOR_RGBA8) return SR_EINVAL;
     if (uniforms && usz != sizeof(sr_uniforms)) return SR_EINVAL;
+    sr_pipeline* p = nullptr;
+    const int rc = pipeline_create_cap(fb, (size_t)fb->width * fb->height, &p);
+    if (rc != SR_OK) return rc;
+    if (uniforms) {
+        std::memcpy(&p->U, uniforms, sizeof(sr_uniforms));
+        sr_uniforms_derive(&p->U);
+    }
+    *out = p;
+    return SR_OK;
+}
+
+int sr::pipeline_create_cap(const sr_fb_desc* fb, size_t cap_px, sr_pipeline** out) {
     sr_pipeline* p = new (std::nothrow) sr_pipeline();
     if (!p) return SR_ENOMEM;
     p->fb = *fb;
     std::memset(&p->U, 0, sizeof(p->U));
-    if (uniforms) std::memcpy(&p->U, uniforms, sizeof(sr_uniforms));
     sr_uniforms_derive(&p->U);
-    size_t n = (size_t)fb->width * fb->height;
+    const size_t n = std::max(cap_px, (size_t)fb->width * fb->height);
+    p->cap_px = n;
     cudaError_t e = cudaSuccess;
     if (bytes_per_color(fb->color_format)) e = cudaMalloc(&p->color, n * bytes_per_color(fb->color_format));
     if (e == cudaSuccess && fb->depth) e = cudaMalloc(&p->depth, n * 4);
@@ -149,6 +161,14 @@ extern "C" SR_API int sr_pipeline_create(const sr_fb_desc* fb, const void* unifo
     if (st != SR_OK) { sr_pipeline_destroy(p); return st; }
     cudaStreamSynchronize(p->stream);
     *out = p;
+    return SR_OK;
+}
+
+int sr::pipeline_retarget(sr_pipeline* p, uint32_t width, uint32_t height) {
+    if (!p || width == 0 || height == 0 || width > 32767 || height > 32767) return SR_EINVAL;
+    if ((size_t)width * height > p->cap_px || !p->pending.empty()) return SR_EINVAL;
+    p->fb.width = width;
+    p->fb.height = height;
     return SR_OK;
 }
 

@@ -53,6 +53,7 @@ struct PendingDraw {
 // The pipeline object behind the opaque sr_pipeline handle.
 struct sr_pipeline {
     sr_fb_desc fb;
+    size_t cap_px = 0;          // pixels the colour/depth/stencil planes were allocated for
     void* color = nullptr;
     float* depth = nullptr;
     uint8_t* stencil = nullptr;
@@ -86,3 +87,12 @@ struct sr_pipeline {
     uint32_t last_launches = 0;
     bool last_profiled = false;
 };
+
+namespace sr {
+// Creates a pipeline whose planes hold cap_px pixels (>= width * height), so
+// that pipeline_retarget can later give it any frame of at most cap_px pixels.
+int pipeline_create_cap(const sr_fb_desc* fb, size_t cap_px, sr_pipeline** out);
+// Changes the frame size of an idle pipeline within its capacity (the planes'
+// contents become undefined: clear before drawing).
+int pipeline_retarget(sr_pipeline* p, uint32_t width, uint32_t height);
+}  // namespace sr

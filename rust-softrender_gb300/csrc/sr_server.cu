@@ -50,8 +50,16 @@ struct Slot {
     std::vector<Req*> reqs;     // the batch on the GPU
 };
 
+// Pooled targets come in pixel-capacity classes (powers of two), so that any
+// frame of a class can reuse any pooled target of that class and format.
+uint64_t px_class(uint32_t w, uint32_t h) {
+    uint64_t c = 4096;
+    while (c < (uint64_t)w * h) c <<= 1;
+    return c;
+}
+
 uint64_t target_bytes(uint32_t w, uint32_t h, uint32_t fmt) {
-    const uint64_t px = (uint64_t)w * h;
+    const uint64_t px = px_class(w, h);
     return px * ((fmt == SR_COLOR_RGBA32F ? 16 : 4) + 4 + 8) + px / 256 + 4096;
 }
 
@@ -71,7 +79,7 @@ struct sr_server {
     std::deque<Req*> pending;
     std::unordered_map<uint64_t, Req*> reqs;
     std::vector<Slot> slots;
-    std::multimap<std::tuple<uint32_t, uint32_t, uint32_t>, sr_pipeline*> pool;
+    std::multimap<std::pair<uint64_t, uint32_t>, sr_pipeline*> pool;   // (pixel class, format)
     uint64_t next_ticket = 1;
     uint64_t in_use = 0, peak = 0;
     uint32_t inflight = 0;
@@ -114,20 +122,21 @@ void CUDART_CB batch_done(void* p) {
 }
 
 sr_pipeline* take_target(sr_server* s, uint32_t w, uint32_t h, uint32_t fmt) {
-    // caller holds no lock; the pool is only touched by the worker and by
-    // read/release under the mutex
+    const uint64_t cls = px_class(w, h);
+    sr_pipeline* p = nullptr;
     {
         std::lock_guard<std::mutex> lk(s->mu);
-        auto it = s->pool.find(std::make_tuple(w, h, fmt));
+        auto it = s->pool.find(std::make_pair(cls, fmt));
         if (it != s->pool.end()) {
-            sr_pipeline* p = it->second;
+            p = it->second;
             s->pool.erase(it);
-            return p;
         }
     }
-    sr_fb_desc fb{w, h, fmt, 1, 0};
-    sr_pipeline* p = nullptr;
-    if (sr_pipeline_create(&fb, nullptr, 0, &p) != SR_OK) return nullptr;
+    if (!p) {
+        sr_fb_desc fb{w, h, fmt, 1, 0};
+        if (pipeline_create_cap(&fb, cls, &p) != SR_OK) return nullptr;
+    }
+    if (pipeline_retarget(p, w, h) != SR_OK) { sr_pipeline_destroy(p); return nullptr; }
     return p;
 }
 
@@ -302,7 +311,7 @@ int finish(sr_server* s, uint64_t ticket, void* color, float* depth) {
     if (q->target && (color || depth) && st == SR_OK) st = sr_framebuffer_read(q->target, color, depth, nullptr);
     {
         std::lock_guard<std::mutex> lk(s->mu);
-        if (q->target) s->pool.emplace(std::make_tuple(q->r.width, q->r.height, q->r.color_format), q->target);
+        if (q->target) s->pool.emplace(std::make_pair(px_class(q->r.width, q->r.height), q->r.color_format), q->target);
         s->in_use -= q->bytes;
     }
     s->cv.notify_all();
