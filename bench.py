@@ -19,6 +19,11 @@ Reported (one JSON line on rank 0):
   roofline  HBM roofline of the raster kernel (and of the whole frame)
   cpu_baseline  the CPU restatement of the reference path (oracle/), all
          host threads, on a bounded sample extrapolated to the frame
+  batched  256 draws of uneven sizes: one batch (one launch per stage, CUDA
+         graph) against the plain per-draw pipeline
+  served   a Poisson request stream (2,000 req/s) through the serving loop
+         and through the plain per-request loop: p50/p99 latency, throughput,
+         saturated throughput of both
 
 --impl reference times the reference's CPU path (the oracle restatement; the
 Rust reference cannot be built here) on the same workload and metric.
@@ -259,6 +264,160 @@ def run_ours(args, rank, world, local):
                 launches=launches_per_step * args.steps, wall_s=t_wall)
 
 
+# ------------------------------------------------------- batched / served
+def run_batched():
+    """256 independent draws of uneven sizes (triangles log-uniform in
+    [500, 200000], frames of 256^2 .. 2048^2, random cameras; seeded), rendered
+    (a) per request through the plain pipeline -- clear, sr_render, sr_sync --
+    and (b) as one batch (sr_batch_render: one launch per stage, CUDA graph
+    replay, tuned launch configuration).  Wall time per set of 256, best of
+    several repetitions after warm-up."""
+    import softrender as sr
+    from softrender import scenes
+    inst = scenes.batch_instances()
+    T = []
+    for sc in inst:
+        fb = sr.Framebuffer(sc.width, sc.height, sc.color_format, sc.depth, sc.stencil)
+        pl = sr.Pipeline.from_framebuffer(fb, sc.uniforms)
+        m = sr.Mesh(sc.planes, sc.indices)
+        T.append((pl, m, sr.draw_for_scene(sc, m), sc))
+    tris = sum(sc.n_tris for sc in inst)
+    px = sum(sc.width * sc.height for sc in inst)
+
+    def plain_once():
+        for pl, m, d, sc in T:
+            pl.clear(list(sc.clear_bytes()))
+            sr.submit_scene(pl, m, None, sc)
+            pl.sync()
+    plain_once()
+    plain_once()
+    plain = min(_timed(plain_once) for _ in range(5))
+    b = sr.Batch(use_graphs=True, autotune=True)
+    arr = b.items([(pl, d, sc.clear_bytes()) for pl, m, d, sc in T])
+
+    def batch_once():
+        st = b.render_items(arr)
+        if st != 0 or b.sync() != 0:
+            raise RuntimeError("batch failed: %d" % st)
+    batch_once()                                   # tunes this size class, records the graph
+    for _ in range(3):
+        batch_once()
+    batched = min(_timed(batch_once) for _ in range(10))
+    st = b.stats()
+    cfg = b.config()
+    # one target checked against its plain rendering
+    plain_once()
+    ref = T[0][0].read()[0].copy()
+    batch_once()
+    same = bool(np.array_equal(ref, T[0][0].read()[0]))
+    b.destroy()
+    for pl, m, d, sc in T:
+        pl.destroy()
+        m.free()
+    return {"workload": "256 instances, grid-spheres of 500-200,000 tris (log-uniform), frames 256^2-2048^2, "
+                        "RGBA8 + f32 depth, Blinn-Phong, no GS, random cameras (seed 4)",
+            "triangles": int(tris), "pixels": int(px), "fragments": int(st["fragments"]),
+            "batched_ms": round(batched * 1e3, 3), "batched_mtris_per_s": round(tris / batched / 1e6, 1),
+            "plain_ms": round(plain * 1e3, 3), "plain_mtris_per_s": round(tris / plain / 1e6, 1),
+            "speedup_vs_plain": round(plain / batched, 2), "cuda_graph": True,
+            "launch_config": {"prims_per_warp": cfg[0], "big_threshold": cfg[1], "raster_ctas_per_sm": cfg[2]},
+            "kernel_launches_per_batch": int(st["kernel_launches"]), "target0_equals_plain": same,
+            "timing": "host wall clock per 256 draws incl. sync, best of repetitions"}
+
+
+def _timed(fn):
+    t0 = time.perf_counter()
+    fn()
+    return time.perf_counter() - t0
+
+
+def run_served(rate=2000.0, duration=5.0, sat_duration=1.0):
+    """Poisson request stream against the serving loop and against the plain
+    per-request loop (same server code, one request at a time through
+    sr_render + sr_sync): p50/p99 latency and throughput at `rate`, the plain
+    pipeline's single-request latency, and each mode's saturated throughput
+    (offered load far above capacity)."""
+    import softrender as sr
+    from softrender import scenes
+    meshes, reqs = scenes.served_workload(rate=rate, duration=duration)
+    dev_meshes = [sr.Mesh(p, i) for p, i in meshes]
+    built = [sr.Server.request(sr.draw_for_scene(sc, dev_meshes[mi]), sc.uniforms, sc.width, sc.height,
+                               sc.color_format, sc.clear_bytes()) for _, mi, sc in reqs]
+    arrivals = [a for a, _, _ in reqs]
+
+    def stream(srv, offered=None, limit=None):
+        n = len(built) if limit is None else min(limit, len(built))
+        scale = 1.0 if offered is None else rate / offered
+        tickets = [None] * n
+        def reader():
+            for k in range(n):
+                while tickets[k] is None:
+                    time.sleep(0.0001)
+                srv.wait(tickets[k], 600000)
+                srv.release(tickets[k])
+        th = threading.Thread(target=reader)
+        th.start()
+        t0 = time.perf_counter()
+        for k in range(n):
+            dt = arrivals[k] * scale - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            st, t = srv.submit(built[k])
+            if st != 0:
+                raise RuntimeError("submit failed: %d" % st)
+            tickets[k] = t
+        th.join()
+        return srv.stats()
+
+    def warm(srv):
+        for k in range(min(2000, len(built))):
+            st, t = srv.submit(built[k])
+            srv.wait(t, 600000)
+            srv.release(t)
+        ts = [srv.submit(built[k])[1] for k in range(min(2000, len(built)))]
+        for t in ts:
+            srv.wait(t, 600000)
+            srv.release(t)
+        srv.reset_stats()
+
+    out = {"workload": "Poisson arrivals at %g req/s for %g s (seed 5); pool of 12 resident sphere meshes, "
+                       "1,000-500,000 tris (log-uniform); frames log-uniform 128..1920 x 128..1080; RGBA8 + f32 "
+                       "depth; Blinn-Phong; HBM admission budget 64 GB" % (rate, duration),
+           "requests": len(built)}
+    res = {}
+    for name, plain in (("served", False), ("plain", True)):
+        srv = sr.Server(hbm_budget=64 << 30, max_inflight=3, max_batch=256, plain=plain)
+        warm(srv)
+        s = stream(srv)
+        srv.reset_stats()
+        # saturation: the same stream offered 20x faster, first 1 s worth
+        sat = stream(srv, offered=rate * 20, limit=int(rate * 20 * sat_duration))
+        res[name] = {"p50_ms": round(s["p50_ms"], 3), "p99_ms": round(s["p99_ms"], 3),
+                     "mean_ms": round(s["mean_ms"], 3), "throughput_rps": round(s["throughput_rps"], 1),
+                     "mean_batch": round(s["mean_batch"], 2), "peak_bytes": int(s["peak_bytes"]),
+                     "saturated_throughput_rps": round(sat["throughput_rps"], 1),
+                     "saturated_p99_ms": round(sat["p99_ms"], 3)}
+        if plain:
+            lat = []
+            for k in range(min(1000, len(built))):
+                t0 = time.perf_counter()
+                st, t = srv.submit(built[k])
+                srv.wait(t, 600000)
+                lat.append((time.perf_counter() - t0) * 1e3)
+                srv.release(t)
+            res[name]["single_request_ms"] = {"mean": round(float(np.mean(lat)), 3),
+                                              "p50": round(float(np.percentile(lat, 50)), 3),
+                                              "p99": round(float(np.percentile(lat, 99)), 3)}
+        srv.destroy()
+    for m in dev_meshes:
+        m.free()
+    out.update(res)
+    out["saturated_throughput_ratio"] = round(res["served"]["saturated_throughput_rps"] /
+                                              max(1e-9, res["plain"]["saturated_throughput_rps"]), 2)
+    out["timing"] = "latency = host clock from submission to the completion callback / sync"
+    return out
+
+
 # -------------------------------------------------------------- reporting
 def config_block(world):
     return {"workload": WORKLOAD, "triangles": 1048576, "vertices": 525825, "resolution": "3840x2160",
@@ -300,6 +459,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-draws measurement")
+    ap.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
     args = ap.parse_args()
     rank, world, local = dist_env()
 
@@ -347,6 +508,10 @@ def main():
             "gpu_launches": int(r["launches"]),
             "clocks": r["clocks"],
         }
+        if not args.no_batched:
+            line["batched"] = run_batched()
+        if not args.no_served:
+            line["served"] = run_served()
         if not args.no_cpu_baseline:
             frame_s, sample, threads = cpu_frame_estimate(scene, every=4, tiles=48)
             line["cpu_baseline"] = {"value": round(n_tris / frame_s / 1e6, 5), "unit": "Mtris/s",

@@ -455,3 +455,34 @@ def batch_instances(n=256, seed=4, tri_lo=500, tri_hi=200000,
                          color_format=A.SR_COLOR_RGBA8, vs="mvp_pos_nrm", fs="blinn_phong_dir",
                          uniforms=u, name="inst%d" % i))
     return out
+
+
+def served_workload(rate=2000.0, duration=5.0, seed=5, pool=12, tri_lo=1000, tri_hi=500000,
+                    res_lo=(128, 128), res_hi=(1920, 1080)):
+    """Request stream of the serving benchmark: a pool of resident seeded
+    sphere meshes (triangle counts log-uniform in [tri_lo, tri_hi]) and
+    Poisson arrivals at `rate` per second for `duration` seconds; each request
+    takes a pool mesh, a random camera and a resolution with width and height
+    log-uniform between res_lo and res_hi, RGBA8 + f32 depth, Blinn-Phong.
+    Returns (meshes, requests): meshes = [(planes, indices)], requests =
+    [(arrival_s, mesh_index, Scene)]."""
+    rng = np.random.default_rng(seed)
+    meshes = []
+    for i in range(pool):
+        t = int(round(math.exp(rng.uniform(math.log(tri_lo), math.log(tri_hi)))))
+        meshes.append(sphere_mesh_for_tris(t, seed * 1000 + i))
+    n = int(rate * duration)
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    reqs = []
+    for k in range(n):
+        mi = int(rng.integers(pool))
+        w = int(round(math.exp(rng.uniform(math.log(res_lo[0]), math.log(res_hi[0])))))
+        h = int(round(math.exp(rng.uniform(math.log(res_lo[1]), math.log(res_hi[1])))))
+        eye = random_camera(rng)
+        u = make_uniforms(view=look_at_rh(eye, (0, 0, 0), (0, 1, 0)),
+                          projection=perspective(w / h, math.radians(60.0), 0.1, 100.0), camera=eye)
+        planes, idx = meshes[mi]
+        reqs.append((float(arrivals[k]), mi, Scene(planes=planes, indices=idx, width=w, height=h,
+                                                   color_format=A.SR_COLOR_RGBA8, vs="mvp_pos_nrm",
+                                                   fs="blinn_phong_dir", uniforms=u, name="req%d" % k)))
+    return meshes, reqs
