@@ -236,7 +236,11 @@ SR_API int sr_shader_lookup(const char* name, int stage, int* id);
 /* --------------------------------------------------------------- render */
 
 SR_API void sr_draw_init(sr_draw* d);
-/* Runs one pass of the chain on the pipeline's stream (see sr_draw). */
+/* One pass of the chain Pipeline::render_mesh (src/pipeline/mod.rs:146-155)
+ * -> VertexShader::run / run_to_fragment (stages/vertex.rs:87-160) ->
+ * GeometryShader::clip_primitives + finish (stages/geometry.rs:60-129,
+ * 261-336) -> FragmentShader::run (stages/fragment.rs:169-318), enqueued on
+ * the pipeline's stream (see sr_draw). */
 SR_API int sr_render(sr_pipeline* p, const sr_draw* d);
 /* Waits for the pipeline's stream; returns the first device-recorded error of
  * the draws since the previous sync (SR_ENAN, SR_EOVERFLOW) or SR_ECUDA. */
