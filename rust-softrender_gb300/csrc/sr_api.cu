@@ -186,6 +186,7 @@ extern "C" SR_API int sr_pipeline_destroy(sr_pipeline* p) {
     p->bin_counts.release(); p->bin_off.release(); p->bin_cursor.release(); p->bin_tmp.release(); p->entries.release(); p->unsafe_list.release();
     p->st_diff.release(); p->st_lines.release(); p->st_glob.release();
     p->area.release(); p->big_list.release(); p->gkeys.release(); p->bitmap.release();
+    p->lpv.release(); p->lpvalid.release();
     for (auto& e : p->ev) if (e) cudaEventDestroy(e);
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
     delete p;
@@ -389,7 +390,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
     P.nrows = H >= 2 ? (H - 1 + d->tile_h - 1) / d->tile_h : 0;
     P.n_verts = m->n_verts;
     P.gen_base = m->n_pad;
-    P.n_in = (uint32_t)(m->n_indices / 3);
+    P.n_in = (uint32_t)(m->n_indices / std::max(1u, d->prim));
     P.cull = d->cull;
     P.vs = d->vs; P.fs = d->fs; P.blend = d->blend;
     std::memcpy(P.vp, &d->viewport, sizeof(P.vp));
@@ -434,6 +435,39 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
     p->last_launches = 0;
     p->last_profiled = false;
     if (nothing) return SR_OK;
+
+    // ---- lines and points (and triangles turned into lines by a named GS)
+    const bool named = d->gs_mode == SR_GS_NAMED && d->gs != GS_CLIP;
+    if (d->prim != SR_PRIM_TRIANGLE || named) {
+        const uint32_t prim_n = d->prim;
+        const uint32_t n_in = (uint32_t)(m->n_indices / prim_n);
+        const uint32_t prim_out = (named && prim_n == 3) ? 2u : prim_n;
+        const uint32_t n_out = (named && prim_n == 3) ? (d->gs == GS_VERTEX_NORMALS ? 3u : 1u) * n_in : n_in;
+        const bool gs = d->gs_mode != SR_GS_NONE;
+        P.aa_lines = d->aa_lines ? 1u : 0u;
+        int rc2;
+        if ((rc2 = p->scr4.ensure(m->n_pad + 4)) || (rc2 = p->vary.ensure(((size_t)m->n_pad + 4) * VSTRIDE)) ||
+            (gs && (rc2 = p->clip4.ensure(m->n_pad + 4))) ||
+            (rc2 = p->lpv.ensure(4 * ((size_t)n_out * prim_out + 1))) || (rc2 = p->lpvalid.ensure((size_t)n_out + 1)))
+            return rc2;
+        VertexStore vs{p->clip4.p, p->scr4.p, p->vary.p, (uint32_t)p->scr4.cap};
+        cudaEvent_t* ev = p->profiling ? p->ev : nullptr;
+        if (ev) cudaEventRecord(ev[0], st);
+        launch_vertex(P, pd.U, m, vs, gs, st);
+        if (ev) { cudaEventRecord(ev[1], st); }
+        LPV* lv = reinterpret_cast<LPV*>(p->lpv.p);
+        launch_lp_geometry(P, pd.U, m, vs, prim_n, d->gs_mode, (uint32_t)d->gs, lv, p->lpvalid.p, p->flags, st);
+        if (ev) { cudaEventRecord(ev[2], st); cudaEventRecord(ev[3], st); }
+        const uint32_t tex_launches = 0;
+        const uint32_t* tex = d->texture ? d->texture->data : nullptr;
+        const uint32_t ph = launch_lp_raster(P, pd.U, lv, p->lpvalid.p, n_out, prim_out, tex, p->color, p->depth,
+                                             p->stencil, p->flags, st);
+        if (ev) { cudaEventRecord(ev[4], st); cudaEventRecord(ev[5], st); }
+        p->last_launches = 2 + ph + tex_launches;
+        p->last_profiled = ev != nullptr;
+        SR_CK(cudaGetLastError());
+        return SR_OK;
+    }
 
     // ---- capacities
     if (!indexed) {
@@ -533,11 +567,14 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
 extern "C" SR_API int sr_render(sr_pipeline* p, const sr_draw* d) {
     if (!p || !d || !d->mesh) return SR_EINVAL;
     const sr_mesh* m = d->mesh;
-    if (d->prim != SR_PRIM_TRIANGLE) return SR_EINVAL;
-    if (m->n_indices % 3 != 0) return SR_EINVAL;                          // mod.rs:148
+    if (d->prim != SR_PRIM_TRIANGLE && d->prim != SR_PRIM_LINE && d->prim != SR_PRIM_POINT) return SR_EINVAL;
+    if (m->n_indices % d->prim != 0) return SR_EINVAL;                     // mod.rs:148
     if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT || d->blend < 0 || d->blend >= BLEND_COUNT)
         return SR_EINVAL;
-    if (d->gs_mode != SR_GS_NONE && d->gs_mode != SR_GS_CLIP) return SR_EINVAL;
+    if (d->gs_mode != SR_GS_NONE && d->gs_mode != SR_GS_CLIP && d->gs_mode != SR_GS_NAMED) return SR_EINVAL;
+    if (d->gs_mode == SR_GS_NAMED && (d->gs < 0 || d->gs >= GS_COUNT)) return SR_EINVAL;
+    // the normal shaders read world position and normal from varyings 0..7
+    if (d->gs_mode == SR_GS_NAMED && d->gs != GS_CLIP && vs_nk(d->vs) < 8) return SR_EINVAL;
     if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
     if (d->cull > SR_CULL_COUNTER_CLOCKWISE) return SR_EINVAL;
     if (m->n_planes < (uint32_t)vs_planes(d->vs)) return SR_EINVAL;
@@ -576,7 +613,7 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
             p->last_stats.nan_bbox = f.nan_bbox;
             p->last_stats.overflow = f.overflow_bits;
             const sr_mesh* m = p->pending.back().d.mesh;
-            p->last_stats.triangles_in = m ? m->n_indices / 3 : 0;
+            p->last_stats.triangles_in = m ? m->n_indices / std::max(1u, p->pending.back().d.prim) : 0;
             p->last_stats.kernel_launches = p->last_launches;
             if (p->last_profiled) {
                 p->last_stats.profiled = 1;

@@ -75,6 +75,8 @@ struct sr_pipeline {
     sr::DevBuf<uint32_t> big_list;
     sr::DevBuf<uint32_t> bitmap;
     sr::DevBuf<int> st_diff, st_lines;
+    sr::DevBuf<float4> lpv;           // line / point vertices (4 x float4 each)
+    sr::DevBuf<uint8_t> lpvalid;      // per line / point: kept by the geometry stage
     sr::DevBuf<unsigned long long> st_glob;
     // capacities (elements) requested for the generated geometry
     uint64_t gen_tri_cap = 0, gen_vert_cap = 0, entry_cap = 0;

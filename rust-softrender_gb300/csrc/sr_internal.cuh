@@ -92,6 +92,7 @@ struct DrawParams {
     uint32_t stencil_active;      // stencil plane changes during this draw
     uint32_t draw_id;             // sequence number of the draw since the last sync
     uint32_t force_unsafe;        // test hook: treat every primitive as unsafe
+    uint32_t aa_lines;            // Xiaolin Wu lines (FragmentShader::antialiased_lines)
 };
 
 // Setup record of a raster triangle (64 bytes):
@@ -285,6 +286,15 @@ struct OpaqueArgs {
 };
 // Opaque draws (sr_opaque.cu); returns the number of kernels launched.
 int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A, cudaStream_t st);
+// Lines and points (sr_lp.cu).  An LP vertex is 64 bytes: screen position
+// and 12 varyings.
+struct LPV;
+void launch_lp_geometry(const DrawParams& P, const sr_uniforms& U, const sr_mesh* m, VertexStore vs, uint32_t prim_n,
+                        uint32_t gs_mode, uint32_t gs, LPV* out, uint8_t* valid, DeviceFlags* flags,
+                        cudaStream_t st);
+uint32_t launch_lp_raster(const DrawParams& P, const sr_uniforms& U, const LPV* v, const uint8_t* valid,
+                          uint32_t n_prims, uint32_t prim_n, const uint32_t* tex, void* color, float* depth,
+                          uint8_t* stencil, DeviceFlags* flags, cudaStream_t st);
 // Blending / stencil-gated draws over sorted bins (sr_raster.cu).
 void launch_ordered(const DrawParams& P, const sr_uniforms& U, const float4* setup, const uint32_t* bin_off,
                     const uint32_t* entries, const uint32_t* vidx, const float* vary, const uint32_t* tex, void* color,

@@ -486,3 +486,35 @@ def served_workload(rate=2000.0, duration=5.0, seed=5, pool=12, tri_lo=1000, tri
                                                    color_format=A.SR_COLOR_RGBA8, vs="mvp_pos_nrm",
                                                    fs="blinn_phong_dir", uniforms=u, name="req%d" % k)))
     return meshes, reqs
+
+
+def lines_scene(n=600, size=200, seed=12, prim=A.SR_PRIM_LINE, outside=0.25, **kw):
+    """Lines (or points, prim=SR_PRIM_POINT) with random end points in clip
+    space (w = 1; about `outside` of the end points beyond the frustum, so the
+    clipping arms have work), depth in (-0.9, 0.9) NDC, RGBA8-packed vertex
+    colours; vertex shader clip_rgba8, fragment shader vertex_color."""
+    rng = np.random.default_rng(seed)
+    W = H = size
+    nv = n * (2 if prim == A.SR_PRIM_LINE else 1)
+    lo, hi = -outside * size, (1.0 + outside) * size
+    sx = rng.uniform(lo, hi, nv)
+    sy = rng.uniform(lo, hi, nv)
+    if prim == A.SR_PRIM_LINE:
+        # mostly short segments, some long ones crossing tiles
+        ln = np.exp(rng.uniform(math.log(0.5), math.log(0.6 * size), n))
+        ang = rng.uniform(0.0, 2.0 * math.pi, n)
+        sx[1::2] = sx[0::2] + np.cos(ang) * ln
+        sy[1::2] = sy[0::2] + np.sin(ang) * ln
+    z = rng.uniform(-0.9, 0.9, nv)
+    x, y, zz = _clip_from_screen(sx, sy, z, W, H)
+    col = rng.integers(0, 256, (nv, 4))
+    col[:, 3] = rng.integers(128, 256, nv)
+    packed = _pack_rgba8(col[:, 0], col[:, 1], col[:, 2], col[:, 3])
+    planes = [np.ascontiguousarray(x, dtype=np.float32), np.ascontiguousarray(y, dtype=np.float32),
+              np.ascontiguousarray(zz, dtype=np.float32), packed.view(np.float32).copy()]
+    sc = Scene(planes=planes, indices=np.arange(nv, dtype=np.uint32), width=W, height=H,
+               color_format=A.SR_COLOR_RGBA8, vs="clip_rgba8", fs="vertex_color", prim=prim, tile=(32, 32),
+               name="%s_%d_%d" % ("lines" if prim == A.SR_PRIM_LINE else "points", n, size))
+    for k, val in kw.items():
+        setattr(sc, k, val)
+    return sc
