@@ -1,0 +1,223 @@
+"""Known-answer tests that pin the CPU oracle (oracle/) to the reference.
+
+The reference's own tests hold one value-pinning test, coordinate_index
+(src/geometry/coordinate.rs:66-87); it is restated first.  The others are
+hand-derived from the reference's formulas (file:line in each test) and are
+computed here independently of the oracle's code: tile walks from the loop
+in fragment.rs:188-216, viewport products from clipvertex.rs:89-127, the
+clip push order of geometry.rs:264-299, coverage from triangle.rs:104-126
+evaluated with numpy float32 (IEEE single, no contraction), the f32::MIN
+depth clear, ties passing `>=`, stencil events per tile pass, and the
+accuracy of the pow used by the shaders.  No GPU needed."""
+import ctypes as C
+import math
+
+import numpy as np
+import pytest
+
+from softrender import _abi as A
+from softrender import scenes
+
+F = np.float32
+
+
+def test_coordinate_index(oracle_mod):
+    """coordinate.rs:66-87: index = x + y * width and back, on a 10 x 20 grid."""
+    L = oracle_mod.lib()
+    i = 0
+    for y in range(20):
+        for x in range(10):
+            assert L.or_coordinate_into_index(x, y, 10) == i
+            ox, oy = C.c_uint32(), C.c_uint32()
+            L.or_coordinate_from_index(i, 10, C.byref(ox), C.byref(oy))
+            assert (ox.value, oy.value) == (x, y)
+            i += 1
+
+
+def _tiles_by_hand(W, H, tw, th):
+    # fragment.rs:188-216, written out independently
+    out = []
+    y = 0
+    while y < H - 1:
+        ny = min(y + th, H - 1)
+        x = 0
+        while x < W - 1:
+            nx = min(x + tw, W - 1)
+            out.append((x, y, nx, ny))
+            x = nx
+        y = ny
+    return out
+
+
+@pytest.mark.parametrize("W,H,tw,th,n", [(5, 4, 2, 2, 4), (1024, 1024, 128, 128, 64), (3840, 2160, 128, 128, 510),
+                                         (2048, 2048, 128, 128, 256), (97, 61, 7, 13, None), (2, 2, 128, 128, 1),
+                                         (1, 9, 4, 4, 0)])
+def test_tiles(oracle_mod, W, H, tw, th, n):
+    t = oracle_mod.tiles(W, H, tw, th)
+    assert t == _tiles_by_hand(W, H, tw, th)
+    if n is not None:
+        assert len(t) == n
+    # adjacent tiles share a column / row (inclusive corners)
+    if len(t) > 1 and t[0][1] == t[1][1]:
+        assert t[0][2] == t[1][0]
+
+
+def test_tiles_small_known_answer(oracle_mod):
+    assert oracle_mod.tiles(5, 4, 2, 2) == [(0, 0, 2, 2), (2, 0, 4, 2), (0, 2, 2, 3), (2, 2, 4, 3)]
+
+
+def test_normalize_known_answers(oracle_mod):
+    """clipvertex.rs:89-127 with viewport (0, 0, W, H, near 0, far 1): x' = W/2 x
+    + W/2, y' = -H/2 y + H/2, z' = -z/2 - 1/2 (nearer is larger), w' = 1/w."""
+    vp = (0.0, 0.0, 640.0, 480.0, 0.0, 1.0)
+    assert np.array_equal(oracle_mod.normalize((0, 0, 0, 1), vp), np.array([320, 240, -0.5, 1], F))
+    assert np.array_equal(oracle_mod.normalize((2, 2, 2, 2), vp), np.array([640, 0, -1, 0.5], F))
+    assert np.array_equal(oracle_mod.normalize((-4, -4, 4, 4), vp), np.array([0, 480, -1, 0.25], F))
+
+
+def test_clip_inside_triangle_structure(oracle_mod):
+    """geometry.rs:264-299: a triangle inside every plane pushes each vertex 6
+    times (poly = b*6, c*6, a*6) and the fan from the last entry yields 16
+    triangles: (a, b, c) at index 5, the other 15 exactly degenerate."""
+    a = (0.1, 0.2, 0.3, 1.0)
+    b = (0.5, -0.2, 0.4, 1.0)
+    c = (-0.3, 0.6, 0.5, 1.0)
+    out = oracle_mod.clip_triangle(a, b, c).reshape(-1, 3, 4)
+    assert out.shape[0] == 16
+    assert np.array_equal(out[5], np.array([a, b, c], F))
+    for k in range(16):
+        if k == 5:
+            continue
+        t = out[k]
+        assert (np.array_equal(t[0], t[1]) or np.array_equal(t[1], t[2]) or np.array_equal(t[0], t[2])), k
+
+
+def test_clip_near_plane(oracle_mod):
+    """Near plane is z >= 0 (clip.rs:33-44).  The push loop of geometry.rs:
+    270-284 tests each plane independently, so with a (z < 0) outside only the
+    near plane the polygon is [b b b b I_ab b b | c*6 | a a a a I_ca a]
+    (19 entries -> 17 fan triangles): the near-plane intersections lie
+    exactly on z = 0 (t = 0.5 here), and a itself is still emitted."""
+    a = (0.0, 0.0, -0.5, 1.0)
+    b = (0.5, 0.0, 0.5, 1.0)
+    c = (0.0, 0.5, 0.5, 1.0)
+    out = oracle_mod.clip_triangle(a, b, c).reshape(-1, 3, 4)
+    assert out.shape[0] == 17
+    verts = {tuple(v) for v in out.reshape(-1, 4).tolist()}
+    assert (0.25, 0.0, 0.0, 1.0) in verts            # I_ab = lerp(0.5, a, b)
+    assert (0.0, 0.25, 0.0, 1.0) in verts            # I_ca = lerp(0.5, c, a)
+    assert a in verts
+    assert sorted(v for v in verts if v[2] == 0.0) == [(0.0, 0.25, 0.0, 1.0), (0.25, 0.0, 0.0, 1.0)]
+
+
+def _one_triangle_scene(tri_screen, W, H, z=(-0.5, -0.5, -0.5), rgba=(255, 0, 0, 255), **kw):
+    tri = np.asarray(tri_screen, dtype=np.float64)
+    x, y, zz = scenes._clip_from_screen(tri[:, 0], tri[:, 1], np.asarray(z) * -2.0 - 1.0, W, H)
+    col = np.array([rgba] * len(tri))
+    packed = scenes._pack_rgba8(col[:, 0], col[:, 1], col[:, 2], col[:, 3])
+    planes = [np.asarray(x, F), np.asarray(y, F), np.asarray(zz, F), packed.view(np.float32).copy()]
+    sc = scenes.Scene(planes=planes, indices=np.arange(len(tri), dtype=np.uint32), width=W, height=H,
+                      color_format=A.SR_COLOR_RGBA8, vs="clip_rgba8", fs="vertex_color", tile=(4, 4),
+                      clear_color=(0, 0, 0, 0))
+    for k, v in kw.items():
+        setattr(sc, k, v)
+    return sc
+
+
+def _coverage_by_hand(v, W, H):
+    """triangle.rs:64,104-113 in float32: inclusive, NaN counts as covered."""
+    (x1, y1), (x2, y2), (x3, y3) = [(F(p[0]), F(p[1])) for p in v]
+    det = (y2 - y3) * (x1 - x3) + (x3 - x2) * (y1 - y3)
+    m = np.zeros((H, W), bool)
+    for py in range(H):
+        for px in range(W):
+            x, y = F(px) + F(0.5), F(py) + F(0.5)
+            u = ((y2 - y3) * (x - x3) + (x3 - x2) * (y - y3)) / det
+            vv = ((y3 - y1) * (x - x3) + (x1 - x3) * (y - y3)) / det
+            w = (F(1) - u) - vv
+            m[py, px] = not (u < 0 or vv < 0 or w < 0)
+    return m
+
+
+def test_single_triangle_mask(oracle_mod):
+    W = H = 12
+    scr = [(1.25, 1.5), (10.5, 3.0), (4.0, 10.75)]
+    sc = _one_triangle_scene(scr, W, H)
+    fb, st, status = oracle_mod.render(sc)
+    assert status == 0
+    # the oracle's screen positions come from the same clip -> normalize path
+    tri = oracle_mod.raster_tris(sc)[0]
+    want = _coverage_by_hand([(tri[0][0], tri[0][1]), (tri[1][0], tri[1][1]), (tri[2][0], tri[2][1])], W, H)
+    got = fb.color.view(np.uint32).reshape(H, W) != 0
+    assert np.array_equal(got, want)
+    assert st["fragments"] == int(want.sum())
+
+
+def test_shared_edge_is_inclusive_and_ties_pass(oracle_mod):
+    """Two triangles sharing an edge at equal depth: the edge pixels are
+    covered by both (no top-left rule) and the later one wins (>=)."""
+    W = H = 10
+    quad = [(1.0, 1.0), (9.0, 1.0), (1.0, 9.0), (9.0, 1.0), (9.0, 9.0), (1.0, 9.0)]
+    sc = _one_triangle_scene(quad, W, H)
+    col = np.array([(255, 0, 0, 255)] * 3 + [(0, 255, 0, 255)] * 3)
+    sc.planes[3] = scenes._pack_rgba8(col[:, 0], col[:, 1], col[:, 2], col[:, 3]).view(np.float32).copy()
+    fb, _, _ = oracle_mod.render(sc)
+    tris = oracle_mod.raster_tris(sc)
+    m1 = _coverage_by_hand([tris[0][j][:2] for j in range(3)], W, H)
+    m2 = _coverage_by_hand([tris[1][j][:2] for j in range(3)], W, H)
+    both = m1 & m2
+    assert both.any()                                  # inclusive edges: the diagonal is in both
+    c = fb.color.view(np.uint32).reshape(H, W)
+    green = scenes._pack_rgba8(np.array([0]), np.array([255]), np.array([0]), np.array([255]))[0]
+    assert (c[both] == green).all()                    # the later triangle passes the >= test
+
+
+def test_depth_clear_is_f32_min(oracle_mod):
+    sc = _one_triangle_scene([(0, 0), (1, 0), (0, 1)], 4, 4)
+    fb = oracle_mod.framebuffer_for(sc)
+    assert (fb.depth == np.float32(-3.4028235e38)).all()
+
+
+def test_stencil_counts_every_tile_pass(oracle_mod):
+    """stencil.rs:112-158 applied per clamped-bbox pixel per tile pass
+    (triangle.rs:90-99): a triangle whose bbox covers the frame increments
+    each pixel once per semantic tile containing it (1, 2 or 4)."""
+    W, H = 9, 9
+    sc = _one_triangle_scene([(-5.0, -5.0), (30.0, -5.0), (-5.0, 30.0)], W, H, stencil=True,
+                             stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT)
+    fb, _, _ = oracle_mod.render(sc)
+    want = np.zeros((H, W), np.uint8)
+    for (x0, y0, x1, y1) in _tiles_by_hand(W, H, 4, 4):
+        want[y0:y1 + 1, x0:x1 + 1] += 1
+    assert np.array_equal(fb.stencil, want)
+    assert want.max() == 4 and want.min() == 1
+
+
+def test_pow_accuracy(oracle_mod):
+    """The shaders' powf (own double-float log2/exp2) is within 2 ULP of the
+    exact power (float64 reference) over the ranges the shaders use."""
+    rng = np.random.default_rng(0)
+    xs = np.concatenate([rng.uniform(0, 1, 3000), np.exp(rng.uniform(-80, 5, 2000))]).astype(F)
+    ys = np.array([2.2, 1 / 2.2, 64.0, 5.0, 0.5, 3.7, -1.3], F)
+    worst = 0.0
+    for y in ys:
+        for x in xs[::7]:
+            got = oracle_mod.powf(x, y)
+            exact = float(x) ** float(y)
+            if exact == 0.0 or not math.isfinite(exact) or exact < 1.2e-38 or exact > 3.0e38:
+                continue
+            ulp = float(np.spacing(np.float32(exact)))
+            worst = max(worst, abs(float(got) - exact) / ulp)
+    assert worst <= 2.0, worst
+
+
+def test_pow_special_cases(oracle_mod):
+    p = oracle_mod.powf
+    assert p(0.0, 2.2) == 0.0 and p(1.0, 123.0) == 1.0 and p(3.0, 0.0) == 1.0
+    assert p(2.0, 10.0) == 1024.0 and p(0.25, 0.5) == 0.5
+    assert np.isnan(p(-2.0, 0.5))
+
+
+def test_byte_to_unit_exact(oracle_mod):
+    for c in range(256):
+        assert oracle_mod.u8_unit(c) == F(c) / F(255)
