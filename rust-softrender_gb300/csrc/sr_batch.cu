@@ -297,7 +297,8 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
                 const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)H - 1);
                 const uint32_t w = x1 - x0 + 1;
                 mark_rect(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1);
-                sxy[wl][lane] = x0 | (y0 << 16);
+                const uint32_t sb = seam_bits(x0, y0, x1, y1, W, H, I.P.tile_w, I.P.tile_h);
+                sxy[wl][lane] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
                 sw[wl][lane] = w;
                 Slot S;
                 S.wh = W | (H << 16);
@@ -332,8 +333,9 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
                 const uint32_t xy = sxy[wl][lo];
                 const Slot& S = sslot[wl][lo];
                 frag_emit(S.wh & 0xffffu, S.wh >> 16, S.tiles & 0xffffu, S.tiles >> 16, S.mx, S.my,
-                          (S.n_depth >> 31) != 0, srec[wl][lo][0], srec[wl][lo][1], srec[wl][lo][2], S.t,
-                          (xy & 0xffffu) + (local - row * w), (xy >> 16) + row, S.n_depth & 0x7fffffffu, S.gkeys,
+                          ((xy >> 15) & 1u) | ((xy >> 30) & 2u), (S.n_depth >> 31) != 0, srec[wl][lo][0],
+                          srec[wl][lo][1], srec[wl][lo][2], S.t, (xy & 0x7fffu) + (local - row * w),
+                          ((xy >> 16) & 0x7fffu) + row, S.n_depth & 0x7fffffffu, S.gkeys,
                           nullptr, 0u, 0u, 0u, frags);
             }
         }
@@ -398,7 +400,7 @@ __global__ void __launch_bounds__(256) batch_raster_big_kernel(BTables T, const 
         const uint32_t t = g - I.tbase;
         for (unsigned long long q = p0 + threadIdx.x; q < p1; q += blockDim.x) {
             const uint32_t row = (uint32_t)(q / w), col = (uint32_t)(q - (unsigned long long)row * w);
-            frag_emit(W, H, I.P.tile_w, I.P.tile_h, I.mx, I.my, I.P.has_depth != 0, r0, r1, r2, t, x0 + col,
+            frag_emit(W, H, I.P.tile_w, I.P.tile_h, I.mx, I.my, 3u, I.P.has_depth != 0, r0, r1, r2, t, x0 + col,
                       y0 + row, I.P.n_raster_host, I.gkeys, nullptr, 0u, 0u, 0u, frags);
         }
     }

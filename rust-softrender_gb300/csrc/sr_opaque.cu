@@ -73,7 +73,8 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
                 const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1);
                 const uint32_t w = x1 - x0 + 1;
                 mark_rect(bitmap, blocks_x, x0, y0, x1, y1);
-                sxy[wl][lane] = x0 | (y0 << 16);
+                const uint32_t sb = seam_bits(x0, y0, x1, y1, P.W, P.H, P.tile_w, P.tile_h);
+                sxy[wl][lane] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
                 sw[wl][lane] = w;
                 smag[wl][lane] = ((1ull << 32) + w - 1) / w;
             }
@@ -98,8 +99,8 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
                 const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][lo]) >> 32);  // local / w
                 const uint32_t xy = sxy[wl][lo];
                 rg_fragment(P, srec[wl][lo][0], srec[wl][lo][1], srec[wl][lo][2], t0 + lo,
-                            (xy & 0xffffu) + (local - row * w), (xy >> 16) + row, N, gkeys, bitmap, stencil,
-                            gate_with_stencil, mx, my, frags);
+                            (xy & 0x7fffu) + (local - row * w), ((xy >> 16) & 0x7fffu) + row, N, gkeys, bitmap,
+                            stencil, gate_with_stencil, mx, my, ((xy >> 15) & 1u) | ((xy >> 30) & 2u), frags);
             }
         }
         __syncwarp();
@@ -128,6 +129,8 @@ __global__ void __launch_bounds__(RG_THREADS) raster_big_kernel(
         const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)P.W - 1);
         const uint32_t w = x1 - x0 + 1;
         const unsigned long long at = area[t];
+        const uint32_t sb = seam_bits(x0, y0, x1, (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1), P.W, P.H,
+                                      P.tile_w, P.tile_h);
         {
             const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1);
             const uint32_t bx0 = x0 >> TOUCH_LOG2, by0 = y0 >> TOUCH_LOG2;
@@ -139,7 +142,8 @@ __global__ void __launch_bounds__(RG_THREADS) raster_big_kernel(
         }
         for (unsigned long long j = threadIdx.x; j < at; j += RG_THREADS) {
             const uint32_t row = (uint32_t)(j / w), col = (uint32_t)(j - (unsigned long long)row * w);
-            rg_fragment(P, r0, r1, r2, t, x0 + col, y0 + row, N, gkeys, bitmap, stencil, gate_with_stencil, mx, my, frags);
+            rg_fragment(P, r0, r1, r2, t, x0 + col, y0 + row, N, gkeys, bitmap, stencil, gate_with_stencil, mx, my,
+                        sb, frags);
         }
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);

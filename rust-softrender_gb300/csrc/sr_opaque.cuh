@@ -43,8 +43,12 @@ __device__ __forceinline__ void mark_rect(uint32_t* bitmap, uint32_t blocks_x, u
 // inclusive coverage, z < 0, optional stencil gate; emits the 64-bit key.
 // The target is given by its scalars (frame size, semantic tile size with
 // its division magics, depth attachment, stencil gate).
+//
+// seams: bit 0 set when the primitive's bbox may contain a seam column, bit 1
+// a seam row (seam_bits); otherwise that axis has one semantic tile.
 __device__ __forceinline__ void frag_emit(uint32_t W, uint32_t H, uint32_t tile_w, uint32_t tile_h, uint32_t mx,
-                                          uint32_t my, bool has_depth, float4 r0, float4 r1, float4 r2, uint32_t t,
+                                          uint32_t my, uint32_t seams, bool has_depth, float4 r0, float4 r1, float4 r2,
+                                          uint32_t t,
                                           uint32_t px, uint32_t py, uint32_t N, unsigned long long* __restrict__ gkeys,
                                           const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
                                           uint32_t stencil_test_id, uint32_t sref, unsigned long long& frags) {
@@ -61,7 +65,8 @@ __device__ __forceinline__ void frag_emit(uint32_t W, uint32_t H, uint32_t tile_
     if (!(z < 0.0f)) return;
     const size_t gi = (size_t)py * W + px;
     if (gate_with_stencil && !stencil_test(stencil_test_id, __ldg(stencil + gi), sref)) return;
-    const int kp = seam_count(px, tile_w, mx, W - 1) * seam_count(py, tile_h, my, H - 1);
+    const int kp = ((seams & 1u) ? seam_count(px, tile_w, mx, W - 1) : 1) *
+                   ((seams & 2u) ? seam_count(py, tile_h, my, H - 1) : 1);
     ++frags;
     const uint32_t zk = has_depth ? zkey(z) : 0u;
     atomicMax(gkeys + gi, ((unsigned long long)zk << 32) | (unsigned long long)((uint32_t)(kp - 1) * N + t + 1u));
@@ -71,9 +76,25 @@ __device__ __forceinline__ void rg_fragment(const DrawParams& P, float4 r0, floa
                                             uint32_t px, uint32_t py, uint32_t N,
                                             unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap,
                                             const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
-                                            uint32_t mx, uint32_t my, unsigned long long& frags) {
-    frag_emit(P.W, P.H, P.tile_w, P.tile_h, mx, my, P.has_depth != 0, r0, r1, r2, t, px, py, N, gkeys, stencil,
-              gate_with_stencil, P.stencil_test, P.sref, frags);
+                                            uint32_t mx, uint32_t my, uint32_t seams, unsigned long long& frags) {
+    frag_emit(P.W, P.H, P.tile_w, P.tile_h, mx, my, seams, P.has_depth != 0, r0, r1, r2, t, px, py, N, gkeys,
+              stencil, gate_with_stencil, P.stencil_test, P.sref, frags);
+}
+
+// Whether the clamped bbox [x0, x1] x [y0, y1] contains a seam column (bit 0:
+// 0 < p < W-1 with p a multiple of the tile width) or a seam row (bit 1).
+__device__ __forceinline__ uint32_t seam_bits(uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, uint32_t W,
+                                              uint32_t H, uint32_t tile_w, uint32_t tile_h) {
+    uint32_t s = 0;
+    {
+        const uint32_t lo = max(x0, 1u), hi = min(x1, W - 2);
+        if (lo <= hi && ((lo + tile_w - 1) / tile_w) * tile_w <= hi) s |= 1u;
+    }
+    {
+        const uint32_t lo = max(y0, 1u), hi = min(y1, H - 2);
+        if (lo <= hi && ((lo + tile_h - 1) / tile_h) * tile_h <= hi) s |= 2u;
+    }
+    return s;
 }
 
 constexpr uint32_t RG_BIG = 2048;   // bbox pixels above which a primitive goes to the block-cooperative pass
