@@ -19,6 +19,8 @@ Reported (one JSON line on rank 0):
   roofline  HBM roofline of the raster kernel (and of the whole frame)
   cpu_baseline  the CPU restatement of the reference path (oracle/), all
          host threads, on a bounded sample extrapolated to the frame
+  other_frames  the small plain frame (icosphere, 1024^2) and the ordering /
+         tiny-triangle stress frame (16.8M tiny + 4,096 alpha triangles)
   batched  256 draws of uneven sizes: one batch (one launch per stage, CUDA
          graph) against the plain per-draw pipeline
   served   a Poisson request stream (2,000 req/s) through the serving loop
@@ -223,7 +225,12 @@ def run_ours(args, rank, world, local):
     pl.set_profiling(False)
     stage = {k: float(np.median(v)) for k, v in stage.items()}
 
-    # end to end through the C ABI with host buffers
+    # end to end through the C ABI with host buffers: every step uploads the
+    # mesh and texture from pinned host memory, renders, and copies colour and
+    # depth back to pinned host memory.  Two pipelines (each with its own
+    # mesh, texture and stream) alternate, so step i's copies overlap step
+    # i+1's work; a pipeline's host result is complete when it is synced
+    # before its next use and at the end.
     e2e = None
     if not args.no_e2e:
         keep = []
@@ -232,32 +239,53 @@ def run_ours(args, rank, world, local):
             t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
             keep.append(t)
             return t.numpy()
+        import ctypes as C
+        from softrender._lib import lib
         h_planes = [pinned(p) for p in scene.planes]
         h_idx = pinned(scene.indices)
         h_tex = pinned(scene.texture)
-        h_color = pinned(np.zeros((scene.height, scene.width), dtype=np.uint32))
-        h_depth = pinned(np.zeros((scene.height, scene.width), dtype=np.float32))
-        import ctypes as C
-        from softrender._lib import lib
+        pl2, mesh2, tex2 = sr.prepare_scene(scene)
+        stream2 = torch.cuda.Stream(device=dev)
+        pl2.set_stream(stream2.cuda_stream)
+        sets = []
+        for p_, m_, t_, s_ in ((pl, mesh, tex, stream), (pl2, mesh2, tex2, stream2)):
+            hc = pinned(np.zeros((scene.height, scene.width), dtype=np.uint32))
+            hd = pinned(np.zeros((scene.height, scene.width), dtype=np.float32))
+            sets.append((p_, m_, t_, s_, hc, hd))
         h2d = sum(p.nbytes for p in h_planes) + h_idx.nbytes + h_tex.nbytes
-        d2h = h_color.nbytes + h_depth.nbytes
-        e2e_steps = max(3, min(args.steps, 10))
-        times = []
-        for i in range(e2e_steps + 2):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            mesh.update(h_planes, h_idx, stream.cuda_stream)
-            tex.update(h_tex, stream.cuda_stream)
-            frame()
-            rc = lib().sr_framebuffer_read(pl.handle, h_color.ctypes.data, h_depth.ctypes.data, None)
-            dt = time.perf_counter() - t0
+        d2h = sets[0][4].nbytes + sets[0][5].nbytes
+
+        def e2e_step(i):
+            p_, m_, t_, s_, hc, hd = sets[i % 2]
+            st_ = p_.sync()                                  # its previous result is complete
+            if st_ != 0:
+                raise RuntimeError("e2e step failed: %d" % st_)
+            m_.update(h_planes, h_idx, s_.cuda_stream)
+            t_.update(h_tex, s_.cuda_stream)
+            p_.clear(clear)
+            sr.submit_scene(p_, m_, t_, scene)
+            rc = lib().sr_framebuffer_read_async(p_.handle, hc.ctypes.data, hd.ctypes.data, None)
             if rc != 0:
                 raise RuntimeError("e2e read failed: %d" % rc)
-            if i >= 2:
-                times.append(dt)
-        e2e_ms = float(np.mean(times)) * 1e3
+        for i in range(4):
+            e2e_step(i)
+        for st_ in sets:
+            st_[0].sync()
+        e2e_steps = max(6, min(args.steps, 20))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for i in range(e2e_steps):
+            e2e_step(i)
+        for st_ in sets:
+            if st_[0].sync() != 0:
+                raise RuntimeError("e2e final sync failed")
+        e2e_ms = (time.perf_counter() - t0) / e2e_steps * 1e3
+        pl2.destroy()
+        mesh2.free()
+        tex2.free()
         e2e = {"value": round(n_tris / (e2e_ms * 1e-3) / 1e6 * world, 3), "unit": "Mtris/s",
-               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4)}
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h), "ms_per_step": round(e2e_ms, 4),
+               "note": "two pipelines alternate so a step's copies overlap the next step's work"}
 
     pl.destroy()
     return dict(ms=ms, step_ms=step_ms, stats=stats, stage=stage, clocks=clk, e2e=e2e, scene=scene,
@@ -323,6 +351,51 @@ def run_batched():
             "launch_config": {"prims_per_warp": cfg[0], "big_threshold": cfg[1], "raster_ctas_per_sm": cfg[2]},
             "kernel_launches_per_batch": int(st["kernel_launches"]), "target0_equals_plain": same,
             "timing": "host wall clock per 256 draws incl. sync, best of repetitions"}
+
+
+def run_frames():
+    """The other frame workloads, device time per frame (CUDA events on the
+    pipeline's stream, median of a few frames after warm-up): the small plain
+    pipeline (icosphere 5,120 tris, 1024^2 RGBA f32 + f32 depth, Blinn-Phong)
+    and the ordering/tiny-triangle stress (16,777,216 tiny tris + 4,096 alpha
+    tris, 2048^2 RGBA8 + f32 depth + u8 stencil, over-blend, stencil
+    increment)."""
+    import torch
+    import softrender as sr
+    from softrender import _abi as A
+    from softrender import scenes
+    out = {}
+    for key, sc, n in (("icosphere_5120tri_1024x1024_rgba32f", scenes.icosphere_scene(1024, 1024), 20),
+                       ("stress_16777216tiny_4096alpha_2048x2048_stencil", scenes.stress_scene(), 3)):
+        pl, mesh, tex = sr.prepare_scene(sc)
+        stream = torch.cuda.Stream()
+        pl.set_stream(stream.cuda_stream)
+        clear = list(sc.clear_bytes()) if sc.color_format == A.SR_COLOR_RGBA8 else sc.clear_color
+        def frame():
+            pl.clear(clear)
+            sr.submit_scene(pl, mesh, tex, sc)
+        for _ in range(2):
+            frame()
+            if pl.sync() != 0:
+                raise RuntimeError("%s failed" % key)
+        ts = []
+        for _ in range(n):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            frame()
+            e1.record(stream)
+            pl.sync()
+            ts.append(e0.elapsed_time(e1))
+        ms = float(np.median(ts))
+        st = pl.stats()
+        out[key] = {"ms_per_frame": round(ms, 4), "mtris_per_s": round(sc.n_tris / ms / 1e3, 2),
+                    "gfrag_per_s": round(st["fragments"] / ms / 1e6, 3), "triangles": int(sc.n_tris),
+                    "fragments": int(st["fragments"]),
+                    "frame_algorithmic_bytes": int(sc.algorithmic_bytes()),
+                    "frame_roofline_gbs": round(sc.algorithmic_bytes() / ms / 1e6, 2)}
+        pl.destroy()
+        mesh.free()
+    return out
 
 
 def _timed(fn):
@@ -460,6 +533,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU baseline leg (profiling runs)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer leg (profiling runs)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-draws measurement")
+    ap.add_argument("--no-frames", action="store_true", help="skip the small and stress frame measurements")
     ap.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
     args = ap.parse_args()
     rank, world, local = dist_env()
@@ -508,6 +582,8 @@ def main():
             "gpu_launches": int(r["launches"]),
             "clocks": r["clocks"],
         }
+        if not args.no_frames:
+            line["other_frames"] = run_frames()
         if not args.no_batched:
             line["batched"] = run_batched()
         if not args.no_served:

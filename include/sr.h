@@ -194,6 +194,12 @@ SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color);
 /* PixelRead / UnsafeFramebuffer getters (src/pixels/mod.rs:46-77): copy planes
  * to host memory (any pointer may be NULL); synchronises the pipeline stream. */
 SR_API int sr_framebuffer_read(sr_pipeline* p, void* color, float* depth, uint8_t* stencil);
+/* Enqueues the same copies on the pipeline's stream after the draws enqueued
+ * so far and returns at once (no counterpart in the reference, whose reads are
+ * synchronous).  The host buffers (pinned for a truly asynchronous copy) hold
+ * the frame after the next sr_sync, which redoes the copies if it had to
+ * replay draws. */
+SR_API int sr_framebuffer_read_async(sr_pipeline* p, void* color, float* depth, uint8_t* stencil);
 /* PixelWrite / UnsafeFramebuffer setters: host planes -> device (NULL skips). */
 SR_API int sr_framebuffer_write(sr_pipeline* p, const void* color, const float* depth,
                                 const uint8_t* stencil);

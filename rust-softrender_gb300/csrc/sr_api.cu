@@ -594,9 +594,27 @@ extern "C" SR_API int sr_render(sr_pipeline* p, const sr_draw* d) {
     return rc;
 }
 
+namespace {
+int enqueue_read(sr_pipeline* p, void* color, float* depth, uint8_t* stencil) {
+    size_t n = (size_t)p->fb.width * p->fb.height;
+    if (color && p->color) SR_CK(cudaMemcpyAsync(color, p->color, n * bytes_per_color(p->fb.color_format), cudaMemcpyDeviceToHost, p->stream));
+    if (depth && p->depth) SR_CK(cudaMemcpyAsync(depth, p->depth, n * 4, cudaMemcpyDeviceToHost, p->stream));
+    if (stencil && p->stencil) SR_CK(cudaMemcpyAsync(stencil, p->stencil, n, cudaMemcpyDeviceToHost, p->stream));
+    return SR_OK;
+}
+}  // namespace
+
+extern "C" SR_API int sr_framebuffer_read_async(sr_pipeline* p, void* color, float* depth, uint8_t* stencil) {
+    if (!p) return SR_EINVAL;
+    const int rc = enqueue_read(p, color, depth, stencil);
+    if (rc == SR_OK && !p->pending.empty()) p->pending_reads.push_back({color, depth, stencil});
+    return rc;
+}
+
 extern "C" SR_API int sr_sync(sr_pipeline* p) {
     if (!p) return SR_EINVAL;
     int status = SR_OK;
+    bool replayed = false;
     for (int attempt = 0; attempt < 8; ++attempt) {
         SR_CK(cudaMemcpyAsync(p->hflags, p->flags, sizeof(DeviceFlags), cudaMemcpyDeviceToHost, p->stream));
         cudaError_t e = cudaStreamSynchronize(p->stream);
@@ -641,8 +659,16 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
             int rc = enqueue_draw(p, p->pending[i], i);
             if (rc != SR_OK) { status = rc; break; }
         }
+        replayed = true;
         if (status != SR_OK) break;
     }
+    // asynchronous reads copied a framebuffer that replayed draws changed
+    if (replayed)
+        for (const auto& r : p->pending_reads) {
+            const int rc = enqueue_read(p, r.color, r.depth, r.stencil);
+            if (rc != SR_OK && status == SR_OK) status = rc;
+        }
+    p->pending_reads.clear();
     p->pending.clear();
     DeviceFlags z;
     std::memset(&z, 0, sizeof(z));

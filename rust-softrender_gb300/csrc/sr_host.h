@@ -81,6 +81,8 @@ struct sr_pipeline {
     // capacities (elements) requested for the generated geometry
     uint64_t gen_tri_cap = 0, gen_vert_cap = 0, entry_cap = 0;
     std::vector<sr::PendingDraw> pending;
+    struct PendingRead { void* color; float* depth; uint8_t* stencil; };
+    std::vector<PendingRead> pending_reads;   // sr_framebuffer_read_async since the last sync
     sr_stats last_stats;
     bool stats_valid = false;
     bool force_unsafe = false;   // SR_FORCE_UNSAFE=1: every primitive takes the exact unsafe path

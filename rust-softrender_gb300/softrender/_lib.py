@@ -21,6 +21,7 @@ SIGNATURES = {
     "sr_pipeline_set_profiling": (C.c_int, [C.c_void_p, C.c_int]),
     "sr_framebuffer_clear": (C.c_int, [C.c_void_p, C.c_void_p]),
     "sr_framebuffer_read": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
+    "sr_framebuffer_read_async": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sr_framebuffer_write": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
     "sr_framebuffer_device_ptrs": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.POINTER(C.c_void_p),
                                              C.POINTER(C.c_void_p)]),

@@ -178,3 +178,24 @@ def test_dense_bins_depth_ties(built_lib, oracle_mod):
     z = sc.planes[2]
     z[:] = np.float32(0.25)
     check(sc, oracle_mod)
+
+
+def test_read_async_matches_read(built_lib):
+    """sr_framebuffer_read_async enqueues the copies; after sr_sync the host
+    buffers equal a synchronous read."""
+    import ctypes as C
+    import numpy as np
+    from softrender._lib import lib
+    sc = scenes.icosphere_scene(160, 120, color_format=A.SR_COLOR_RGBA8)
+    pl, mesh, tex = sr.prepare_scene(sc)
+    try:
+        sr.submit_scene(pl, mesh, tex, sc)
+        hc = np.zeros((sc.height, sc.width), np.uint32)
+        hd = np.zeros((sc.height, sc.width), np.float32)
+        assert lib().sr_framebuffer_read_async(pl.handle, hc.ctypes.data, hd.ctypes.data, None) == 0
+        assert pl.sync() == 0
+        c, d, _ = pl.read()
+        assert np.array_equal(hc, c) and np.array_equal(hd.view(np.uint32), d.view(np.uint32))
+    finally:
+        pl.destroy()
+        mesh.free()
