@@ -16,8 +16,10 @@
  *   - f32::min / f32::max: NaN-ignoring (fminf / fmaxf)
  *   - f32::powi: square-and-multiply, the algorithm of LLVM's __powisf2
  *   - `as u8`: truncate toward zero, saturate to [0,255], NaN -> 0
- * f32::powf is libm's in the reference; here it is sr_powf below (double-float
- * log2 + exp2, own implementation from the series stated in its comment).
+ * f32::powf is libm's in the reference; here it is sr_powf below (own
+ * implementation: table-driven double-float log2 and exp2, tables generated by
+ * rust-softrender_gb300/gen_pow_tables.py; measured within 0.51 ULP of the
+ * exact power).
  * Explicit fused multiply-adds (sr_fma) appear only inside these library
  * functions (pow, the byte -> unit conversion), which are defined here, not
  * restated from the reference.
@@ -183,12 +185,16 @@ SR_HD void sr_two_prod(float a, float b, float* p, float* e) {
 /* 2^n for integer n in [-126, 127] */
 SR_HD float sr_exp2i(int n) { return sr_u2f((uint32_t)(n + 127) << 23); }
 
+#include "sr_pow_tables.h"
+
 /*
- * log2(x) for finite x > 0, returned as a double-float hi + lo.
- * x = m * 2^e with m in [sqrt(1/2), sqrt(2)); ln(m) = 2*atanh(s), s = (m-1)/(m+1),
- * atanh(s) = s + s^3/3 + s^5/5 + ... (|s| <= 0.1716, truncated after s^13,
- * truncation error < 1e-12 relative).  The leading term 2s is carried as a
- * double-float (compensated division), the odd-power tail in single precision.
+ * log2(x) for finite x > 0, returned as a double-float hi + lo (table-driven).
+ * x = m * 2^e with m in [1, 2); i = the top 6 fraction bits of m selects
+ * INV[i] ~ 1/c_i (c_i the centre of m's 1/64-wide interval) and
+ * L[i] = -log2(INV[i]) (a float pair); r = m * INV[i] - 1 is formed exactly as
+ * a double-float (|r| < 2^-7) and ln(1 + r) = r + r^2 q(r) with
+ * q = -1/2 + r/3 - r^2/4 + r^3/5 - r^4/6 (truncation < 2^-52).
+ * log2(x) = e + L[i] + ln(1 + r) * log2(e).
  */
 SR_HD void sr_log2_df(float x, float* lhi, float* llo) {
     uint32_t bits = sr_f2u(x);
@@ -199,67 +205,70 @@ SR_HD void sr_log2_df(float x, float* lhi, float* llo) {
         e = (int)((bits >> 23) & 0xffu) - 23;
     }
     e -= 127;
-    float m = sr_u2f((bits & 0x007fffffu) | 0x3f800000u);  /* [1,2) */
-    if (m > 1.41421353816986083984375f) { m = m * 0.5f; e += 1; }
-    float f = m - 1.0f;               /* exact (Sterbenz) */
-    float dh, dl;
-    sr_two_sum(m, 1.0f, &dh, &dl);    /* m + 1 as double-float */
-    float sh = f / dh;
+    const float m = sr_u2f((bits & 0x007fffffu) | 0x3f800000u);  /* [1,2) */
+    const int i = (int)((bits >> 17) & 63u);
+    const float inv = SR_TAB(SR_LOG2_INV, i);
     float ph, pl;
-    sr_two_prod(sh, dh, &ph, &pl);
-    float r = ((f - ph) - pl) - sh * dl;
-    float sl = r / dh;
-    float s2 = sh * sh;
-    float poly = 0.1538461538461538f;                 /* 2/13 */
-    poly = sr_fma(s2, poly, 0.1818181818181818f);     /* 2/11 */
-    poly = sr_fma(s2, poly, 0.2222222222222222f);     /* 2/9  */
-    poly = sr_fma(s2, poly, 0.2857142857142857f);     /* 2/7  */
-    poly = sr_fma(s2, poly, 0.4f);                    /* 2/5  */
-    poly = sr_fma(s2, poly, 0.6666666666666666f);     /* 2/3  */
-    float tail = (sh * s2) * poly;
-    float ln_h, ln_l;
-    sr_fast_two_sum(2.0f * sh, 2.0f * sl + tail, &ln_h, &ln_l);
-    /* multiply by log2(e) = LOG2E_HI + LOG2E_LO */
+    sr_two_prod(m, inv, &ph, &pl);    /* m * inv exactly */
+    float rh, rl;
+    sr_two_sum(ph - 1.0f, pl, &rh, &rl);   /* ph - 1 is exact (|ph - 1| < 2^-6) */
+    float q = -0.16666666666666666f;                  /* -1/6 */
+    q = sr_fma(rh, q, 0.2f);                          /*  1/5 */
+    q = sr_fma(rh, q, -0.25f);                        /* -1/4 */
+    q = sr_fma(rh, q, 0.33333333333333333f);          /*  1/3 */
+    q = sr_fma(rh, q, -0.5f);                         /* -1/2 */
+    const float tail = sr_fma(rh * rh, q, rl);
+    float lnh, lnl;
+    sr_fast_two_sum(rh, tail, &lnh, &lnl);
+    /* ln -> log2: multiply by log2(e) = LOG2E_HI + LOG2E_LO */
     const float LOG2E_HI = 0x1.715476p+0f;
     const float LOG2E_LO = 0x1.4ae0cp-26f;
     float qh, ql;
-    sr_two_prod(ln_h, LOG2E_HI, &qh, &ql);
-    ql = ql + (ln_h * LOG2E_LO + ln_l * LOG2E_HI);
+    sr_two_prod(lnh, LOG2E_HI, &qh, &ql);
+    ql = ql + (lnh * LOG2E_LO + lnl * LOG2E_HI);
+    /* + e + L[i] */
+    float sh, sl;
+    sr_two_sum((float)e, SR_TAB(SR_LOG2_HI, i), &sh, &sl);
+    sl = sl + SR_TAB(SR_LOG2_LO, i);
     float th, tl;
-    sr_two_sum((float)e, qh, &th, &tl);
-    tl = tl + ql;
+    sr_two_sum(sh, qh, &th, &tl);
+    tl = tl + (sl + ql);
     sr_fast_two_sum(th, tl, lhi, llo);
 }
 
 /*
- * 2^(th + tl) for a double-float exponent.  n = rint(th), f = (th - n) + tl,
- * r = f*ln2 (double-float), e^r by its Taylor series to r^8 (|r| <= 0.35,
- * truncation < 2e-9 relative), then an exact scale by 2^n.
+ * 2^(th + tl) for a double-float exponent (table-driven).  n = rint(th),
+ * f = (th - n) + tl kept as a double-float, j = rint(64 f),
+ * g = f - j/64 (|g| <= 1/128, exact); 2^f = T[j] * e^(g ln 2) with T[j] =
+ * 2^(j/64) (a float pair) and e^x = 1 + x + x^2 (1/2 + x/6 + x^2/24 +
+ * x^3/120) (truncation < 2^-52); then an exact scale by 2^n.
  */
 SR_HD float sr_exp2_df(float th, float tl) {
     if (sr_isnan(th)) return th;
     if (th >= 128.0f) return sr_u2f(0x7f800000u);
     if (th < -151.0f) return 0.0f;
-    float n = sr_rint(th);
-    float f = (th - n) + tl;
+    const float n = sr_rint(th);
+    float fh, fl;
+    sr_two_sum(th - n, tl, &fh, &fl);                 /* th - n is exact */
+    const float jf = sr_rint(fh * 64.0f);
+    const int j = (int)jf;
+    const float gh = fh - jf * 0.015625f;             /* exact: |gh| <= 1/128 + ulp */
     const float LN2_HI = 0x1.62e43p-1f;
     const float LN2_LO = -0x1.05c61p-29f;
-    float rh, rl;
-    sr_two_prod(f, LN2_HI, &rh, &rl);
-    rl = rl + f * LN2_LO;
-    float p = 2.4801587301587302e-05f;                /* 1/8! */
-    p = sr_fma(rh, p, 1.9841269841269841e-04f);       /* 1/7! */
-    p = sr_fma(rh, p, 1.3888888888888889e-03f);       /* 1/6! */
-    p = sr_fma(rh, p, 8.3333333333333332e-03f);       /* 1/5! */
-    p = sr_fma(rh, p, 4.1666666666666664e-02f);       /* 1/4! */
-    p = sr_fma(rh, p, 1.6666666666666666e-01f);       /* 1/3! */
-    p = sr_fma(rh, p, 0.5f);                          /* 1/2! */
-    p = (rh * rh) * p;
-    float res = 1.0f + (rh + (rl + p));
-    int ni = (int)n;
+    float xh, xl;
+    sr_two_prod(gh, LN2_HI, &xh, &xl);
+    xl = xl + (gh * LN2_LO + fl * LN2_HI);
+    float p = 8.3333333333333332e-03f;                /* 1/5! */
+    p = sr_fma(xh, p, 4.1666666666666664e-02f);       /* 1/4! */
+    p = sr_fma(xh, p, 1.6666666666666666e-01f);       /* 1/3! */
+    p = sr_fma(xh, p, 0.5f);                          /* 1/2! */
+    const float ex = xh + sr_fma(xh * xh, p, xl);     /* e^x - 1 */
+    const float t_hi = SR_TAB(SR_EXP2_HI, j + 32), t_lo = SR_TAB(SR_EXP2_LO, j + 32);
+    const float res = t_hi + sr_fma(t_hi, ex, t_lo);
+    const int ni = (int)n;
     if (ni >= -126 && ni <= 127) return res * sr_exp2i(ni);
-    int n1 = ni / 2;
-    int n2 = ni - n1;
+    const int n1 = ni / 2;
+    const int n2 = ni - n1;
     return (res * sr_exp2i(n1)) * sr_exp2i(n2);
 }
 
