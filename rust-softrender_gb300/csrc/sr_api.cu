@@ -187,6 +187,8 @@ extern "C" SR_API int sr_pipeline_destroy(sr_pipeline* p) {
     p->st_diff.release(); p->st_lines.release(); p->st_glob.release();
     p->area.release(); p->big_list.release(); p->gkeys.release(); p->bitmap.release();
     p->lpv.release(); p->lpvalid.release();
+    p->pcount.release(); p->poff.release(); p->pkeys0.release(); p->pkeys1.release(); p->pvals0.release();
+    p->pvals1.release(); p->hist.release(); p->hist_off.release(); p->ranges.release();
     for (auto& e : p->ev) if (e) cudaEventDestroy(e);
     if (p->own_stream) cudaStreamDestroy(p->own_stream);
     delete p;
@@ -493,10 +495,21 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
             return rc;
     }
     if ((rc = p->setup.ensure(4 * n_raster_cap)) || (rc = p->binrect.ensure(n_raster_cap)) ||
-        (rc = p->bin_counts.ensure(n_bins)) || (rc = p->bin_off.ensure((size_t)n_bins + 1)) ||
-        (rc = p->bin_cursor.ensure(n_bins)) || (rc = p->bin_tmp.ensure(scan_blocks(n_bins) + 2)) ||
-        (rc = p->entries.ensure(p->entry_cap)) || (rc = p->unsafe_list.ensure(n_raster_cap)))
+        (rc = p->unsafe_list.ensure(n_raster_cap)))
         return rc;
+    BinBuffers B{};
+    if (ordered && !P.mode_b) {
+        const size_t nblk = radix_blocks(p->entry_cap);
+        const size_t tmp = std::max(scan_blocks(n_raster_cap + 1), scan_blocks(256 * nblk)) + 2;
+        if ((rc = p->pcount.ensure(n_raster_cap + 1)) || (rc = p->poff.ensure(n_raster_cap + 1)) ||
+            (rc = p->pkeys0.ensure(p->entry_cap)) || (rc = p->pkeys1.ensure(p->entry_cap)) ||
+            (rc = p->pvals0.ensure(p->entry_cap)) || (rc = p->pvals1.ensure(p->entry_cap)) ||
+            (rc = p->hist.ensure(256 * nblk)) || (rc = p->hist_off.ensure(256 * nblk)) ||
+            (rc = p->ranges.ensure(2 * (size_t)n_bins)) || (rc = p->bin_tmp.ensure(tmp)))
+            return rc;
+        B = BinBuffers{p->pcount.p, p->poff.p, p->bin_tmp.p, {p->pkeys0.p, p->pkeys1.p}, {p->pvals0.p, p->pvals1.p},
+                       p->hist.p, p->hist_off.p, p->ranges.p, p->entry_cap};
+    }
     if (!ordered) {
         const size_t npx = (size_t)W * H;
         const size_t nblk = (size_t)((W + 31) / 32) * ((H + 31) / 32);
@@ -535,15 +548,21 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
         launches += 5;
     }
     if (ev) cudaEventRecord(ev[2], st);
-    launch_setup_bin(P, vidx, vs, p->setup.p, reinterpret_cast<uint32_t*>(p->binrect.p), p->bin_counts.p, p->bin_off.p,
-                     p->bin_cursor.p, p->entries.p, p->bin_tmp.p, p->unsafe_list.p, ordered ? nullptr : p->area.p, S,
-                     p->flags, st);
-    launches += !ordered ? 1 : (P.mode_b ? 6 : 8);
+    launch_setup_bin(P, vidx, vs, p->setup.p, reinterpret_cast<uint32_t*>(p->binrect.p), nullptr, nullptr,
+                     nullptr, nullptr, nullptr, p->unsafe_list.p, ordered ? nullptr : p->area.p, S, p->flags, st);
+    launches += 1;
+    const uint32_t* bin_list = nullptr;
+    if (ordered && !P.mode_b) {
+        bin_list = launch_bins(P, p->binrect.p, p->setup.p, p->unsafe_list.p, B, p->flags, st);
+        uint32_t bits = 1;
+        while ((1ull << bits) < n_bins) ++bits;
+        launches += 7 + 2 * ((bits + 7) / 8) + 3;   // counts, scan, check, emits, radix passes, ranges
+    }
     if (ev) cudaEventRecord(ev[3], st);
     const uint32_t* tex = d->texture ? d->texture->data : nullptr;
     if (ordered) {
-        launch_ordered(P, pd.U, p->setup.p, p->bin_off.p, p->entries.p, vidx, p->vary.p, tex, p->color, p->depth,
-                       p->stencil, gate, p->flags, st);
+        launch_ordered(P, pd.U, p->setup.p, P.mode_b ? nullptr : p->ranges.p, bin_list, vidx, p->vary.p, tex, p->color,
+                       p->depth, p->stencil, gate, p->flags, st);
         launches += 1;
     } else {
         OpaqueArgs A{p->setup.p, p->area.p, p->big_list.p, p->gkeys.p, p->bitmap.p, p->unsafe_list.p,

@@ -75,6 +75,7 @@ struct sr_pipeline {
     sr::DevBuf<uint32_t> big_list;
     sr::DevBuf<uint32_t> bitmap;
     sr::DevBuf<int> st_diff, st_lines;
+    sr::DevBuf<uint32_t> pcount, poff, pkeys0, pkeys1, pvals0, pvals1, hist, hist_off, ranges;   // ordered bins
     sr::DevBuf<float4> lpv;           // line / point vertices (4 x float4 each)
     sr::DevBuf<uint8_t> lpvalid;      // per line / point: kept by the geometry stage
     sr::DevBuf<unsigned long long> st_glob;

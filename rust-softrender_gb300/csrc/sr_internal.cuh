@@ -286,6 +286,24 @@ struct OpaqueArgs {
 };
 // Opaque draws (sr_opaque.cu); returns the number of kernels launched.
 int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A, cudaStream_t st);
+// Bin lists of the ordered path (sr_bins.cu): pairs counted per primitive,
+// written in primitive order and stably radix-sorted by bin.
+struct BinBuffers {
+    uint32_t* pcount;       // n + 1 pair counts
+    uint32_t* poff;         // n + 1 exclusive offsets (poff[n] = pairs)
+    uint32_t* scan_tmp;     // scratch of the scans
+    uint32_t* keys[2];      // bin ids (ping-pong), capacity cap
+    uint32_t* vals[2];      // primitive ids (ping-pong), capacity cap
+    uint32_t* hist;         // 256 x radix_blocks(cap)
+    uint32_t* hist_off;     // its exclusive scan
+    uint32_t* ranges;       // [begin, end) per bin
+    uint64_t cap;           // pair capacity
+};
+uint32_t radix_blocks(uint64_t cap);
+// Returns the sorted primitive list (one of vals[]).
+uint32_t* launch_bins(const DrawParams& P, const uint2* binrect, const float4* setup, const uint32_t* unsafe_list,
+                      const BinBuffers& B, DeviceFlags* flags, cudaStream_t st);
+
 // Lines and points (sr_lp.cu).  An LP vertex is 64 bytes: screen position
 // and 12 varyings.
 struct LPV;

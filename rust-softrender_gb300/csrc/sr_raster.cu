@@ -13,7 +13,7 @@
 // Opaque draws take the order-independent path of sr_opaque.cu.
 //
 // raster_ordered_kernel (blending, stencil-gated draws): one thread per pixel
-// walks the bin's primitives in submission order (sorted in shared memory),
+// walks the bin's primitives in submission order (sorted lists, sr_bins.cu),
 // once per semantic tile containing the pixel, applying the reference's
 // sequence literally.
 #include "sr_internal.cuh"
@@ -63,7 +63,6 @@ __device__ __forceinline__ void store_color(void* color, size_t idx, sr_v4 c) {
 // ---------------------------------------------------------------- ordered
 constexpr int ORD_THREADS = 256;      // 16 x 16 bin, one pixel per thread
 constexpr int ORD_CHUNK = 128;        // setup records staged per step
-constexpr int SORT_CAP = 16384;       // bin entries sortable in shared memory
 
 template <int FMT>
 struct PixelColor;
@@ -71,50 +70,31 @@ template <> struct PixelColor<SR_COLOR_RGBA32F> { float4 v; };
 template <> struct PixelColor<SR_COLOR_RGBA8> { uint32_t v; };
 template <> struct PixelColor<SR_COLOR_NONE> { uint32_t v; };
 
-// Bitonic sort of n (power of two) keys in shared memory.
-__device__ void block_bitonic_sort(uint32_t* a, uint32_t n) {
-    for (uint32_t k = 2; k <= n; k <<= 1) {
-        for (uint32_t j = k >> 1; j > 0; j >>= 1) {
-            for (uint32_t i = threadIdx.x; i < n; i += blockDim.x) {
-                uint32_t l = i ^ j;
-                if (l > i) {
-                    uint32_t x = a[i], y = a[l];
-                    bool up = (i & k) == 0;
-                    if ((x > y) == up) { a[i] = y; a[l] = x; }
-                }
-            }
-            __syncthreads();
-        }
-    }
-}
-
 template <int FS, int FMT, int BLEND>
 __global__ void __launch_bounds__(ORD_THREADS) raster_ordered_kernel(
     DrawParams P, sr_uniforms U, const float4* __restrict__ setup, const uint32_t* __restrict__ bin_off,
     const uint32_t* __restrict__ entries, const uint32_t* __restrict__ vidx, const float* __restrict__ vary,
     const uint32_t* __restrict__ tex, void* __restrict__ color, float* __restrict__ depth, uint8_t* __restrict__ stencil,
     uint32_t gate_with_stencil, DeviceFlags* flags) {
-    extern __shared__ uint32_t list[];              // sorted bin entries (not used in mode B)
     __shared__ float4 rec[ORD_CHUNK][3];
     __shared__ int4 rbb[ORD_CHUNK];
     __shared__ uint32_t rtri[ORD_CHUNK];
+    // per chunk: for each pixel of the bin the chunk entries whose bbox holds
+    // it (entries with small bin rectangles), and the entries every pixel
+    // tests (larger rectangles, unsafe primitives, exhaustive mode)
+    __shared__ uint32_t pmask[ORD_THREADS][ORD_CHUNK / 32];
+    __shared__ uint32_t lmask[ORD_CHUNK / 32];
+    // the chunk entries' vertex varyings, staged once per chunk
+    constexpr int NKQ = FsTraits<FS>::NK > 0 ? (FsTraits<FS>::NK + 3) / 4 : 1;
+    __shared__ float4 svary[FsTraits<FS>::NK > 0 ? ORD_CHUNK : 1][3][NKQ];
     if (flags->poison) return;
     const uint32_t bin = blockIdx.x;
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
     uint32_t beg = 0, cnt = N;
-    if (!P.mode_b) {
-        beg = bin_off[bin];
-        cnt = bin_off[bin + 1] - beg;
+    if (!P.mode_b) {   // the bin's primitives, sorted in submission order (sr_bins.cu)
+        beg = bin_off[2 * (size_t)bin];
+        cnt = bin_off[2 * (size_t)bin + 1] - beg;
         if (cnt == 0) return;
-        if (cnt > (uint32_t)SORT_CAP) {
-            if (threadIdx.x == 0) { atomicOr(&flags->overflow_bits, (unsigned)OVF_SORT); atomicOr(&flags->poison, 1u); atomicMin(&flags->poison_draw, P.draw_id); }
-            return;
-        }
-        uint32_t n2 = 1;
-        while (n2 < cnt) n2 <<= 1;
-        for (uint32_t i = threadIdx.x; i < n2; i += ORD_THREADS) list[i] = i < cnt ? entries[beg + i] : 0xffffffffu;
-        __syncthreads();
-        block_bitonic_sort(list, n2);
     }
     const uint32_t bx = bin % P.bins_x, by = bin / P.bins_x;
     const uint32_t BW = 1u << P.bin_w_log2, BH = 1u << P.bin_h_log2;
@@ -144,12 +124,15 @@ __global__ void __launch_bounds__(ORD_THREADS) raster_ordered_kernel(
         const int ri = my_pass ? pass / cs.count : 0, ci = my_pass ? pass % cs.count : 0;
         for (uint32_t cb = 0; cb < cnt; cb += ORD_CHUNK) {
             uint32_t m = min((uint32_t)ORD_CHUNK, cnt - cb);
+#pragma unroll
+            for (int w = 0; w < ORD_CHUNK / 32; ++w) pmask[threadIdx.x][w] = 0;   // this pixel's previous chunk is done
+            if (threadIdx.x < ORD_CHUNK / 32) lmask[threadIdx.x] = 0;
             __syncthreads();
             if (threadIdx.x < m) {
                 uint32_t j = cb + threadIdx.x;
-                uint32_t t = P.mode_b ? j : list[j];
+                uint32_t t = P.mode_b ? j : __ldg(entries + beg + j);
                 // the extension pass may list a primitive twice in a bin
-                bool dup = !P.mode_b && j > 0 && list[j - 1] == t;
+                bool dup = !P.mode_b && j > 0 && __ldg(entries + beg + j - 1) == t;
                 const float4* r = setup + 4 * (size_t)t;
                 rec[threadIdx.x][0] = __ldg(r);
                 rec[threadIdx.x][1] = __ldg(r + 1);
@@ -159,10 +142,38 @@ __global__ void __launch_bounds__(ORD_THREADS) raster_ordered_kernel(
                 rbb[threadIdx.x] = make_int4(__float_as_int(r3.x), __float_as_int(r3.y), __float_as_int(r3.z),
                                              __float_as_int(r3.w));
                 rtri[threadIdx.x] = t;
+                const uint32_t fl = __float_as_uint(r2.z);
+                if (FsTraits<FS>::NK > 0 && (fl & REC_RASTER)) {
+#pragma unroll
+                    for (int vq = 0; vq < 3; ++vq) {
+                        const uint32_t slot = __ldg(vidx + 3 * (size_t)t + vq);
+                        const float4* kq = reinterpret_cast<const float4*>(vary + (size_t)slot * VSTRIDE);
+#pragma unroll
+                        for (int q = 0; q < NKQ; ++q) svary[threadIdx.x][vq][q] = __ldg(kq + q);
+                    }
+                }
+                if (fl & REC_RASTER) {
+                    const uint32_t bit = 1u << (threadIdx.x & 31), wi = threadIdx.x >> 5;
+                    const int bx0 = (int)(bx * BW), by0 = (int)(by * BH);
+                    const int x0 = max(__float_as_int(r3.x), bx0), x1 = min(__float_as_int(r3.z), bx0 + (int)BW - 1);
+                    const int y0 = max(__float_as_int(r3.y), by0), y1 = min(__float_as_int(r3.w), by0 + (int)BH - 1);
+                    if (P.mode_b || (fl & REC_UNSAFE) || (x1 - x0 + 1) * (y1 - y0 + 1) > 16) {
+                        atomicOr(&lmask[wi], bit);
+                    } else if (x0 <= x1 && y0 <= y1) {
+                        for (int yy = y0; yy <= y1; ++yy)
+                            for (int xx = x0; xx <= x1; ++xx)
+                                atomicOr(&pmask[((yy - by0) << P.bin_w_log2) + (xx - bx0)][wi], bit);
+                    }
+                }
             }
             __syncthreads();
             if (!my_pass) continue;
-            for (uint32_t e = 0; e < m; ++e) {
+            uint32_t mk[ORD_CHUNK / 32];
+#pragma unroll
+            for (int w = 0; w < ORD_CHUNK / 32; ++w) mk[w] = pmask[threadIdx.x][w] | lmask[w];
+            for (int w = 0; w < ORD_CHUNK / 32; ++w) while (mk[w]) {
+                const uint32_t e = (uint32_t)w * 32 + (uint32_t)(__ffs(mk[w]) - 1);
+                mk[w] &= mk[w] - 1;
                 float4 r2 = rec[e][2];
                 uint32_t fl = __float_as_uint(r2.z);
                 if (!(fl & REC_RASTER)) continue;
@@ -186,13 +197,18 @@ __global__ void __launch_bounds__(ORD_THREADS) raster_ordered_kernel(
                 if (!b.covered || !(b.z < 0.0f)) continue;
                 if (pass == kp - 1) ++frags;
                 if (P.has_depth && !(b.z >= d)) continue;
-                uint32_t t = rtri[e];
                 constexpr int NK = FsTraits<FS>::NK;
                 float kv[NK > 0 ? ((NK + 3) / 4) * 4 : 4];
                 if (NK > 0) {
-                    uint32_t a = __ldg(vidx + 3 * (size_t)t), bq = __ldg(vidx + 3 * (size_t)t + 1),
-                             c = __ldg(vidx + 3 * (size_t)t + 2);
-                    interp_varyings<NK>(vary, a, bq, c, b.u, b.v, b.w, kv);
+                    // (ka*u + kb*v) + kc*w, interpolate.rs:43-52
+#pragma unroll
+                    for (int q = 0; q < NKQ; ++q) {
+                        const float4 xa = svary[e][0][q], xb = svary[e][1][q], xc = svary[e][2][q];
+                        kv[4 * q + 0] = (xa.x * b.u + xb.x * b.v) + xc.x * b.w;
+                        kv[4 * q + 1] = (xa.y * b.u + xb.y * b.v) + xc.y * b.w;
+                        kv[4 * q + 2] = (xa.z * b.u + xb.z * b.v) + xc.z * b.w;
+                        kv[4 * q + 3] = (xa.w * b.u + xb.w * b.v) + xc.w * b.w;
+                    }
                 }
                 sr_v4 col = shade_fs<FS>(U, kv, tex, P);
                 if (FMT == SR_COLOR_RGBA32F) {
@@ -224,14 +240,7 @@ static void launch_ordered_t(const DrawParams& P, const sr_uniforms& U, const fl
                              void* color, float* depth, uint8_t* stencil, uint32_t gate, DeviceFlags* flags,
                              cudaStream_t st) {
     uint32_t nb = P.bins_x * P.bins_y;
-    size_t smem = P.mode_b ? 16 : (size_t)SORT_CAP * 4;
-    static bool configured = false;
-    if (!configured) {
-        cudaFuncSetAttribute(raster_ordered_kernel<FS, FMT, BLEND>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             SORT_CAP * 4);
-        configured = true;
-    }
-    raster_ordered_kernel<FS, FMT, BLEND><<<nb, ORD_THREADS, smem, st>>>(P, U, setup, bin_off, entries, vidx, vary,
+    raster_ordered_kernel<FS, FMT, BLEND><<<nb, ORD_THREADS, 0, st>>>(P, U, setup, bin_off, entries, vidx, vary,
                                                                           tex, color, depth, stencil, gate, flags);
 }
 

@@ -5,6 +5,79 @@
 
 namespace sr {
 
+constexpr uint32_t RECT_EMPTY = 0xffffffffu;   // binrect of a primitive with no regular bins
+
+// ------------------------------------------------------- extension pass
+// An unsafe primitive can produce fragments outside its bbox, but only at
+// the pixels where the reference evaluates it there: the projection of its
+// bbox onto each semantic tile it does not overlap (a column segment, a row
+// segment or a corner pixel on that tile's edge).  For each such segment a
+// sound sign test clears the whole segment when one of u, v, w is certainly
+// negative on it; remaining pixels are evaluated exactly (the reference's
+// expressions), and the primitive is added to the bin of every pixel that
+// yields a fragment, unless that bin already lists it.
+//
+// Sign test: the reference's numerator n_u(P) differs from the exact edge
+// function N_u(P) by at most gamma_4 * S_u(P), S_u = |y2-y3||x-x3| + |x3-x2||y-y3|
+// (convex on the segment, so its maximum is at an end point).  N_u is affine,
+// so s*n_u(end) + 2 gamma_4 max S_u < 0 at both ends (s = sign of the computed
+// det) makes u < 0 on the whole segment; v likewise.  For w = (1-u)-v the
+// quantity det - N_u - N_v is affine and w < 0 follows when it is negative
+// beyond the numerator errors plus 8 eps |det| (the roundings of the two
+// quotients and two subtractions while u, v lie in [0, 2]; outside that range
+// u < 0, v < 0 or w < 0 holds anyway).
+__device__ __forceinline__ uint32_t clampu(int v, uint32_t lo, uint32_t hi) {
+    return v < (int)lo ? lo : (v > (int)hi ? hi : (uint32_t)v);
+}
+
+// The extension bins of unsafe primitive t (one warp; lane strides over the
+// semantic tiles): for every tile its bbox misses, the clamped tile-edge
+// segment (triangle.rs:66-78) is skipped when the sound sign test clears it,
+// otherwise its pixels are evaluated exactly and every bin holding a
+// fragment outside the regular bin rectangle is reported through emit(bin)
+// (consecutive repeats of a bin within a segment collapse).
+template <class Emit>
+__device__ __forceinline__ void ext_bins(const DrawParams& P, const float4* __restrict__ setup, uint2 br, uint32_t t,
+                                         uint32_t lane, Emit emit) {
+    const uint32_t ntiles = P.ncols * P.nrows;
+    const float4* r = setup + 4 * (size_t)t;
+    const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+    const int ix0 = __float_as_int(r3.x), iy0 = __float_as_int(r3.y);
+    const int ix1 = __float_as_int(r3.z), iy1 = __float_as_int(r3.w);
+    const bool has_rect = br.x != RECT_EMPTY;
+    const uint32_t bx0 = br.x & 0xffffu, by0 = br.x >> 16, bx1 = br.y & 0xffffu, by1 = br.y >> 16;
+    for (uint32_t ti = lane; ti < ntiles; ti += 32) {
+        const uint32_t C = ti % P.ncols, R = ti / P.ncols;
+        const uint32_t lx = C * P.tile_w, hx = min((C + 1) * P.tile_w, P.W - 1);
+        const uint32_t ly = R * P.tile_h, hy = min((R + 1) * P.tile_h, P.H - 1);
+        const bool ox = ix1 >= (int)lx && ix0 <= (int)hx;
+        const bool oy = iy1 >= (int)ly && iy0 <= (int)hy;
+        if (ox && oy) continue;   // bbox meets the tile: those pixels lie in the bbox bins
+        const uint32_t cx0 = clampu(ix0, lx, hx), cx1 = clampu(ix1, lx, hx);
+        const uint32_t cy0 = clampu(iy0, ly, hy), cy1 = clampu(iy1, ly, hy);
+        if (segment_cleared(r0, r1, cx0, cy0, cx1, cy1)) continue;
+        uint32_t last_b = 0xffffffffu;
+        for (uint32_t py = cy0; py <= cy1; ++py) {
+            for (uint32_t px = cx0; px <= cx1; ++px) {
+                const float x = (float)px + 0.5f, y = (float)py + 0.5f;
+                const float dx = x - r1.x, dy = y - r1.y;
+                const float u = (r0.x * dx + r0.y * dy) / r1.z;
+                const float v = (r0.z * dx + r0.w * dy) / r1.z;
+                const float w = 1.0f - u - v;
+                if (u < 0.0f || v < 0.0f || w < 0.0f) continue;
+                const float z = (r1.w * u + r2.x * v) + r2.y * w;
+                if (!(z < 0.0f)) continue;
+                const uint32_t bxx = px >> P.bin_w_log2, byy = py >> P.bin_h_log2;
+                if (has_rect && bxx >= bx0 && bxx <= bx1 && byy >= by0 && byy <= by1) continue;
+                const uint32_t b = byy * P.bins_x + bxx;
+                if (b == last_b) continue;
+                last_b = b;
+                emit(b);
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ void tri_slots(uint32_t t, const uint32_t* __restrict__ vidx, uint32_t& a, uint32_t& b,
                                           uint32_t& c) {
     a = __ldg(vidx + 3 * (size_t)t);
