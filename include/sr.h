@@ -103,7 +103,10 @@ typedef enum sr_stage {
 
 /* Sampling for the textured shaders (src/texture.rs:14-18,89-113). */
 typedef enum sr_filter { SR_SAMPLE_NEAREST = 0, SR_SAMPLE_BILINEAR = 1 } sr_filter;
-typedef enum sr_edge { SR_SAMPLE_CLAMP = 0, SR_SAMPLE_WRAP = 1 } sr_edge;
+/* Clamp: coordinates clamped to [0, 1]; wrap: fractional part; border:
+ * outside [0, 1] reads transparent black (the reference's TextureRead::sample
+ * is unimplemented, src/texture.rs:14-53). */
+typedef enum sr_edge { SR_SAMPLE_CLAMP = 0, SR_SAMPLE_WRAP = 1, SR_SAMPLE_BORDER = 2 } sr_edge;
 
 /* --------------------------------------------------------------- structs */
 
@@ -231,6 +234,12 @@ SR_API int sr_texture_upload(const uint32_t* rgba8, uint32_t width, uint32_t hei
  * `stream` (NULL: synchronous). */
 SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, uint32_t width, uint32_t height, void* stream);
 SR_API int sr_texture_free(sr_texture* t);
+/* Render to texture: copies an RGBA8 framebuffer's colour plane into a
+ * texture of the same size, ordered on the pipeline's stream after its draws
+ * (sr_sync the pipeline before draws on other pipelines sample it).  The
+ * reference's texture-buffer framebuffers (src/framebuffer/texturebuffer.rs)
+ * serve the same purpose. */
+SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t);
 
 /* Shader registry: device functions compiled into the library, looked up by
  * name.  Stage is sr_stage.  Names: vertex "mvp_pos_nrm", "mvp_pos_nrm_uv",

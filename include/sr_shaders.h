@@ -379,7 +379,7 @@ SR_HD float sr_aces_component(float x) {
  * clamped to the last texel, and x, y to [0, W-1] / [0, H-1].
  */
 enum { SR_FILTER_NEAREST = 0, SR_FILTER_BILINEAR = 1 };
-enum { SR_EDGE_CLAMP = 0, SR_EDGE_WRAP = 1 };
+enum { SR_EDGE_CLAMP = 0, SR_EDGE_WRAP = 1, SR_EDGE_BORDER = 2 };
 
 SR_HD float sr_fract(float v) {  /* Rust f32::fract: v - trunc(v) */
     return v - truncf(v);
@@ -398,6 +398,12 @@ SR_HD sr_v4 sr_texel(const uint32_t* tex, uint32_t w, uint32_t x, uint32_t y) {
 }
 SR_HD sr_v4 sr_sample_rgba8(const uint32_t* tex, uint32_t w, uint32_t h, float u, float v,
                             int filter, int edge) {
+    /* Border: coordinates outside [0, 1] (or NaN) read the border colour,
+     * transparent black; inside, sampling is as with clamp. */
+    if (edge == SR_EDGE_BORDER) {
+        if (!(u >= 0.0f && u <= 1.0f && v >= 0.0f && v <= 1.0f)) return sr_make_v4(0.0f, 0.0f, 0.0f, 0.0f);
+        edge = SR_EDGE_CLAMP;
+    }
     if (edge == SR_EDGE_CLAMP) {
         u = sr_max(sr_min(u, 1.0f), 0.0f);
         v = sr_max(sr_min(v, 1.0f), 0.0f);

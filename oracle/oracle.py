@@ -116,7 +116,9 @@ def framebuffer_for(scene):
 
 
 def _draw(scene, keep):
-    planes = [np.ascontiguousarray(p, dtype=np.float32) for p in scene.planes]
+    planes = [np.ascontiguousarray(p, dtype=np.float32).reshape(-1) for p in scene.planes]
+    if any(p.shape[0] != planes[0].shape[0] for p in planes):
+        raise ValueError("every attribute plane must hold one value per vertex")
     keep += planes
     parr = (C.POINTER(C.c_float) * len(planes))(*[p.ctypes.data_as(C.POINTER(C.c_float)) for p in planes])
     keep.append(parr)

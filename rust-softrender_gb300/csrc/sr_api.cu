@@ -369,6 +369,13 @@ extern "C" SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, ui
     return SR_OK;
 }
 
+extern "C" SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t) {
+    if (!p || !t || p->fb.color_format != SR_COLOR_RGBA8 || !p->color) return SR_EINVAL;
+    if (t->w != p->fb.width || t->h != p->fb.height) return SR_EINVAL;
+    SR_CK(cudaMemcpyAsync(t->data, p->color, (size_t)t->w * t->h * 4, cudaMemcpyDeviceToDevice, p->stream));
+    return SR_OK;
+}
+
 extern "C" SR_API int sr_texture_free(sr_texture* t) {
     if (!t) return SR_EINVAL;
     if (t->data) cudaFree(t->data);

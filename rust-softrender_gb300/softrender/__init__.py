@@ -69,9 +69,11 @@ class Mesh:
     """Mesh<V> (src/mesh.rs:38-64) uploaded as SoA f32 planes + u32 indices."""
 
     def __init__(self, planes, indices):
-        planes = [np.ascontiguousarray(p, dtype=np.float32) for p in planes]
+        planes = [np.ascontiguousarray(p, dtype=np.float32).reshape(-1) for p in planes]
         idx = np.ascontiguousarray(indices, dtype=np.uint32)
         n = planes[0].shape[0] if planes else 0
+        if any(p.shape[0] != n for p in planes):
+            raise ValueError("every attribute plane must hold one value per vertex")
         arr = (C.c_void_p * max(1, len(planes)))(*[p.ctypes.data for p in planes])
         h = C.c_void_p()
         check(lib().sr_mesh_upload(arr, len(planes), n, idx.ctypes.data if idx.size else None, idx.size,

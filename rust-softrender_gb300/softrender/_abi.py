@@ -28,7 +28,7 @@ SR_CULL_NONE, SR_CULL_CLOCKWISE, SR_CULL_COUNTER_CLOCKWISE = 0, 1, 2
 SR_STAGE_VERTEX, SR_STAGE_GEOMETRY, SR_STAGE_FRAGMENT, SR_STAGE_BLEND = range(4)
 # sampling
 SR_SAMPLE_NEAREST, SR_SAMPLE_BILINEAR = 0, 1
-SR_SAMPLE_CLAMP, SR_SAMPLE_WRAP = 0, 1
+SR_SAMPLE_CLAMP, SR_SAMPLE_WRAP, SR_SAMPLE_BORDER = 0, 1, 2
 
 F32_MIN = -3.4028234663852886e38   # f32::MIN, the cleared depth
 

@@ -110,9 +110,11 @@ def test_clip_near_plane(oracle_mod):
     assert sorted(v for v in verts if v[2] == 0.0) == [(0.0, 0.25, 0.0, 1.0), (0.25, 0.0, 0.0, 1.0)]
 
 
-def _one_triangle_scene(tri_screen, W, H, z=(-0.5, -0.5, -0.5), rgba=(255, 0, 0, 255), **kw):
+def _one_triangle_scene(tri_screen, W, H, z=-0.5, rgba=(255, 0, 0, 255), **kw):
+    """Triangles given in screen space (every vertex at screen depth z)."""
     tri = np.asarray(tri_screen, dtype=np.float64)
-    x, y, zz = scenes._clip_from_screen(tri[:, 0], tri[:, 1], np.asarray(z) * -2.0 - 1.0, W, H)
+    z_ndc = np.full(len(tri), z * -2.0 - 1.0)
+    x, y, zz = scenes._clip_from_screen(tri[:, 0], tri[:, 1], z_ndc, W, H)
     col = np.array([rgba] * len(tri))
     packed = scenes._pack_rgba8(col[:, 0], col[:, 1], col[:, 2], col[:, 3])
     planes = [np.asarray(x, F), np.asarray(y, F), np.asarray(zz, F), packed.view(np.float32).copy()]
