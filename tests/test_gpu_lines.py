@@ -46,3 +46,48 @@ def test_normal_geometry_shaders(built_lib, oracle_mod, gs):
     sc = scenes.icosphere_scene(160, 120, subdiv=2, gs_mode=A.SR_GS_NAMED, gs=gs, fs="constant_color",
                                 tile=(32, 32))
     check(sc, oracle_mod)
+
+
+@pytest.mark.parametrize("filt", [A.SR_SAMPLE_NEAREST, A.SR_SAMPLE_BILINEAR])
+@pytest.mark.parametrize("edge", [A.SR_SAMPLE_CLAMP, A.SR_SAMPLE_WRAP, A.SR_SAMPLE_BORDER])
+def test_sampler_modes(built_lib, oracle_mod, filt, edge):
+    sc = scenes.grid_sphere_scene(96, 64, n_lat=12, n_lon=24, tex_size=16, tex_filter=filt, tex_edge=edge,
+                                  camera=dict(eye=(0.3, 0.2, 2.4), target=(0.0, 0.0, 0.0)))
+    sc.planes[6] = (sc.planes[6] * 3.0 - 1.0).astype("float32")     # uv beyond [0, 1]
+    sc.planes[7] = (sc.planes[7] * 3.0 - 1.0).astype("float32")
+    check(sc, oracle_mod)
+
+
+def test_render_to_texture(built_lib, oracle_mod):
+    """A frame rendered into an RGBA8 framebuffer becomes the texture of the
+    next draw (sr_texture_from_framebuffer)."""
+    import numpy as np
+    import softrender as sr
+    from util import compare_frame
+    first = scenes.icosphere_scene(64, 64, color_format=A.SR_COLOR_RGBA8)
+    pl, mesh, _ = sr.prepare_scene(first)
+    tex = sr.Texture(np.zeros((64, 64), np.uint32))
+    try:
+        sr.submit_scene(pl, mesh, None, first)
+        assert pl.sync() == 0
+        assert sr.lib().sr_texture_from_framebuffer(pl.handle, tex.handle) == 0
+        assert pl.sync() == 0
+        second = scenes.grid_sphere_scene(80, 60, n_lat=10, n_lon=20, tex_size=64, gs_mode=A.SR_GS_NONE,
+                                          camera=dict(eye=(0.2, 0.1, 2.6), target=(0.0, 0.0, 0.0)))
+        pl2, mesh2, _ = sr.prepare_scene(second)
+        try:
+            sr.submit_scene(pl2, mesh2, tex, second)
+            assert pl2.sync() == 0
+            got = pl2.read()
+        finally:
+            pl2.destroy()
+            mesh2.free()
+        # the oracle: render the first frame, use its colour as the texture
+        fb1, _, _ = oracle_mod.render(first)
+        second.texture = fb1.color.view(np.uint32).reshape(64, 64).copy()
+        fb2, _, _ = oracle_mod.render(second)
+        compare_frame(got, fb2)
+    finally:
+        pl.destroy()
+        mesh.free()
+        tex.free()

@@ -203,7 +203,7 @@ def test_read_async_matches_read(built_lib):
 
 def test_ordered_bins_longer_than_16k(built_lib, oracle_mod):
     """Blended draws whose bins hold more than 16,384 primitives (every bin
-    of a 64x64 frame is covered by 20,000 large alpha triangles)."""
-    sc = scenes.stress_scene(n_tiny=64, n_large=20000, size=64, seed=3, seed_large=5)
+    of a 64x64 frame is covered by some 22,000 of 40,000 large alpha triangles)."""
+    sc = scenes.stress_scene(n_tiny=64, n_large=40000, size=64, seed=3, seed_large=5)
     stats, _ = check(sc, oracle_mod)
     assert stats["bin_entries"] > 16 * 16384
