@@ -60,6 +60,21 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value, device):
+    """The largest `value` over all ranks (every rank gets it); the job's time
+    is the slowest replica's."""
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(units_per_rank, world, max_ms):
+    """Whole-job throughput in millions of units per second: every rank
+    processes units_per_rank in the timed steps, the job takes max_ms per step."""
+    return units_per_rank * world / (max_ms * 1e-3) / 1e6
+
+
 def measured_peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -208,9 +223,7 @@ def run_ours(args, rank, world, local):
     step_ms = [a.elapsed_time(b) for a, b in evs]
     ms = float(np.mean(step_ms))
     if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms, dev)
     stats = pl.stats()
 
     # per-stage device times (a separate profiled pass, same work)
@@ -550,7 +563,7 @@ def main():
     n_tris = scene.n_tris
     peak, peak_kind = measured_peaks()
     ms = r["ms"]
-    value = n_tris * world / (ms * 1e-3) / 1e6
+    value = whole_job_rate(n_tris, world, ms)
     frags = r["stats"]["fragments"]
     line = None
     if rank == 0:
