@@ -602,7 +602,7 @@ def main():
         if not args.no_served:
             line["served"] = run_served()
         if not args.no_cpu_baseline:
-            frame_s, sample, threads = cpu_frame_estimate(scene, every=4, tiles=48)
+            frame_s, sample, threads = cpu_frame_estimate(scene, every=2, tiles=256)
             line["cpu_baseline"] = {"value": round(n_tris / frame_s / 1e6, 5), "unit": "Mtris/s",
                                     "cores": threads, "kind": "port", "sample": sample}
     if world > 1:
@@ -621,10 +621,10 @@ def run_reference(args, rank, world):
     scene = scenes.grid_sphere_scene()
     n_tris = scene.n_tris
     for i in range(args.warmup):
-        cpu_frame_estimate(scene, every=64, tiles=2, tile_begin=i)
+        cpu_frame_estimate(scene, every=64, tiles=4, tile_begin=4 * i)
     frames, sample, threads = [], "", os.cpu_count()
     for i in range(args.steps):
-        f, sample, threads = cpu_frame_estimate(scene, every=16, tiles=32, tile_begin=32 * i)
+        f, sample, threads = cpu_frame_estimate(scene, every=4, tiles=128, tile_begin=128 * i)
         frames.append(f)
     frame_s = float(np.mean(frames))
     value = n_tris / frame_s / 1e6
