@@ -917,6 +917,11 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         } else if (b->autotune) {
             cfg = tune(b, NB);
             b->tuned[cls] = cfg;
+        } else {
+            // untuned: as many primitives per warp as still leave every SM
+            // its full complement of warps (a few large primitives on a big
+            // frame need one warp each, or most of the GPU idles)
+            while (cfg.G > 1 && tris / cfg.G < (uint64_t)sm_count() * 48u) cfg.G >>= 1;
         }
     }
     // the large-primitive counter packs the count into 24 bits
