@@ -550,6 +550,179 @@ SR_HD sr_v4 sr_blinn_phong(const sr_uniforms* U, sr_v4 position, sr_v4 normal, s
                       1.0f);
 }
 
+/* ------------------------------------------------ RGBA8 shading, fast path
+ * An RGBA8 target stores trunc(c * 255) of each gamma-encoded channel, so a
+ * power known to within a stated relative error decides the stored byte
+ * whenever c * 255 lies farther than that error from an integer.  The
+ * functions below compute the Blinn-Phong channels with single-precision
+ * powers on the tables of sr_log2_df / sr_exp2_df, carry a rigorous bound on
+ * the distance to the exactly computed value (sr_powf and the same f32 ops)
+ * through every step, and fall back to the exact computation for any pixel
+ * whose byte the bound does not decide or whose values leave the ranges the
+ * bound covers.  The returned word therefore equals
+ * sr_to_rgba8(sr_blinn_phong(...)) for every input.
+ *
+ * Error budget of the two primitives (each term over-estimated 4x or more in
+ * SR_FAST_POW_ERR; the CPU tests check the stated bounds on random and
+ * boundary inputs):
+ *   sr_ylog2_fast:  |t - y log2 x| <= |y| 2^-28 + |t| 2^-23
+ *                   (ln(1+r) to 2^-29 absolute, the table pair exact to 2^-48,
+ *                    y*e split exactly, two final roundings)
+ *   sr_exp2_fast:   relative error <= 2^-22.9 (table value and final fma
+ *                   rounding 2^-24 each, e^a - 1 to 2^-29 absolute)
+ *   so 2^t / x^y - 1 is within ln 2 (|y| 2^-28 + |t| 2^-23) + 2^-22.9.
+ */
+
+/* y log2(x) for a normal x > 0 */
+SR_HD float sr_ylog2_fast(float x, float y) {
+    const uint32_t bits = sr_f2u(x);
+    const float e = (float)((int)((bits >> 23) & 0xffu) - 127);
+    const float m = sr_u2f((bits & 0x007fffffu) | 0x3f800000u);
+    const int i = (int)((bits >> 17) & 63u);
+    const float r = sr_fma(m, SR_TAB(SR_LOG2_INV, i), -1.0f);     /* |r| < 2^-7, one rounding */
+    /* ln(1 + r) = r - r^2/2 + r^3/3 - r^4/4, truncation < 2^-37 */
+    const float lnr = r * sr_fma(r, sr_fma(r, sr_fma(r, -0.25f, 0.33333334f), -0.5f), 1.0f);
+    float sh, sl;
+    sr_two_sum(SR_TAB(SR_LOG2_HI, i), lnr * 0x1.715476p+0f, &sh, &sl);
+    sl = sl + SR_TAB(SR_LOG2_LO, i);
+    const float p = y * e;
+    const float pe = sr_fma(y, e, -p);                             /* y e = p + pe exactly */
+    return sr_fma(y, sh, p) + (pe + y * sl);
+}
+
+/* 2^t for |t| <= 120 (a normal result) */
+SR_HD float sr_exp2_fast(float t) {
+    const float n = sr_rint(t);
+    const float f = t - n;                                         /* exact, |f| <= 1/2 */
+    const float jf = sr_rint(f * 64.0f);
+    const float g = f - jf * 0.015625f;                            /* exact, |g| <= 1/128 */
+    const float a = g * 0x1.62e430p-1f;                            /* g ln 2 */
+    /* e^a - 1 = a + a^2/2 + a^3/6, truncation < 2^-34 */
+    const float em1 = a * sr_fma(a, sr_fma(a, 0.16666667f, 0.5f), 1.0f);
+    const float th = SR_TAB(SR_EXP2_HI, (int)jf + 32);
+    return sr_fma(th, em1, th) * sr_exp2i((int)n);
+}
+
+/* Relative error bound of sr_exp2_fast(sr_ylog2_fast(x, y)) against x^y,
+ * plus sr_powf's own (0.51 ulp <= 2^-23): a bound on |fast - sr_powf| / fast
+ * up to a factor 1 + 2^-20. */
+SR_HD float sr_fast_pow_err(float y, float t) {
+    return sr_fabs(y) * 0x1p-26f + sr_fabs(t) * 0x1p-21f + 0x1p-20f;
+}
+
+/* `as u8` of a value known to be non-NaN */
+SR_HD uint32_t sr_u8_of(float v) { return v >= 255.0f ? 255u : (v > 0.0f ? (uint32_t)v : 0u); }
+
+/*
+ * The stored byte of one gamma-encoded channel, trunc(u^g * 255) with
+ * u^g = sr_powf(u, g), where the u given is within du of the exactly
+ * computed u.  Returns 256 when the bound does not decide the byte.
+ */
+SR_HD uint32_t sr_encode_byte_fast(float u, float du, float g) {
+    /* unlit: |u_exact| <= 2^-63, so |u_exact^g| * 255 < 1 for g >= 1/4 (a
+     * negative u_exact gives NaN or a value of the same tiny size): byte 0 */
+    if (sr_fabs(u) + du <= 0x1p-64f && g >= 0.25f && g <= 256.0f) return 0u;
+    if (!(u >= 0x1p-100f && u <= 0x1p100f && du <= u * 0x1p-10f && sr_fabs(g) <= 256.0f)) return 256u;
+    const float t = sr_ylog2_fast(u, g);
+    if (!(sr_fabs(t) <= 120.0f)) return 256u;
+    const float G = sr_exp2_fast(t);
+    /* |G - sr_powf(u_exact, g)| <= R G: the fast power's error and the
+     * input's, |(1 +- d)^g - 1| <= 1.25 |g| d, which holds because R <= 2^-8
+     * below keeps |g| d under 2^-8 */
+    const float R = sr_fast_pow_err(g, t) + 1.25f * sr_fabs(g) * (du / u);
+    if (!(R <= 0x1p-8f)) return 256u;
+    const float v = G * 255.0f;
+    /* both sides round G * 255 (2^-24 each); 2 ulp(v) more keep the rounded
+     * ends v -+ B outside the exact interval */
+    const float B = v * (R * 1.0625f + 0x1p-20f) + 0x1p-30f;
+    const uint32_t lo = sr_u8_of(v - B), hi = sr_u8_of(v + B);
+    return lo == hi ? lo : 256u;
+}
+
+/*
+ * x^y for the decoded texel channel or the specular term: the value and a
+ * bound on its distance to sr_powf(x, y), for x in [0, 1] and y in (0, 256].
+ * Returns false when the case is outside the bound's domain.
+ */
+SR_HD bool sr_pow_bounded(float x, float y, float* val, float* err) {
+    if (!(y > 0.0f && y <= 256.0f)) return false;
+    if (x == 0.0f) { *val = sr_powf(x, y); *err = 0.0f; return true; }   /* exact zero (+0 or -0) */
+    if (!(x >= 0x1p-100f && x <= 1.0f)) return false;
+    const float t = sr_ylog2_fast(x, y);
+    if (t < -120.0f) { *val = 0.0f; *err = 0x1p-119f; return true; }  /* exact value < 2^-119.9 */
+    if (!(t <= 120.0f)) return false;
+    const float p = sr_exp2_fast(t);
+    *val = p;
+    *err = p * (sr_fast_pow_err(y, t) * 1.0625f) + 0x1p-140f;
+    return true;
+}
+
+/*
+ * sr_to_rgba8(sr_blinn_phong(U, position, normal, color)) where `color` is
+ * within dcol (per channel, absolute) of the colour the exact computation
+ * uses; returns false when the fast path cannot decide a byte.
+ */
+SR_HD bool sr_blinn_phong_rgba8_fast(const sr_uniforms* U, sr_v4 position, sr_v4 normal, sr_v4 color,
+                                     sr_v4 dcol, uint32_t* out) {
+    /* the same operations as sr_blinn_phong up to the powers */
+    sr_v4 camera = sr_make_v4(U->camera[0], U->camera[1], U->camera[2], U->camera[3]);
+    sr_v4 light_dir = sr_make_v4(U->light_dir[0], U->light_dir[1], U->light_dir[2], U->light_dir[3]);
+    sr_v4 view_dir = sr_normalize4(sr_sub4(camera, position));
+    sr_v4 halfway = sr_normalize4(sr_add4(light_dir, view_dir));
+    float NdotL = sr_max(sr_min(sr_dot4(light_dir, normal), 1.0f), 0.0f);
+    float NdotH = sr_max(sr_min(sr_dot4(normal, halfway), 1.0f), 0.0f);
+    float VdotH = sr_max(sr_min(sr_dot4(view_dir, halfway), 1.0f), 0.0f);
+    float f = sr_fresnel_schlick(VdotH, U->ior);
+    float diffuse = NdotL * (1.0f - f);
+    float P, dP;
+    if (!sr_pow_bounded(NdotH, U->shininess * 2.0f, &P, &dP)) return false;
+    const float specular = f * P;
+    if (!(sr_fabs(specular) <= 0x1p100f && sr_fabs(diffuse) <= 0x1p100f)) return false;
+    /* |f P - f P_exact| plus the rounding of both products */
+    const float dspec = sr_fabs(f) * dP * 1.0625f + sr_fabs(specular) * 0x1p-22f + 0x1p-140f;
+    const float inv_gamma = 1.0f / U->gamma;
+    const float I = U->intensity;
+    const float cc[3] = {color.x, color.y, color.z};
+    const float dc[3] = {dcol.x, dcol.y, dcol.z};
+    uint32_t bytes[3];
+    for (int ch = 0; ch < 3; ++ch) {
+        const float dcl = diffuse * cc[ch];
+        const float t = specular + dcl;
+        /* the two sums and products round on both sides (2^-23 of each) */
+        const float dt = dspec + (sr_fabs(diffuse) * dc[ch] * 1.0625f + sr_fabs(dcl) * 0x1p-22f) +
+                         sr_fabs(t) * 0x1p-22f;
+        const float u = I * t;
+        const float du = sr_fabs(I) * dt * 1.0625f + sr_fabs(u) * 0x1p-22f;
+        const uint32_t b = sr_encode_byte_fast(u, du, inv_gamma);
+        if (b > 255u) return false;
+        bytes[ch] = b;
+    }
+    *out = bytes[0] | (bytes[1] << 8) | (bytes[2] << 16) | (255u << 24);   /* alpha 1.0 */
+    return true;
+}
+
+/* The RGBA8 word of the Blinn-Phong fragment shader (uniform colour). */
+SR_HD uint32_t sr_blinn_phong_rgba8(const sr_uniforms* U, sr_v4 position, sr_v4 normal, sr_v4 color) {
+    uint32_t w;
+    if (sr_blinn_phong_rgba8_fast(U, position, normal, color, sr_make_v4(0.0f, 0.0f, 0.0f, 0.0f), &w)) return w;
+    return sr_to_rgba8(sr_blinn_phong(U, position, normal, color));
+}
+
+/* The RGBA8 word of the textured Blinn-Phong fragment shader: `texel` is the
+ * sampled colour before decode_gamma. */
+SR_HD uint32_t sr_textured_blinn_phong_rgba8(const sr_uniforms* U, sr_v4 position, sr_v4 normal, sr_v4 texel) {
+    const float g = U->gamma;
+    sr_v4 col, dcol;
+    uint32_t w;
+    if (sr_pow_bounded(texel.x, g, &col.x, &dcol.x) && sr_pow_bounded(texel.y, g, &col.y, &dcol.y) &&
+        sr_pow_bounded(texel.z, g, &col.z, &dcol.z)) {
+        col.w = texel.w;
+        dcol.w = 0.0f;
+        if (sr_blinn_phong_rgba8_fast(U, position, normal, col, dcol, &w)) return w;
+    }
+    return sr_to_rgba8(sr_blinn_phong(U, position, normal, sr_decode_gamma(texel, g)));
+}
+
 /* 4-point-light Blinn-Phong with ACES tonemap (full_example/src/shaders.rs:108-163). */
 SR_HD sr_v4 sr_aces_lights(const sr_uniforms* U, sr_v4 position, sr_v4 normal) {
     sr_v4 camera = sr_make_v4(U->camera[0], U->camera[1], U->camera[2], U->camera[3]);

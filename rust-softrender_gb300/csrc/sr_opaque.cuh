@@ -210,9 +210,12 @@ __device__ __forceinline__ void resolve_block(const DrawParams& P, const sr_unif
                 kv[4 * q + 3] = (xa.w * u + xb.w * v) + xc.w * w;
             }
         }
-        const sr_v4 col = shade_fs<FS>(U, kv, tex, P);
-        if (FMT == SR_COLOR_RGBA32F) reinterpret_cast<float4*>(color)[gi] = make_float4(col.x, col.y, col.z, col.w);
-        else if (FMT == SR_COLOR_RGBA8) reinterpret_cast<uint32_t*>(color)[gi] = sr_to_rgba8(col);
+        if (FMT == SR_COLOR_RGBA32F) {
+            const sr_v4 col = shade_fs<FS>(U, kv, tex, P);
+            reinterpret_cast<float4*>(color)[gi] = make_float4(col.x, col.y, col.z, col.w);
+        } else if (FMT == SR_COLOR_RGBA8) {
+            reinterpret_cast<uint32_t*>(color)[gi] = shade_fs_rgba8<FS>(U, kv, tex, P);
+        }
         if (P.has_depth) depth[gi] = z;
     }
     __syncthreads();

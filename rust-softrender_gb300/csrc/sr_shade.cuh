@@ -28,6 +28,24 @@ __device__ __forceinline__ sr_v4 shade_fs(const sr_uniforms& U, const float* k, 
     return sr_make_v4(U.color[0], U.color[1], U.color[2], U.color[3]);
 }
 
+// The RGBA8 word of the fragment closure's colour, equal to
+// sr_to_rgba8(shade_fs<FS>(...)) for every input: the Blinn-Phong shaders
+// take the bounded-error fast path of sr_shaders.h, which repeats the exact
+// computation for the pixels its bound does not decide.
+template <int FS>
+__device__ __forceinline__ uint32_t shade_fs_rgba8(const sr_uniforms& U, const float* k, const uint32_t* tex,
+                                                   const DrawParams& P) {
+    if (FS == FS_BLINN_PHONG_DIR)
+        return sr_blinn_phong_rgba8(&U, sr_make_v4(k[0], k[1], k[2], k[3]), sr_make_v4(k[4], k[5], k[6], k[7]),
+                                    sr_make_v4(U.color[0], U.color[1], U.color[2], U.color[3]));
+    if (FS == FS_TEXTURED_BLINN_PHONG) {
+        const sr_v4 t = sr_sample_rgba8(tex, P.tex_w, P.tex_h, k[8], k[9], (int)P.tex_filter, (int)P.tex_edge);
+        return sr_textured_blinn_phong_rgba8(&U, sr_make_v4(k[0], k[1], k[2], k[3]),
+                                             sr_make_v4(k[4], k[5], k[6], k[7]), t);
+    }
+    return sr_to_rgba8(shade_fs<FS>(U, k, tex, P));
+}
+
 // Barycentric varyings (interpolate.rs:43-52): (ka*u + kb*v) + kc*w
 template <int NK>
 __device__ __forceinline__ void interp_varyings(const float* __restrict__ vary, uint32_t a, uint32_t b, uint32_t c,
