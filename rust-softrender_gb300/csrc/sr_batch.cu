@@ -203,7 +203,8 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float
                             float4* rr = setup + 4 * (size_t)g;
                             rr[0] = make_float4(y2 - y3, x3 - x2, y3 - y1, x1 - x3);
                             rr[1] = make_float4(x3, y3, det, s0.z);
-                            rr[2] = make_float4(s1.z, s2.z, __uint_as_float(REC_RASTER | (safe ? 0u : REC_UNSAFE)), 0.0f);
+                            rr[2] = make_float4(s1.z, s2.z, __uint_as_float(REC_RASTER | (safe ? 0u : REC_UNSAFE)),
+                                                det_sign(det));
                             rr[3] = make_float4(__int_as_float(ix0), __int_as_float(iy0), __int_as_float(ix1),
                                                 __int_as_float(iy1));
                             n_raster = 1;
@@ -255,6 +256,7 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
     __shared__ float4 srec[8][32][3];
     __shared__ uint32_t sxy[8][32];
     __shared__ uint32_t sw[8][32];
+    __shared__ uint32_t sst[8][32];     // first item of the staged primitive
     __shared__ Slot sslot[8][32];
     __shared__ unsigned long long smag[8][32];
     const uint32_t n = *T.n;
@@ -281,53 +283,57 @@ __global__ void __launch_bounds__(256) batch_raster_small_kernel(BTables T, cons
                 const unsigned long long old = atomicAdd(queues + Q_BIG, (1ull << 40) | nch);
                 big_list[old >> 40] = g;
                 big_base[old >> 40] = (uint32_t)(old & ((1ull << 40) - 1));
-            } else if (at) {
+            } else {
                 a = (uint32_t)at;
-                const uint32_t i = owner_from(T.tbase, n, i0, g);
-                const BInst& I = T.inst[i];
-                const float4* r = setup + 4 * (size_t)g;
-                srec[wl][lane][0] = __ldg(r);
-                srec[wl][lane][1] = __ldg(r + 1);
-                srec[wl][lane][2] = __ldg(r + 2);
-                const float4 r3 = __ldg(r + 3);
-                const uint32_t W = I.P.W, H = I.P.H;
-                const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
-                const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
-                const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)W - 1);
-                const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)H - 1);
-                const uint32_t w = x1 - x0 + 1;
-                mark_rect(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1);
-                const uint32_t sb = seam_bits(x0, y0, x1, y1, W, H, I.P.tile_w, I.P.tile_h);
-                sxy[wl][lane] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
-                sw[wl][lane] = w;
-                Slot S;
-                S.wh = W | (H << 16);
-                S.tiles = I.P.tile_w | (I.P.tile_h << 16);
-                S.mx = I.mx;
-                S.my = I.my;
-                S.n_depth = I.P.n_raster_host | (I.P.has_depth ? 0x80000000u : 0u);
-                S.t = g - I.tbase;
-                S.gkeys = I.gkeys;
-                sslot[wl][lane] = S;
-                smag[wl][lane] = ((1ull << 32) + w - 1) / w;
             }
         }
-        __syncwarp();
         const uint32_t inc = warp_inclusive_scan(a);
         const uint32_t tot = __shfl_sync(0xffffffffu, inc, 31);
         const uint32_t ex = inc - a;
+        const uint32_t nonempty = __ballot_sync(0xffffffffu, a != 0);
+        if (a) {
+            // compacted slot: the rank of this primitive among the non-empty ones
+            const uint32_t lane_c = __popc(nonempty & ((1u << lane) - 1u));
+            const uint32_t i = owner_from(T.tbase, n, i0, g);
+            const BInst& I = T.inst[i];
+            const float4* r = setup + 4 * (size_t)g;
+            srec[wl][lane_c][0] = __ldg(r);
+            srec[wl][lane_c][1] = __ldg(r + 1);
+            srec[wl][lane_c][2] = __ldg(r + 2);
+            const float4 r3 = __ldg(r + 3);
+            const uint32_t W = I.P.W, H = I.P.H;
+            const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
+            const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
+            const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)W - 1);
+            const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)H - 1);
+            const uint32_t w = x1 - x0 + 1;
+            mark_rect(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1);
+            const uint32_t sb = seam_bits(x0, y0, x1, y1, W, H, I.P.tile_w, I.P.tile_h);
+            sxy[wl][lane_c] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
+            sw[wl][lane_c] = w;
+            Slot S;
+            S.wh = W | (H << 16);
+            S.tiles = I.P.tile_w | (I.P.tile_h << 16);
+            S.mx = I.mx;
+            S.my = I.my;
+            S.n_depth = I.P.n_raster_host | (I.P.has_depth ? 0x80000000u : 0u);
+            S.t = g - I.tbase;
+            S.gkeys = I.gkeys;
+            sslot[wl][lane_c] = S;
+            sst[wl][lane_c] = ex;
+            smag[wl][lane_c] = ((1ull << 32) + w - 1) / w;
+        }
+        __syncwarp();
+        const uint32_t le = (2u << lane) - 1u;   // lanes 0..lane
+        uint32_t before = 0;                     // primitive starts before the window
         for (uint32_t base = 0; base < tot; base += 32) {
             const uint32_t q = base + lane;
-            uint32_t lo = 0;
-#pragma unroll
-            for (uint32_t step = G >> 1; step >= 1; step >>= 1) {
-                const uint32_t c = lo + step;
-                const uint32_t v = __shfl_sync(0xffffffffu, ex, c & 31u);
-                if (c < G && v <= q) lo = c;
-            }
-            const uint32_t exo = __shfl_sync(0xffffffffu, ex, lo);
+            const uint32_t rel = ex - base;
+            const uint32_t starts = __reduce_or_sync(0xffffffffu, (a && rel < 32u) ? (1u << rel) : 0u);
+            const uint32_t lo = before + __popc(starts & le) - 1u;
+            before += __popc(starts);
             if (q < tot) {
-                const uint32_t local = q - exo;
+                const uint32_t local = q - sst[wl][lo];
                 const uint32_t w = sw[wl][lo];
                 const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][lo]) >> 32);  // local / w
                 const uint32_t xy = sxy[wl][lo];

@@ -31,8 +31,10 @@ namespace sr {
 // Each warp takes G consecutive primitives (G a power of two <= 32, chosen by
 // the host so that small meshes still spread over every SM); their bbox pixels
 // are flattened into items spread over the lanes (warp prefix sum of the pixel
-// counts and a log2(G)-step shuffle search for each lane's owner), so adjacent
-// lanes test adjacent pixels.  Records are staged in shared memory per warp.
+// counts), so adjacent lanes test adjacent pixels.  The non-empty primitives'
+// records are staged, compacted, in shared memory per warp; for each window of
+// 32 items the lanes OR-reduce a mask of the primitive starts inside it, and
+// an item's owner is the number of starts at or before it, less one.
 template <uint32_t G>
 __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
     DrawParams P, const float4* __restrict__ setup, const unsigned long long* __restrict__ area,
@@ -41,6 +43,8 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
     __shared__ float4 srec[RG_THREADS / 32][32][3];
     __shared__ uint32_t sxy[RG_THREADS / 32][32];           // x0 | y0 << 16
     __shared__ uint32_t sw[RG_THREADS / 32][32];            // bbox width
+    __shared__ uint32_t sst[RG_THREADS / 32][32];           // first item
+    __shared__ uint32_t st[RG_THREADS / 32][32];            // primitive index
     __shared__ unsigned long long smag[RG_THREADS / 32][32]; // ceil(2^32 / width)
     if (flags->poison) return;
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
@@ -58,47 +62,49 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
         uint32_t a = 0;
         if (lane < G && t < N) {
             const unsigned long long at = area[t];
-            if (at > RG_BIG) {
-                big_list[atomicAdd(&flags->n_big, 1ull)] = t;
-            } else if (at) {
-                a = (uint32_t)at;
-                const float4* r = setup + 4 * (size_t)t;
-                srec[wl][lane][0] = __ldg(r);
-                srec[wl][lane][1] = __ldg(r + 1);
-                srec[wl][lane][2] = __ldg(r + 2);
-                const float4 r3 = __ldg(r + 3);
-                const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
-                const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
-                const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)P.W - 1);
-                const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1);
-                const uint32_t w = x1 - x0 + 1;
-                mark_rect(bitmap, blocks_x, x0, y0, x1, y1);
-                const uint32_t sb = seam_bits(x0, y0, x1, y1, P.W, P.H, P.tile_w, P.tile_h);
-                sxy[wl][lane] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
-                sw[wl][lane] = w;
-                smag[wl][lane] = ((1ull << 32) + w - 1) / w;
-            }
+            if (at > RG_BIG) big_list[atomicAdd(&flags->n_big, 1ull)] = t;
+            else a = (uint32_t)at;
         }
-        __syncwarp();
         const uint32_t inc = warp_inclusive_scan(a);
         const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
         const uint32_t ex = inc - a;
+        const uint32_t nonempty = __ballot_sync(0xffffffffu, a != 0);
+        if (a) {
+            // compacted slot: the rank of this primitive among the non-empty ones
+            const uint32_t c = __popc(nonempty & ((1u << lane) - 1u));
+            const float4* r = setup + 4 * (size_t)t;
+            srec[wl][c][0] = __ldg(r);
+            srec[wl][c][1] = __ldg(r + 1);
+            srec[wl][c][2] = __ldg(r + 2);
+            const float4 r3 = __ldg(r + 3);
+            const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
+            const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
+            const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)P.W - 1);
+            const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1);
+            const uint32_t w = x1 - x0 + 1;
+            mark_rect(bitmap, blocks_x, x0, y0, x1, y1);
+            const uint32_t sb = seam_bits(x0, y0, x1, y1, P.W, P.H, P.tile_w, P.tile_h);
+            sxy[wl][c] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
+            sw[wl][c] = w;
+            sst[wl][c] = ex;
+            st[wl][c] = t;
+            smag[wl][c] = ((1ull << 32) + w - 1) / w;
+        }
+        __syncwarp();
+        const uint32_t le = (2u << lane) - 1u;   // lanes 0..lane
+        uint32_t before = 0;                     // primitive starts before the window
         for (uint32_t base = 0; base < total; base += 32) {
             const uint32_t q = base + lane;
-            uint32_t lo = 0;
-#pragma unroll
-            for (uint32_t step = G >> 1; step >= 1; step >>= 1) {
-                const uint32_t c = lo + step;
-                const uint32_t v = __shfl_sync(0xffffffffu, ex, c & 31u);
-                if (c < G && v <= q) lo = c;
-            }
-            const uint32_t exo = __shfl_sync(0xffffffffu, ex, lo);
+            const uint32_t rel = ex - base;
+            const uint32_t starts = __reduce_or_sync(0xffffffffu, (a && rel < 32u) ? (1u << rel) : 0u);
+            const uint32_t o = before + __popc(starts & le) - 1u;
+            before += __popc(starts);
             if (q < total) {
-                const uint32_t local = q - exo;
-                const uint32_t w = sw[wl][lo];
-                const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][lo]) >> 32);  // local / w
-                const uint32_t xy = sxy[wl][lo];
-                rg_fragment(P, srec[wl][lo][0], srec[wl][lo][1], srec[wl][lo][2], t0 + lo,
+                const uint32_t local = q - sst[wl][o];
+                const uint32_t w = sw[wl][o];
+                const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][o]) >> 32);  // local / w
+                const uint32_t xy = sxy[wl][o];
+                rg_fragment(P, srec[wl][o][0], srec[wl][o][1], srec[wl][o][2], st[wl][o],
                             (xy & 0x7fffu) + (local - row * w), ((xy >> 16) & 0x7fffu) + row, N, gkeys, bitmap,
                             stencil, gate_with_stencil, mx, my, ((xy >> 15) & 1u) | ((xy >> 30) & 2u), frags);
             }

@@ -9,9 +9,6 @@ namespace sr {
 constexpr int RG_THREADS = 256;
 constexpr uint32_t TOUCH_LOG2 = 5;               // touched-block bitmap granularity: 32 x 32
 
-__device__ __forceinline__ bool surely_negative(float n, float det) {
-    return (n * det < 0.0f) && fabsf(n) > 1.0e-18f && fabsf(det) < 1.0e18f;
-}
 
 __device__ __forceinline__ void mark_touched(uint32_t* bitmap, uint32_t blocks_x, uint32_t px, uint32_t py) {
     uint32_t b = (py >> TOUCH_LOG2) * blocks_x + (px >> TOUCH_LOG2);
@@ -54,10 +51,12 @@ __device__ __forceinline__ void frag_emit(uint32_t W, uint32_t H, uint32_t tile_
                                           uint32_t stencil_test_id, uint32_t sref, unsigned long long& frags) {
     const float x = (float)px + 0.5f, y = (float)py + 0.5f;
     const float dx = x - r1.x, dy = y - r1.y;
+    // r2.w = det_sign(det): a certainly negative u or v rejects the pixel
+    // without the divisions
     const float nu = r0.x * dx + r0.y * dy;
-    if (surely_negative(nu, r1.z)) return;
+    if (r2.w * nu < -1.0e-18f) return;
     const float nv = r0.z * dx + r0.w * dy;
-    if (surely_negative(nv, r1.z)) return;
+    if (r2.w * nv < -1.0e-18f) return;
     const float u = nu / r1.z, v = nv / r1.z;
     const float w = 1.0f - u - v;
     if (u < 0.0f || v < 0.0f || w < 0.0f) return;

@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
                         r[0] = make_float4(y2 - y3, x3 - x2, y3 - y1, x1 - x3);
                         r[1] = make_float4(x3, y3, det, s0.z);
                         uint32_t fl = REC_RASTER | (safe ? 0u : REC_UNSAFE);
-                        r[2] = make_float4(s1.z, s2.z, __uint_as_float(fl), 0.0f);
+                        r[2] = make_float4(s1.z, s2.z, __uint_as_float(fl), det_sign(det));
                         r[3] = make_float4(__int_as_float(ix0), __int_as_float(iy0), __int_as_float(ix1),
                                            __int_as_float(iy1));
                         n_raster = 1;

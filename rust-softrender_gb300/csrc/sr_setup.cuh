@@ -7,6 +7,18 @@ namespace sr {
 
 constexpr uint32_t RECT_EMPTY = 0xffffffffu;   // binrect of a primitive with no regular bins
 
+// Setup record, 4 x float4 per raster primitive:
+//   r0 = (y2-y3, x3-x2, y3-y1, x1-x3)   edge coefficients of the numerators
+//   r1 = (x3, y3, det, z1)
+//   r2 = (z2, z3, flags, s)             s = det_sign(det)
+//   r3 = clamped-to-frame bbox as ints (x0, y0, x1, y1)
+// s is +1 or -1 for 0 < |det| < 1e18 and 0 otherwise: s * n < -1e-18 then
+// proves that the quotient n / det rounds to a negative non-zero value
+// (|n / det| > 1e-36 cannot underflow), so such a pixel is outside that edge.
+__device__ __forceinline__ float det_sign(float det) {
+    return (det > 0.0f && det < 1.0e18f) ? 1.0f : ((det < 0.0f && det > -1.0e18f) ? -1.0f : 0.0f);
+}
+
 // ------------------------------------------------------- extension pass
 // An unsafe primitive can produce fragments outside its bbox, but only at
 // the pixels where the reference evaluates it there: the projection of its
