@@ -4,8 +4,11 @@
 //
 // Every stage is a persistent kernel (a fixed grid sized to the GPU) that
 // pulls work items from the flattened (instance, item) space: vertex quads,
-// primitives, 32x32 resolve blocks and clear chunks.  An item's instance is
-// found by binary search over per-instance exclusive prefix sums.  Per-draw
+// primitives, 32x32 resolve blocks and 32x32 clear blocks.  An item's
+// instance is found by binary search over per-instance exclusive prefix sums
+// (once per warp where a warp's items are consecutive).  A cleared target is
+// cleared after the raster passes, and only where no fragment landed: resolve
+// writes the clear values into the rest of the blocks it visits.  Per-draw
 // results are identical to sr_render's: the per-primitive, per-pixel and
 // per-block device code is the same (sr_vertex.cuh, sr_setup.cuh,
 // sr_opaque.cuh), only the indexing differs; each instance keeps its own
@@ -58,10 +61,9 @@ struct BTables {
     const uint32_t* qbase;        // exclusive prefix of vertex quads        (NB + 1)
     const uint32_t* tbase;        // exclusive prefix of primitives          (NB + 1)
     const uint32_t* bbase;        // exclusive prefix of 32x32 resolve blocks (NB + 1)
-    const uint32_t* cbase;        // exclusive prefix of clear chunks        (NB + 1)
+    const uint32_t* cbase;        // exclusive prefix of 32x32 clear blocks  (NB + 1)
 };
 
-constexpr uint32_t CLEAR_CHUNK = 8192;   // pixels per clear work item
 constexpr uint32_t BIG_CHUNK = 4096;     // bbox pixels per work item of a large primitive
 // Work-queue counters of a batch (device array of 32 u64):
 //   [fs * 3 + format]  resolve launch of that (fragment shader, colour format)
@@ -94,33 +96,31 @@ __device__ __forceinline__ uint32_t owner_from(const uint32_t* __restrict__ base
 }
 
 // ---------------------------------------------------------------- clear
+// The clears of the batch's cleared targets, deferred until after the raster
+// passes: one warp per 32x32 block of a cleared target.  A block with
+// fragments (its bitmap bit set) is left to resolve, which writes every pixel
+// of it (the winner's shade or the clear values).
 __global__ void __launch_bounds__(256) batch_clear_kernel(BTables T) {
     const uint32_t n = *T.n;
     const uint32_t total = __ldg(T.cbase + n);
-    for (uint32_t j = blockIdx.x; j < total; j += gridDim.x) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t j = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5); j < total; j += warps) {
         const uint32_t i = owner_of(T.cbase, n, j);
         const BInst& I = T.inst[i];
-        const size_t npx = (size_t)I.P.W * I.P.H;
-        const size_t p0 = (size_t)(j - __ldg(T.cbase + i)) * CLEAR_CHUNK;
-        const size_t p1 = min(npx, p0 + CLEAR_CHUNK);
+        const uint32_t b = j - __ldg(T.cbase + i);
+        if ((I.bitmap[b >> 5] >> (b & 31)) & 1u) continue;
+        const uint32_t W = I.P.W, H = I.P.H;
+        const uint32_t bx = (W + 31) >> 5;
+        const uint32_t x = ((b % bx) << 5) + lane, y0 = (b / bx) << 5;
+        if (x >= W) continue;
+        const uint32_t y1 = min(y0 + 32u, H);
         const uint4 cv = I.clear_color;
-        const float far_ = -3.40282347e+38f;   // f32::MIN (attachments/depth.rs:31)
-        const uint32_t dv = __float_as_uint(far_);
-        for (size_t p = p0 + 4 * (size_t)threadIdx.x; p < p1; p += 4 * (size_t)blockDim.x) {
-            const bool full = p + 4 <= p1;
-            if (I.P.color_format == SR_COLOR_RGBA32F) {
-                uint4* c = reinterpret_cast<uint4*>(I.color) + p;
-                for (uint32_t k = 0; k < 4 && p + k < p1; ++k) c[k] = cv;
-            } else if (I.P.color_format == SR_COLOR_RGBA8) {
-                uint32_t* c = reinterpret_cast<uint32_t*>(I.color) + p;
-                if (full) *reinterpret_cast<uint4*>(c) = cv;
-                else for (uint32_t k = 0; p + k < p1; ++k) c[k] = cv.x;
-            }
-            if (I.P.has_depth) {
-                float* d = I.depth + p;
-                if (full) *reinterpret_cast<uint4*>(d) = make_uint4(dv, dv, dv, dv);
-                else for (uint32_t k = 0; p + k < p1; ++k) d[k] = far_;
-            }
+        for (uint32_t y = y0; y < y1; ++y) {
+            const size_t gi = (size_t)y * W + x;
+            if (I.P.color_format == SR_COLOR_RGBA32F) reinterpret_cast<uint4*>(I.color)[gi] = cv;
+            else if (I.P.color_format == SR_COLOR_RGBA8) reinterpret_cast<uint32_t*>(I.color)[gi] = cv.x;
+            if (I.P.has_depth) I.depth[gi] = F32_LOWEST;
         }
     }
 }
@@ -130,8 +130,15 @@ __global__ void __launch_bounds__(128) batch_vertex_kernel(BTables T, float4* __
                                                            float* __restrict__ vary) {
     const uint32_t n = *T.n;
     const uint32_t total = __ldg(T.qbase + n);
-    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
-        const uint32_t i = owner_of(T.qbase, n, j);
+    const uint32_t lane = threadIdx.x & 31;
+    // a warp takes 32 consecutive quads per round; lane 0 finds the draw
+    for (uint32_t jw = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); jw < total; jw += gridDim.x * blockDim.x) {
+        uint32_t i0 = 0;
+        if (lane == 0) i0 = owner_of(T.qbase, n, jw);
+        i0 = __shfl_sync(0xffffffffu, i0, 0);
+        const uint32_t j = jw + lane;
+        if (j >= total) continue;
+        const uint32_t i = owner_from(T.qbase, n, i0, j);
         const BInst& I = T.inst[i];
         const uint32_t q = j - __ldg(T.qbase + i);
         float4* s4 = scr4 + I.vbase;
@@ -156,14 +163,16 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float
     const uint32_t total = __ldg(T.tbase + n);
     const uint32_t stride = gridDim.x * blockDim.x;
     const uint32_t lane = threadIdx.x & 31;
-    // every thread runs the same number of iterations (warp reductions below)
-    const uint32_t rounds = (total + stride - 1) / stride;
-    for (uint32_t r = 0; r < rounds; ++r) {
-        const uint32_t g = r * stride + blockIdx.x * blockDim.x + threadIdx.x;
-        unsigned long long n_raster = 0, n_unsafe = 0;
-        uint32_t nan_cnt = 0;
+    uint32_t n_raster = 0, n_unsafe = 0, nan_cnt = 0;
+    // a warp takes 32 consecutive primitives per round: lane 0 finds the draw
+    // of the first, the others step forward from it
+    for (uint32_t gw = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); gw < total; gw += stride) {
+        uint32_t i0 = 0;
+        if (lane == 0) i0 = owner_of(T.tbase, n, gw);
+        i0 = __shfl_sync(0xffffffffu, i0, 0);
+        const uint32_t g = gw + lane;
         if (g < total) {
-            const uint32_t i = owner_of(T.tbase, n, g);
+            const uint32_t i = owner_from(T.tbase, n, i0, g);
             const BInst& I = T.inst[i];
             const DrawParams& P = I.P;
             const uint32_t t = g - I.tbase;
@@ -188,7 +197,7 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float
                 const float mnx = sr_min(sr_min(x1, x2), x3), mny = sr_min(sr_min(y1, y2), y3);
                 const float mxx = sr_max(sr_max(x1, x2), x3), mxy = sr_max(sr_max(y1, y2), y3);
                 if (isnan(mnx) || isnan(mny)) {
-                    nan_cnt = 1;
+                    ++nan_cnt;
                 } else {
                     const int W = (int)P.W, H = (int)P.H;
                     const int ix0 = floor_sat(mnx, -1, W), ix1 = floor_sat(mxx, -1, W);
@@ -207,26 +216,28 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float
                                                 det_sign(det));
                             rr[3] = make_float4(__int_as_float(ix0), __int_as_float(iy0), __int_as_float(ix1),
                                                 __int_as_float(iy1));
-                            n_raster = 1;
-                            n_unsafe = safe ? 0 : 1;
+                            ++n_raster;
+                            if (!safe) {
+                                ++n_unsafe;
+                                unsafe_list[atomicAdd(&flags->n_unsafe_list, 1ull)] = g;
+                            }
                             area[g] = b_in ? (unsigned long long)(qx1 - qx0 + 1) * (unsigned long long)(qy1 - qy0 + 1)
                                            : 0ull;
-                            if (!safe) unsafe_list[atomicAdd(&flags->n_unsafe_list, 1ull)] = g;
                         }
                     }
                 }
             }
         }
-        for (int o = 16; o > 0; o >>= 1) {
-            n_raster += __shfl_down_sync(0xffffffffu, n_raster, o);
-            n_unsafe += __shfl_down_sync(0xffffffffu, n_unsafe, o);
-            nan_cnt += __shfl_down_sync(0xffffffffu, nan_cnt, o);
-        }
-        if (lane == 0) {
-            if (n_raster) atomicAdd(&flags->triangles_raster, n_raster);
-            if (n_unsafe) atomicAdd(&flags->unsafe, n_unsafe);
-            if (nan_cnt) { atomicAdd(&flags->nan_bbox, nan_cnt); atomicAdd(&flags->nan_total, nan_cnt); }
-        }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        n_raster += __shfl_down_sync(0xffffffffu, n_raster, o);
+        n_unsafe += __shfl_down_sync(0xffffffffu, n_unsafe, o);
+        nan_cnt += __shfl_down_sync(0xffffffffu, nan_cnt, o);
+    }
+    if (lane == 0) {
+        if (n_raster) atomicAdd(&flags->triangles_raster, (unsigned long long)n_raster);
+        if (n_unsafe) atomicAdd(&flags->unsafe, (unsigned long long)n_unsafe);
+        if (nan_cnt) { atomicAdd(&flags->nan_bbox, nan_cnt); atomicAdd(&flags->nan_total, nan_cnt); }
     }
 }
 
@@ -485,7 +496,7 @@ __global__ void __launch_bounds__(256) batch_resolve_kernel(BTables T, const flo
         if (I.P.fs != FS || (int)I.P.color_format != FMT) continue;
         resolve_block<FS, FMT>(I.P, T.U[i], b, I.P.n_raster_host, setup + 4 * (size_t)I.tbase, I.indices,
                                vary + (size_t)I.vbase * VSTRIDE, I.tex, I.color, I.depth, nullptr, 0u, I.gkeys,
-                               I.bitmap);
+                               I.bitmap, I.clear != 0, I.clear_color);
     }
 }
 
@@ -611,7 +622,6 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     cudaMemcpyAsync(b->dtab.p, b->htab, L.bytes, cudaMemcpyHostToDevice, st);
     cudaMemsetAsync(b->flags, 0, sizeof(DeviceFlags), st);
     cudaMemsetAsync(b->queues, 0, N_QUEUES * sizeof(unsigned long long), st);
-    batch_clear_kernel<<<resident_grid(batch_clear_kernel, 256, 8), 256, 0, st>>>(T);
     batch_vertex_kernel<<<resident_grid(batch_vertex_kernel, 128, 16), 128, 0, st>>>(T, b->scr4.p, b->vary.p);
     batch_setup_kernel<<<resident_grid(batch_setup_kernel, 256, 8), 256, 0, st>>>(T, b->scr4.p, b->setup.p, b->area.p,
                                                                                 b->unsafe_list.p, b->flags);
@@ -631,6 +641,7 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     batch_ext_kernel<<<resident_grid(batch_ext_kernel, 256, 4), 256, 0, st>>>(T, b->setup.p, b->unsafe_list.p,
                                                                              b->tlist.p, b->queues, b->flags);
     batch_collect_kernel<<<resident_grid(batch_collect_kernel, 256, 8), 256, 0, st>>>(T, b->tlist.p, b->queues);
+    batch_clear_kernel<<<resident_grid(batch_clear_kernel, 256, 8), 256, 0, st>>>(T);
     for (int fs = 0; fs < FS_COUNT; ++fs)
         for (int fmt = 0; fmt < 3; ++fmt) {
             if (!(b->combos & (1u << (fs * 3 + fmt)))) continue;
@@ -802,7 +813,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         tris += m->n_indices / 3;
         quads += (m->n_verts + 3) / 4;
         blocks += (uint64_t)((p->fb.width + 31) / 32) * ((p->fb.height + 31) / 32);
-        if (it.clear) chunks += (npx + CLEAR_CHUNK - 1) / CLEAR_CHUNK;
+        if (it.clear) chunks += (uint64_t)((p->fb.width + 31) / 32) * ((p->fb.height + 31) / 32);
         px += npx;
     }
     if (slots >= (1ull << 31) || tris >= (1ull << 31) || blocks >= (1ull << 31) || chunks >= (1ull << 31))
@@ -908,7 +919,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         qb[i + 1] = qb[i] + (nothing ? 0u : (m->n_verts + 3) / 4);
         tb[i + 1] = tb[i] + nt;
         bb[i + 1] = bb[i] + (nothing ? 0u : (uint32_t)nblk);
-        cb[i + 1] = cb[i] + (it.clear ? (uint32_t)((npx + CLEAR_CHUNK - 1) / CLEAR_CHUNK) : 0u);
+        cb[i + 1] = cb[i] + (it.clear ? (uint32_t)nblk : 0u);
     }
     b->combos = combos;
     // ---- configuration: forced, tuned for this size class, or the default

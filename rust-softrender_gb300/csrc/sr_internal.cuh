@@ -27,6 +27,7 @@ namespace sr {
 
 constexpr int VSTRIDE = 12;        // varying floats per vertex (10 used at most)
 constexpr int MAX_PLANES = 8;      // attribute planes read by a vertex shader
+constexpr float F32_LOWEST = -3.40282347e+38f;   // f32::MIN, the depth clear value (attachments/depth.rs:31)
 
 enum VsId { VS_MVP_POS_NRM = 0, VS_MVP_POS_NRM_UV = 1, VS_CLIP_COLOR = 2, VS_CLIP_RGBA8 = 3, VS_COUNT };
 enum FsId { FS_BLINN_PHONG_DIR = 0, FS_TEXTURED_BLINN_PHONG = 1, FS_VERTEX_COLOR = 2,

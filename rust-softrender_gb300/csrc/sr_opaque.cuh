@@ -159,14 +159,18 @@ __device__ __forceinline__ void ext_prim(const DrawParams& P, uint32_t t, uint32
 // Resolve of one touched 32x32 block b: each pixel's winning key against the
 // depth the draw started from, barycentrics of the winner recomputed, its
 // varyings interpolated and shaded, colour and depth written once; the keys
-// and the block's bitmap bit are reset for the next draw.
+// and the block's bitmap bit are reset for the next draw.  With `clear_first`
+// the draw follows a clear of its target that has not been written (the
+// batched path defers it): the start depth is the cleared f32::MIN and every
+// pixel without a winner receives the clear colour and depth here.
 template <int FS, int FMT>
 __device__ __forceinline__ void resolve_block(const DrawParams& P, const sr_uniforms& U, uint32_t b, uint32_t N,
                                               const float4* __restrict__ setup, const uint32_t* __restrict__ vidx,
                                               const float* __restrict__ vary, const uint32_t* __restrict__ tex,
                                               void* __restrict__ color, float* __restrict__ depth,
                                               const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
-                                              unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap) {
+                                              unsigned long long* __restrict__ gkeys, uint32_t* __restrict__ bitmap,
+                                              bool clear_first = false, uint4 clear_color = uint4{}) {
     const uint32_t blocks_x = (P.W + 31) >> 5;
     const uint32_t X0 = (b % blocks_x) << 5, Y0 = (b / blocks_x) << 5;
     const uint32_t bw = min(32u, P.W - X0), bh = min(32u, P.H - Y0);
@@ -176,13 +180,23 @@ __device__ __forceinline__ void resolve_block(const DrawParams& P, const sr_unif
         const uint32_t px = X0 + lx, py = Y0 + ly;
         const size_t gi = (size_t)py * P.W + px;
         const unsigned long long k = gkeys[gi];
-        if (k == 0) continue;
-        gkeys[gi] = 0;
-        if (P.has_depth) {
-            const float d0 = depth[gi];
-            if (isnan(d0) || (uint32_t)(k >> 32) < zkey(d0)) continue;
+        bool win = k != 0;
+        if (win) {
+            gkeys[gi] = 0;
+            if (P.has_depth) {
+                const float d0 = clear_first ? F32_LOWEST : depth[gi];
+                if (isnan(d0) || (uint32_t)(k >> 32) < zkey(d0)) win = false;
+            }
+            if (gate_with_stencil && !stencil_test(P.stencil_test, stencil[gi], P.sref)) win = false;
         }
-        if (gate_with_stencil && !stencil_test(P.stencil_test, stencil[gi], P.sref)) continue;
+        if (!win) {
+            if (clear_first) {
+                if (FMT == SR_COLOR_RGBA32F) reinterpret_cast<uint4*>(color)[gi] = clear_color;
+                else if (FMT == SR_COLOR_RGBA8) reinterpret_cast<uint32_t*>(color)[gi] = clear_color.x;
+                if (P.has_depth) depth[gi] = F32_LOWEST;
+            }
+            continue;
+        }
         const uint32_t t = ((uint32_t)(k & 0xffffffffull) - 1u) % N;
         const float4* r = setup + 4 * (size_t)t;
         const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2);

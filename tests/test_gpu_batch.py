@@ -154,6 +154,52 @@ def test_batch_autotune_and_two_batches_in_a_row(built_lib):
         T.free()
 
 
+def test_batch_mixed_clears(built_lib):
+    """One batch where only the even items clear (the clear is deferred past
+    the raster passes and merged into resolve): even targets must equal a
+    draw on a cleared framebuffer, odd ones a draw over the previous output;
+    a target one pixel high renders nothing and is only cleared."""
+    import copy
+    import softrender as sr
+    from softrender import scenes
+    scs = _mix(n=7, seed=13)
+    flat = copy.copy(scs[0])
+    flat.width, flat.height = 50, 1
+    flat.viewport = (0.0, 0.0, 50.0, 1.0, 0.0, 1.0)
+    scs.append(flat)
+    first = _plain(scs)
+    rng = np.random.default_rng(8)
+    second_scs = []
+    for sc in scs:
+        s2 = copy.copy(sc)
+        eye = scenes.random_camera(rng)
+        view = scenes.look_at_rh(eye, (0, 0, 0), (0, 1, 0))
+        s2.uniforms = scenes.make_uniforms(view=view, projection=scenes.perspective(
+            sc.width / sc.height, np.radians(60.0), 0.1, 100.0), camera=eye)
+        second_scs.append(s2)
+    want = []
+    for k, s2 in enumerate(second_scs):
+        if k % 2 == 0:
+            want += _plain([s2])
+        else:
+            want += _plain([s2], initial=[(first[k][0], first[k][1], None)])
+    T = Targets(scs)
+    b = sr.Batch(use_graphs=True, autotune=False)
+    try:
+        b.render([(T.pls[k], T.draws[k], _clear_bytes(sc)) for k, sc in enumerate(scs)])
+        assert b.sync() == 0
+        _same(T.read(), first)
+        for k, s2 in enumerate(second_scs):
+            T.pls[k].set_uniforms(s2.uniforms)
+        b.render([(T.pls[k], T.draws[k], _clear_bytes(s2) if k % 2 == 0 else None)
+                  for k, s2 in enumerate(second_scs)])
+        assert b.sync() == 0
+        _same(T.read(), want)
+    finally:
+        b.destroy()
+        T.free()
+
+
 def test_batch_rejects_ineligible(built_lib):
     import softrender as sr
     from softrender import _abi as A
