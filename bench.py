@@ -167,9 +167,13 @@ def cpu_frame_estimate(scene, every, tiles, tile_begin=0, threads=None):
     t_all = time.perf_counter() - t0
     t_ras = max(0.0, t_all - t_geo)
     frame = t_vs + every * max(0.0, t_geo - t_vs) + every * t_ras * n_tiles / tiles
-    sample = ("every %d-th of %d triangles through vertex+clip GS, rasterised over %d of %d tiles, "
-              "extrapolated linearly to the frame; %.1f s of CPU wall time" % (
-                  every, scene.n_tris, tiles, n_tiles, t_vs + t_geo + t_all))
+    if every == 1 and tiles == n_tiles:
+        sample = ("one full frame: all %d triangles through vertex+clip GS, rasterised over all %d tiles; "
+                  "%.1f s of CPU wall time" % (scene.n_tris, n_tiles, t_vs + t_geo + t_all))
+    else:
+        sample = ("every %d-th of %d triangles through vertex+clip GS, rasterised over %d of %d tiles, "
+                  "extrapolated linearly to the frame; %.1f s of CPU wall time" % (
+                      every, scene.n_tris, tiles, n_tiles, t_vs + t_geo + t_all))
     return frame, sample, threads
 
 
@@ -603,7 +607,7 @@ def main():
         if not args.no_served:
             line["served"] = run_served()
         if not args.no_cpu_baseline:
-            frame_s, sample, threads = cpu_frame_estimate(scene, every=2, tiles=256)
+            frame_s, sample, threads = cpu_frame_estimate(scene, every=1, tiles=510)
             line["cpu_baseline"] = {"value": round(n_tris / frame_s / 1e6, 5), "unit": "Mtris/s",
                                     "cores": threads, "kind": "port", "sample": sample}
     if world > 1:
@@ -625,7 +629,7 @@ def run_reference(args, rank, world):
         cpu_frame_estimate(scene, every=64, tiles=4, tile_begin=4 * i)
     frames, sample, threads = [], "", os.cpu_count()
     for i in range(args.steps):
-        f, sample, threads = cpu_frame_estimate(scene, every=4, tiles=128, tile_begin=128 * i)
+        f, sample, threads = cpu_frame_estimate(scene, every=2, tiles=128, tile_begin=128 * i)
         frames.append(f)
     frame_s = float(np.mean(frames))
     value = n_tris / frame_s / 1e6
