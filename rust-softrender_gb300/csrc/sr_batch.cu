@@ -411,14 +411,22 @@ __global__ void __launch_bounds__(256) batch_raster_big_kernel(BTables T, const 
                 if (!(I.bitmap[bb >> 5] & bit)) atomicOr(I.bitmap + (bb >> 5), bit);
             }
         }
-        const unsigned long long at = area[g];
-        const unsigned long long p0 = (unsigned long long)c * BIG_CHUNK;
-        const unsigned long long p1 = min(at, p0 + BIG_CHUNK);
+        const uint32_t sb = seam_bits(x0, y0, x1, y1, W, H, I.P.tile_w, I.P.tile_h);
+        // bbox pixels of the chunk, row-major; each thread steps its (row,
+        // column) by blockDim pixels instead of dividing per pixel
+        const uint32_t at = (uint32_t)area[g];
+        const uint32_t p0 = c * BIG_CHUNK;
+        const uint32_t p1 = min(at, p0 + BIG_CHUNK);
         const uint32_t t = g - I.tbase;
-        for (unsigned long long q = p0 + threadIdx.x; q < p1; q += blockDim.x) {
-            const uint32_t row = (uint32_t)(q / w), col = (uint32_t)(q - (unsigned long long)row * w);
-            frag_emit(W, H, I.P.tile_w, I.P.tile_h, I.mx, I.my, 3u, I.P.has_depth != 0, r0, r1, r2, t, x0 + col,
+        const uint32_t q0 = p0 + threadIdx.x;
+        uint32_t row = q0 / w, col = q0 - row * w;
+        const uint32_t drow = blockDim.x / w, dcol = blockDim.x - drow * w;
+        for (uint32_t q = q0; q < p1; q += blockDim.x) {
+            frag_emit(W, H, I.P.tile_w, I.P.tile_h, I.mx, I.my, sb, I.P.has_depth != 0, r0, r1, r2, t, x0 + col,
                       y0 + row, I.P.n_raster_host, I.gkeys, nullptr, 0u, 0u, 0u, frags);
+            row += drow;
+            col += dcol;
+            if (col >= w) { col -= w; ++row; }
         }
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);

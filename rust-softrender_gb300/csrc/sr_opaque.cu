@@ -146,10 +146,16 @@ __global__ void __launch_bounds__(RG_THREADS) raster_big_kernel(
                 if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);
             }
         }
-        for (unsigned long long j = threadIdx.x; j < at; j += RG_THREADS) {
-            const uint32_t row = (uint32_t)(j / w), col = (uint32_t)(j - (unsigned long long)row * w);
+        // each thread steps its (row, column) by RG_THREADS bbox pixels
+        // instead of dividing per pixel
+        uint32_t row = threadIdx.x / w, col = threadIdx.x - row * w;
+        const uint32_t drow = RG_THREADS / w, dcol = RG_THREADS - drow * w;
+        for (uint32_t j = threadIdx.x; j < (uint32_t)at; j += RG_THREADS) {
             rg_fragment(P, r0, r1, r2, t, x0 + col, y0 + row, N, gkeys, bitmap, stencil, gate_with_stencil, mx, my,
                         sb, frags);
+            row += drow;
+            col += dcol;
+            if (col >= w) { col -= w; ++row; }
         }
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
