@@ -200,7 +200,8 @@ __device__ __forceinline__ void resolve_block(const DrawParams& P, const sr_unif
         // the key's low word is pass * N + t + 1 with pass < 4 (a pixel lies in
         // at most four semantic tiles)
         uint32_t t = (uint32_t)(k & 0xffffffffull) - 1u;
-        while (t >= N) t -= N;
+#pragma unroll
+        for (int pass = 0; pass < 3; ++pass) t = t >= N ? t - N : t;
         const float4* r = setup + 4 * (size_t)t;
         const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2);
         const float x = (float)px + 0.5f, y = (float)py + 0.5f;
