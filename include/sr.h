@@ -130,6 +130,26 @@ typedef struct sr_pipeline sr_pipeline;
 typedef struct sr_mesh sr_mesh;
 typedef struct sr_texture sr_texture;
 
+/* Re-rendering the outputs of earlier stages, as the reference's duplicate()
+ * does (src/pipeline/stages/geometry.rs:40-54, fragment.rs:118-135: the
+ * duplicate holds copies of the processed vertices and primitives, so a later
+ * change of the uniforms does not reach them).
+ *   SR_REUSE_VERTICES  the vertex-stage outputs of the pipeline's previous
+ *                      draw feed this draw's geometry stage; both draws use a
+ *                      geometry stage (SR_GS_CLIP or SR_GS_NAMED), the same
+ *                      mesh, vertex shader and viewport
+ *                      (GeometryShader::duplicate, then replace/finish)
+ *   SR_REUSE_GEOMETRY  the previous draw's geometry-stage output is rasterised
+ *                      again; primitive type, geometry mode and shader must
+ *                      also match, so only culling, blend, tiles, stencil
+ *                      reference, fragment shader, texture and line
+ *                      anti-aliasing can differ (FragmentShader::duplicate)
+ * A mismatch, no previous draw, or a mesh updated since is SR_EINVAL.  The
+ * stages are skipped while their outputs are still resident and recomputed
+ * from the saved inputs (the earlier uniforms) otherwise: the results are the
+ * same either way. */
+typedef enum sr_reuse { SR_REUSE_NONE = 0, SR_REUSE_VERTICES = 1, SR_REUSE_GEOMETRY = 2 } sr_reuse;
+
 /* One pass of the typestate chain, flattened.  Defaults (sr_draw_init):
  * triangles, no GS, no culling, blend 0 (the `()` blend: replace), 128x128
  * semantic tiles (DEFAULT_TILE_SIZE, fragment.rs:29), stencil ref 0. */
@@ -149,6 +169,7 @@ typedef struct sr_draw {
     const sr_texture* texture;/* texture read by textured fragment shaders         */
     uint32_t tex_filter;      /* sr_filter */
     uint32_t tex_edge;        /* sr_edge */
+    uint32_t reuse;           /* sr_reuse: duplicate() of an earlier stage         */
 } sr_draw;
 
 /* Per-draw counters gathered on the device. */

@@ -8,6 +8,7 @@
 // buffers and replays the draws from the first poisoned one, so the
 // framebuffer always ends up exactly as if capacities had been large enough.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -24,6 +25,13 @@ using namespace sr;
 namespace {
 
 uint32_t bytes_per_color(uint32_t f) { return f == SR_COLOR_RGBA32F ? 16 : f == SR_COLOR_RGBA8 ? 4 : 0; }
+
+// Mesh contents versions, unique across meshes (a freed mesh's address can
+// come back for a new one), checked by sr_draw.reuse.
+uint64_t next_mesh_version() {
+    static std::atomic<uint64_t> v{0};
+    return ++v;
+}
 
 struct ShaderName { const char* name; int stage; int id; };
 const ShaderName kShaders[] = {
@@ -316,6 +324,7 @@ extern "C" SR_API int sr_mesh_upload(const float* const* planes, uint32_t n_plan
         return e == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA;
     }
     m->bytes = pb + n_indices * 4;
+    m->version = next_mesh_version();
     *out = m;
     return SR_OK;
 }
@@ -325,6 +334,7 @@ extern "C" SR_API int sr_mesh_update(sr_mesh* m, const float* const* planes, uin
     if (!m || n_planes != m->n_planes || n_verts != m->n_verts || n_indices != m->n_indices) return SR_EINVAL;
     if ((n_planes && !planes) || (n_indices && !indices)) return SR_EINVAL;
     cudaStream_t st = (cudaStream_t)stream;
+    m->version = next_mesh_version();   // before the copies: a failed update also invalidates
     for (uint32_t j = 0; j < n_planes; ++j)
         SR_CK(cudaMemcpyAsync(m->planes + (size_t)j * m->n_pad, planes[j], (size_t)n_verts * 4, cudaMemcpyHostToDevice, st));
     if (n_indices) SR_CK(cudaMemcpyAsync(m->indices, indices, n_indices * 4, cudaMemcpyHostToDevice, st));
@@ -386,7 +396,9 @@ extern "C" SR_API int sr_texture_free(sr_texture* t) {
 // ================================================================ render
 namespace {
 
-int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
+// `replay`: re-enqueued by sr_sync after an overflow (stage outputs are then
+// always recomputed, from the saved inputs of the draw).
+int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool replay) {
     const sr_draw* d = &pd.d;
     const sr_mesh* m = d->mesh;
     cudaStream_t st = p->stream;
@@ -438,12 +450,36 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
     P.bins_y = (H + (1u << P.bin_h_log2) - 1) >> P.bin_h_log2;
     const uint32_t n_bins = P.bins_x * P.bins_y;
 
-    // per-draw statistics start from zero
-    SR_CK(cudaMemsetAsync(reinterpret_cast<char*>(p->flags) + FLAGS_STATS_OFFSET, 0,
-                          sizeof(DeviceFlags) - FLAGS_STATS_OFFSET, st));
+    // per-draw statistics start from zero; a draw that rasterises the
+    // previous draw's geometry again keeps its geometry counters
+    auto reset_stats = [&](bool keep_geometry) -> int {
+        char* f = reinterpret_cast<char*>(p->flags);
+        if (!keep_geometry) {
+            SR_CK(cudaMemsetAsync(f + FLAGS_STATS_OFFSET, 0, sizeof(DeviceFlags) - FLAGS_STATS_OFFSET, st));
+            return SR_OK;
+        }
+        const size_t a = offsetof(DeviceFlags, triangles_raster), b = offsetof(DeviceFlags, n_gen_tris);
+        const size_t c = offsetof(DeviceFlags, n_unsafe_list);
+        SR_CK(cudaMemsetAsync(f + a, 0, b - a, st));
+        SR_CK(cudaMemsetAsync(f + c, 0, sizeof(DeviceFlags) - c, st));
+        return SR_OK;
+    };
+    // the stage-output buffers before this draw's capacity checks (vertex
+    // store first, then the geometry stage's): a reuse draw skips its
+    // producer stages only if the buffers it reads did not move
+    const void* const out0[6] = {p->scr4.p, p->vary.p, p->clip4.p, p->refs.p, p->lpv.p, p->lpvalid.p};
+    auto outputs_kept = [&]() {
+        const void* const out1[6] = {p->scr4.p, p->vary.p, p->clip4.p, p->refs.p, p->lpv.p, p->lpvalid.p};
+        const size_t n = d->reuse == SR_REUSE_GEOMETRY ? 6 : 3;
+        return d->reuse != SR_REUSE_NONE && p->outputs_intact && !replay &&
+               std::memcmp(out0, out1, n * sizeof(void*)) == 0;
+    };
     p->last_launches = 0;
     p->last_profiled = false;
-    if (nothing) return SR_OK;
+    if (nothing) {
+        p->outputs_intact = false;
+        return reset_stats(false);
+    }
 
     // ---- lines and points (and triangles turned into lines by a named GS)
     const bool named = d->gs_mode == SR_GS_NAMED && d->gs != GS_CLIP;
@@ -460,21 +496,27 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
             (rc2 = p->lpv.ensure(4 * ((size_t)n_out * prim_out + 1))) || (rc2 = p->lpvalid.ensure((size_t)n_out + 1)))
             return rc2;
         VertexStore vs{p->clip4.p, p->scr4.p, p->vary.p, (uint32_t)p->scr4.cap};
+        const bool skip_v = outputs_kept();
+        const bool skip_g = skip_v && d->reuse == SR_REUSE_GEOMETRY;
+        if ((rc2 = reset_stats(skip_g))) return rc2;
+        p->outputs_intact = false;
         cudaEvent_t* ev = p->profiling ? p->ev : nullptr;
         if (ev) cudaEventRecord(ev[0], st);
-        launch_vertex(P, pd.U, m, vs, gs, st);
+        if (!skip_v) launch_vertex(P, pd.vU, m, vs, gs, st);
         if (ev) { cudaEventRecord(ev[1], st); }
         LPV* lv = reinterpret_cast<LPV*>(p->lpv.p);
-        launch_lp_geometry(P, pd.U, m, vs, prim_n, d->gs_mode, (uint32_t)d->gs, lv, p->lpvalid.p, p->flags, st);
+        if (!skip_g)
+            launch_lp_geometry(P, pd.gU, m, vs, prim_n, d->gs_mode, (uint32_t)d->gs, lv, p->lpvalid.p, p->flags, st);
         if (ev) { cudaEventRecord(ev[2], st); cudaEventRecord(ev[3], st); }
         const uint32_t tex_launches = 0;
         const uint32_t* tex = d->texture ? d->texture->data : nullptr;
         const uint32_t ph = launch_lp_raster(P, pd.U, lv, p->lpvalid.p, n_out, prim_out, tex, p->color, p->depth,
                                              p->stencil, p->flags, st);
         if (ev) { cudaEventRecord(ev[4], st); cudaEventRecord(ev[5], st); }
-        p->last_launches = 2 + ph + tex_launches;
+        p->last_launches = (skip_v ? 0 : 1) + (skip_g ? 0 : 1) + ph + tex_launches;
         p->last_profiled = ev != nullptr;
         SR_CK(cudaGetLastError());
+        p->outputs_intact = true;
         return SR_OK;
     }
 
@@ -541,18 +583,27 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
         S = StencilCountArgs{p->st_diff.p, p->st_lines.p, p->st_glob.p};
     }
     VertexStore vs{p->clip4.p, p->scr4.p, p->vary.p, (uint32_t)vslots};
+    const bool skip_v = outputs_kept();
+    const bool skip_g = skip_v && d->reuse == SR_REUSE_GEOMETRY;
+    if ((rc = reset_stats(skip_g))) return rc;
+    p->outputs_intact = false;
 
     // ---- stages, with optional events between them
     cudaEvent_t* ev = p->profiling ? p->ev : nullptr;
     if (ev) cudaEventRecord(ev[0], st);
-    launch_vertex(P, pd.U, m, vs, !indexed, st);
-    uint32_t launches = 1;
+    uint32_t launches = 0;
+    if (!skip_v) {
+        launch_vertex(P, pd.vU, m, vs, !indexed, st);
+        launches += 1;
+    }
     if (ev) cudaEventRecord(ev[1], st);
     const uint32_t* vidx = m->indices;
     if (!indexed) {
-        launch_clip(P, m, vs, p->clip_counts.p, p->clip_offsets.p, p->clip_tmp.p, p->refs.p, p->flags, st);
+        if (!skip_g) {
+            launch_clip(P, m, vs, p->clip_counts.p, p->clip_offsets.p, p->clip_tmp.p, p->refs.p, p->flags, st);
+            launches += 5;
+        }
         vidx = p->refs.p;
-        launches += 5;
     }
     if (ev) cudaEventRecord(ev[2], st);
     launch_setup_bin(P, vidx, vs, p->setup.p, reinterpret_cast<uint32_t*>(p->binrect.p), nullptr, nullptr,
@@ -585,6 +636,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id) {
     p->last_launches = launches;
     p->last_profiled = ev != nullptr;
     SR_CK(cudaGetLastError());
+    p->outputs_intact = true;
     return SR_OK;
 }
 
@@ -607,17 +659,39 @@ extern "C" SR_API int sr_render(sr_pipeline* p, const sr_draw* d) {
     if (vs_nk(d->vs) < fs_min_varyings(d->fs)) return SR_EINVAL;
     if (d->fs == FS_TEXTURED_BLINN_PHONG && !d->texture) return SR_EINVAL;
     if (p->stencil && d->stencil_ref > 255) return SR_EINVAL;
+    // duplicate(): the producing draw must be the previous one, over the same
+    // mesh contents, vertex shader and viewport (and geometry stage)
+    if (d->reuse > SR_REUSE_GEOMETRY) return SR_EINVAL;
+    if (d->reuse != SR_REUSE_NONE) {
+        const sr_draw& q = p->prev.d;
+        if (!p->have_prev || q.mesh != d->mesh || p->prev.mesh_version != m->version || q.vs != d->vs ||
+            std::memcmp(&q.viewport, &d->viewport, sizeof(sr_viewport)) != 0)
+            return SR_EINVAL;
+        if (d->reuse == SR_REUSE_VERTICES && (q.gs_mode == SR_GS_NONE || d->gs_mode == SR_GS_NONE)) return SR_EINVAL;
+        if (d->reuse == SR_REUSE_GEOMETRY &&
+            (q.prim != d->prim || q.gs_mode != d->gs_mode || (d->gs_mode == SR_GS_NAMED && q.gs != d->gs)))
+            return SR_EINVAL;
+    }
     PendingDraw pd;
     pd.d = *d;
     pd.U = p->U;
+    pd.vU = d->reuse != SR_REUSE_NONE ? p->prev.vU : p->U;
+    pd.gU = d->reuse == SR_REUSE_GEOMETRY ? p->prev.gU : p->U;
+    pd.mesh_version = m->version;
     pd.stencil_test = p->stencil_test;
     pd.stencil_op = p->stencil_op;
     pd.stencil_wrap = p->stencil_wrap;
     uint32_t id = (uint32_t)p->pending.size();
     p->pending.push_back(pd);
-    int rc = enqueue_draw(p, pd, id);
-    if (rc != SR_OK) p->pending.pop_back();
-    return rc;
+    int rc = enqueue_draw(p, pd, id, false);
+    if (rc != SR_OK) {
+        p->pending.pop_back();
+        p->outputs_intact = false;
+        return rc;
+    }
+    p->prev = pd;
+    p->have_prev = true;
+    return SR_OK;
 }
 
 namespace {
@@ -682,7 +756,7 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
         SR_CK(cudaStreamSynchronize(p->stream));
         if (status == SR_EOVERFLOW || from >= p->pending.size()) break;
         for (uint32_t i = from; i < p->pending.size(); ++i) {
-            int rc = enqueue_draw(p, p->pending[i], i);
+            int rc = enqueue_draw(p, p->pending[i], i, true);
             if (rc != SR_OK) { status = rc; break; }
         }
         replayed = true;

@@ -808,6 +808,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         if (!p->pending.empty()) return SR_EBUSY;
         if (!seen.insert(p).second) return SR_EINVAL;                       // targets must be distinct
         if (d->prim != SR_PRIM_TRIANGLE || d->gs_mode != SR_GS_NONE || d->blend != BLEND_REPLACE) return SR_EINVAL;
+        if (d->reuse != SR_REUSE_NONE) return SR_EINVAL;
         if (m->n_indices % 3 != 0) return SR_EINVAL;                        // mod.rs:148
         if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT) return SR_EINVAL;
         if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
@@ -874,6 +875,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
             SR_CK(cudaMemsetAsync(p->gkeys.p, 0, p->gkeys.cap * 8, b->stream));
             SR_CK(cudaMemsetAsync(p->bitmap.p, 0, p->bitmap.cap * 4, b->stream));
         }
+        p->have_prev = false;   // sr_draw.reuse after a batch has no previous sr_render to refer to
         BInst& I = hi[i];
         DrawParams& P = I.P;
         P.W = W; P.H = H;

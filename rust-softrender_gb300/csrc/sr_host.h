@@ -35,7 +35,9 @@ struct DevBuf {
 
 struct PendingDraw {
     sr_draw d;
-    sr_uniforms U;
+    sr_uniforms U;              // the fragment stage's uniforms
+    sr_uniforms vU, gU;         // the vertex and geometry stages' (earlier ones under sr_draw.reuse)
+    uint64_t mesh_version;      // of the mesh the vertex outputs derive from
     uint32_t stencil_test, stencil_op, stencil_wrap;
 };
 
@@ -82,6 +84,12 @@ struct sr_pipeline {
     // capacities (elements) requested for the generated geometry
     uint64_t gen_tri_cap = 0, gen_vert_cap = 0, entry_cap = 0;
     std::vector<sr::PendingDraw> pending;
+    // the previous sr_render (what sr_draw.reuse refers to), and whether the
+    // stage-output buffers (vertex store, generated geometry, line/point
+    // vertices) still hold its outputs
+    sr::PendingDraw prev;
+    bool have_prev = false;
+    bool outputs_intact = false;
     struct PendingRead { void* color; float* depth; uint8_t* stencil; };
     std::vector<PendingRead> pending_reads;   // sr_framebuffer_read_async since the last sync
     sr_stats last_stats;

@@ -218,6 +218,7 @@ struct sr_mesh {
     uint32_t* indices;
     uint64_t n_indices;
     uint64_t bytes;
+    uint64_t version;     // bumped by every sr_mesh_update
 };
 
 struct sr_texture {

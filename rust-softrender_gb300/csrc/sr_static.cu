@@ -104,6 +104,7 @@ extern "C" SR_API int sr_render_static(const sr_draw* d, const void* uniforms, s
     if (!d || !fb || !uniforms || uniforms_size != sizeof(sr_uniforms)) return SR_EINVAL;
     if (d->mesh || d->texture) return SR_EINVAL;               // handles are for sr_render
     if (d->prim != SR_PRIM_TRIANGLE || d->gs_mode != SR_GS_NONE || d->blend != BLEND_REPLACE) return SR_EINVAL;
+    if (d->reuse != SR_REUSE_NONE) return SR_EINVAL;           // no previous draw to refer to
     if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT) return SR_EINVAL;
     if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
     if (d->cull > SR_CULL_COUNTER_CLOCKWISE) return SR_EINVAL;

@@ -146,6 +146,7 @@ class Pipeline:
         self.handle = h
         self._uniforms = uniforms
         self._keep = []
+        self._last_outputs = None   # stage outputs of the previous draw (duplicate())
 
     @classmethod
     def from_framebuffer(cls, framebuffer, uniforms=None):
@@ -235,28 +236,50 @@ class Pipeline:
             pass
 
 
+class _Outputs:
+    """The outputs of one vertex (or geometry) stage, shared by a stage object
+    and its duplicates: the first of them to render computes them, the
+    others render from them (sr_draw.reuse)."""
+
+    def __init__(self):
+        self.rendered = False
+
+
+def _copy_draw(d):
+    return A.SrDraw.from_buffer_copy(d)
+
+
 class VertexShader:
     """stages/vertex.rs: run(vs) -> GeometryShader, run_to_fragment(vp, vs) -> FragmentShader."""
 
     def __init__(self, pipeline, draw, keep):
         self.pipeline, self.draw, self.keep = pipeline, draw, keep
 
+    def duplicate(self):
+        """VertexShader::duplicate (vertex.rs:39-50): nothing is processed yet."""
+        return VertexShader(self.pipeline, _copy_draw(self.draw), list(self.keep))
+
     def run(self, vs):
         self.draw.vs = shader_id(vs, A.SR_STAGE_VERTEX)
-        return GeometryShader(self.pipeline, self.draw, self.keep)
+        return GeometryShader(self.pipeline, self.draw, self.keep, _Outputs())
 
     def run_to_fragment(self, viewport, vs):
         self.draw.vs = shader_id(vs, A.SR_STAGE_VERTEX)
         self.draw.gs_mode = A.SR_GS_NONE
         self.draw.viewport = viewport.c()
-        return FragmentShader(self.pipeline, self.draw, self.keep)
+        return FragmentShader(self.pipeline, self.draw, self.keep, None, _Outputs())
 
 
 class GeometryShader:
-    """stages/geometry.rs: clip_primitives(), run(gs), finish(viewport)."""
+    """stages/geometry.rs: clip_primitives(), run(gs) / replace(gs), finish(viewport), duplicate()."""
 
-    def __init__(self, pipeline, draw, keep):
-        self.pipeline, self.draw, self.keep = pipeline, draw, keep
+    def __init__(self, pipeline, draw, keep, vertices):
+        self.pipeline, self.draw, self.keep, self.vertices = pipeline, draw, keep, vertices
+
+    def duplicate(self):
+        """GeometryShader::duplicate (geometry.rs:40-54): a copy that renders
+        from the same processed vertices (SR_REUSE_VERTICES)."""
+        return GeometryShader(self.pipeline, _copy_draw(self.draw), list(self.keep), self.vertices)
 
     def clip_primitives(self):
         self.draw.gs_mode = A.SR_GS_CLIP
@@ -268,16 +291,24 @@ class GeometryShader:
         self.draw.gs = shader_id(gs, A.SR_STAGE_GEOMETRY)
         return self
 
+    replace = run
+
     def finish(self, viewport):
         self.draw.viewport = viewport.c()
-        return FragmentShader(self.pipeline, self.draw, self.keep)
+        return FragmentShader(self.pipeline, self.draw, self.keep, self.vertices, _Outputs())
 
 
 class FragmentShader:
-    """stages/fragment.rs: with_blend, cull_faces, antialiased_lines, tile_size, run."""
+    """stages/fragment.rs: with_blend, cull_faces, antialiased_lines, tile_size, duplicate, run."""
 
-    def __init__(self, pipeline, draw, keep):
+    def __init__(self, pipeline, draw, keep, vertices=None, geometry=None):
         self.pipeline, self.draw, self.keep = pipeline, draw, keep
+        self.vertices, self.geometry = vertices, geometry
+
+    def duplicate(self):
+        """FragmentShader::duplicate (fragment.rs:118-135): the same geometry
+        rasterised again with other settings (SR_REUSE_GEOMETRY)."""
+        return FragmentShader(self.pipeline, _copy_draw(self.draw), list(self.keep), self.vertices, self.geometry)
 
     def with_blend(self, blend):
         self.draw.blend = shader_id(blend, A.SR_STAGE_BLEND)
@@ -313,7 +344,21 @@ class FragmentShader:
 
     def run(self, fs):
         self.draw.fs = shader_id(fs, A.SR_STAGE_FRAGMENT)
+        # reuse what a duplicate rendered, when it was the pipeline's previous
+        # draw (the library keeps the outputs of that draw only)
+        last = self.pipeline._last_outputs
+        reuse = A.SR_REUSE_NONE
+        if self.geometry is not None and self.geometry.rendered and last == (self.vertices, self.geometry):
+            reuse = A.SR_REUSE_GEOMETRY
+        elif (self.vertices is not None and self.vertices.rendered and last is not None and last[0] is self.vertices
+              and self.draw.gs_mode != A.SR_GS_NONE):
+            reuse = A.SR_REUSE_VERTICES
+        self.draw.reuse = reuse
         check(lib().sr_render(self.pipeline.handle, C.byref(self.draw)), "sr_render")
+        for o in (self.vertices, self.geometry):
+            if o is not None:
+                o.rendered = True
+        self.pipeline._last_outputs = (self.vertices, self.geometry)
         self.pipeline._keep.extend(self.keep)
         return self.pipeline
 
@@ -426,6 +471,7 @@ class Batch:
         """entries: (pipeline, SrDraw, clear_bytes or None) -> ctypes array."""
         arr = (A.SrBatchItem * len(entries))()
         for i, (pl, d, clear) in enumerate(entries):
+            pl._last_outputs = None   # a batched draw leaves nothing for duplicate() to reuse
             arr[i].target = pl.handle.value if isinstance(pl.handle, C.c_void_p) else pl.handle
             arr[i].draw = d
             arr[i].clear = 1 if clear is not None else 0

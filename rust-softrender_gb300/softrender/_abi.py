@@ -13,6 +13,7 @@ SR_COLOR_NONE, SR_COLOR_RGBA32F, SR_COLOR_RGBA8 = 0, 1, 2
 SR_PRIM_POINT, SR_PRIM_LINE, SR_PRIM_TRIANGLE = 1, 2, 3
 # sr_gs_mode
 SR_GS_NONE, SR_GS_CLIP, SR_GS_NAMED = 0, 1, 2
+SR_REUSE_NONE, SR_REUSE_VERTICES, SR_REUSE_GEOMETRY = 0, 1, 2   # sr_draw.reuse (duplicate())
 # limits of sr_render_static (its fixed scratch)
 SR_STATIC_MAX_PIXELS, SR_STATIC_MAX_TRIANGLES, SR_STATIC_MAX_VERTICES = 1 << 20, 1 << 16, 1 << 16
 # sr_cull
@@ -65,7 +66,7 @@ class SrDraw(C.Structure):
         ("cull", C.c_uint32), ("fs", C.c_int32), ("blend", C.c_int32),
         ("aa_lines", C.c_uint32), ("tile_w", C.c_uint32), ("tile_h", C.c_uint32),
         ("stencil_ref", C.c_uint32), ("texture", C.c_void_p),
-        ("tex_filter", C.c_uint32), ("tex_edge", C.c_uint32),
+        ("tex_filter", C.c_uint32), ("tex_edge", C.c_uint32), ("reuse", C.c_uint32),
     ]
 
 
