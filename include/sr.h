@@ -255,12 +255,24 @@ SR_API int sr_texture_upload(const uint32_t* rgba8, uint32_t width, uint32_t hei
  * `stream` (NULL: synchronous). */
 SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, uint32_t width, uint32_t height, void* stream);
 SR_API int sr_texture_free(sr_texture* t);
-/* Render to texture: copies an RGBA8 framebuffer's colour plane into a
- * texture of the same size, ordered on the pipeline's stream after its draws
- * (sr_sync the pipeline before draws on other pipelines sample it).  The
- * reference's texture-buffer framebuffers (src/framebuffer/texturebuffer.rs)
- * serve the same purpose. */
+/* An RGBA f32 texture (four floats per texel, r first), sampled by the
+ * textured shaders like the RGBA8 ones but without the /255 conversion. */
+SR_API int sr_texture_upload_rgba32f(const float* rgba, uint32_t width, uint32_t height, sr_texture** out);
+/* Render to texture: copies a framebuffer's colour plane (RGBA8 or RGBA f32)
+ * into a texture of the same size and texel type, ordered on the pipeline's
+ * stream after its draws (sr_sync the pipeline before draws on other
+ * pipelines sample it). */
 SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t);
+/* Texture-buffer colour attachment (src/framebuffer/texturebuffer.rs:13-48,
+ * 111-117, TextureBufferRef: the framebuffer's colour, stored apart from depth
+ * and stencil, read as a texture without a copy): a texture that reads the
+ * pipeline's colour plane in place, RGBA8 or RGBA f32.  It sees the
+ * pipeline's draws once they are complete (sr_sync the pipeline, or draw on
+ * the same stream), stays valid until the pipeline is destroyed, and is
+ * released with sr_texture_free (which leaves the plane alone).  A draw may
+ * not sample the plane it writes, a batch or a server request may not sample
+ * a view at all, and sr_texture_update of a view is refused (SR_EINVAL). */
+SR_API int sr_texture_view_framebuffer(sr_pipeline* p, sr_texture** out);
 
 /* Shader registry: device functions compiled into the library, looked up by
  * name.  Stage is sr_stage.  Names: vertex "mvp_pos_nrm", "mvp_pos_nrm_uv",

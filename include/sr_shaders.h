@@ -372,7 +372,7 @@ SR_HD float sr_aces_component(float x) {
 }
 
 /* ----------------------------------------------------------------- texture
- * Bilinear / nearest sampling of an RGBA8 texture, restating
+ * Bilinear / nearest sampling of an RGBA8 or RGBA f32 texture, restating
  * full_example/src/texture.rs:47-84 (clamp: u.min(1).max(0); wrap: u.fract()).
  * Divergence, documented: the reference reads texel x+1 == width when
  * u*(W-1)+0.5 >= W-1 (an out-of-bounds panic at u == 1); here x+1 and y+1 are
@@ -389,15 +389,29 @@ SR_HD uint32_t sr_clamp_index(float f, uint32_t n) {
     if (f >= (float)(n - 1)) return n - 1;
     return (uint32_t)f;
 }
-SR_HD sr_v4 sr_texel(const uint32_t* tex, uint32_t w, uint32_t x, uint32_t y) {
+/* One texel as RGBA f32: an RGBA8 texel as c/255 per channel
+ * (from_image_texel), an RGBA f32 texel (the colour attachment of an RGBA f32
+ * texture buffer, src/framebuffer/texturebuffer.rs:211-221) as stored. */
+SR_HD sr_v4 sr_texel(const void* tex, uint32_t f32, uint32_t w, uint32_t x, uint32_t y) {
+    const size_t i = (size_t)y * w + x;
+    if (f32) {
 #if defined(__CUDA_ARCH__)
-    return sr_from_rgba8(__ldg(tex + (size_t)y * w + x));
+        const float4 t = __ldg(reinterpret_cast<const float4*>(tex) + i);
+        return sr_make_v4(t.x, t.y, t.z, t.w);
 #else
-    return sr_from_rgba8(tex[(size_t)y * w + x]);
+        const float* t = (const float*)tex + 4 * i;
+        return sr_make_v4(t[0], t[1], t[2], t[3]);
+#endif
+    }
+#if defined(__CUDA_ARCH__)
+    return sr_from_rgba8(__ldg((const uint32_t*)tex + i));
+#else
+    return sr_from_rgba8(((const uint32_t*)tex)[i]);
 #endif
 }
-SR_HD sr_v4 sr_sample_rgba8(const uint32_t* tex, uint32_t w, uint32_t h, float u, float v,
-                            int filter, int edge) {
+/* `f32`: the texture holds RGBA f32 texels, else RGBA8 */
+SR_HD sr_v4 sr_sample(const void* tex, uint32_t f32, uint32_t w, uint32_t h, float u, float v,
+                      int filter, int edge) {
     /* Border: coordinates outside [0, 1] (or NaN) read the border colour,
      * transparent black; inside, sampling is as with clamp. */
     if (edge == SR_EDGE_BORDER) {
@@ -414,7 +428,7 @@ SR_HD sr_v4 sr_sample_rgba8(const uint32_t* tex, uint32_t w, uint32_t h, float u
     if (filter == SR_FILTER_NEAREST) {
         uint32_t x = sr_clamp_index(roundf(u * (float)(w - 1)), w);
         uint32_t y = sr_clamp_index(roundf(v * (float)(h - 1)), h);
-        return sr_texel(tex, w, x, y);
+        return sr_texel(tex, f32, w, x, y);
     }
     float uu = (u * (float)(w - 1)) + 0.5f;
     float vv = (v * (float)(h - 1)) + 0.5f;
@@ -426,10 +440,10 @@ SR_HD sr_v4 sr_sample_rgba8(const uint32_t* tex, uint32_t w, uint32_t h, float u
     float v_opp = 1.0f - v_ratio;
     uint32_t x1 = x + 1 < w ? x + 1 : w - 1;
     uint32_t y1 = y + 1 < h ? y + 1 : h - 1;
-    sr_v4 a = sr_texel(tex, w, x, y);
-    sr_v4 b = sr_texel(tex, w, x1, y);
-    sr_v4 c = sr_texel(tex, w, x, y1);
-    sr_v4 d = sr_texel(tex, w, x1, y1);
+    sr_v4 a = sr_texel(tex, f32, w, x, y);
+    sr_v4 b = sr_texel(tex, f32, w, x1, y);
+    sr_v4 c = sr_texel(tex, f32, w, x, y1);
+    sr_v4 d = sr_texel(tex, f32, w, x1, y1);
     sr_v4 r;
     r.x = (a.x * u_opp + b.x * u_ratio) * v_opp + (c.x * u_opp + d.x * u_ratio) * v_ratio;
     r.y = (a.y * u_opp + b.y * u_ratio) * v_opp + (c.y * u_opp + d.y * u_ratio) * v_ratio;

@@ -34,8 +34,9 @@ class OrDraw(C.Structure):
         ("blend", C.c_char_p), ("aa_lines", C.c_uint32), ("tile_w", C.c_uint32),
         ("tile_h", C.c_uint32), ("stencil_ref", C.c_uint32), ("stencil_test", C.c_uint32),
         ("stencil_op", C.c_uint32), ("stencil_wrap", C.c_uint32),
-        ("texture", C.POINTER(C.c_uint32)), ("tex_w", C.c_uint32), ("tex_h", C.c_uint32),
-        ("tex_filter", C.c_uint32), ("tex_edge", C.c_uint32), ("uniforms", C.c_void_p),
+        ("texture", C.c_void_p), ("tex_w", C.c_uint32), ("tex_h", C.c_uint32),
+        ("tex_filter", C.c_uint32), ("tex_edge", C.c_uint32), ("tex_f32", C.c_uint32),
+        ("uniforms", C.c_void_p),
     ]
 
 
@@ -143,10 +144,14 @@ def _draw(scene, keep):
     d.stencil_ref = scene.stencil_ref
     d.stencil_test, d.stencil_op, d.stencil_wrap = scene.stencil_test, scene.stencil_op, scene.stencil_wrap
     if scene.texture is not None:
-        tex = np.ascontiguousarray(scene.texture, dtype=np.uint32)
+        if np.asarray(scene.texture).dtype == np.float32:     # RGBA f32 texels, (h, w, 4)
+            tex = np.ascontiguousarray(scene.texture, dtype=np.float32)
+            d.tex_f32 = 1
+        else:                                                  # RGBA8 texels, (h, w) uint32
+            tex = np.ascontiguousarray(scene.texture, dtype=np.uint32)
         keep.append(tex)
-        d.texture = tex.ctypes.data_as(C.POINTER(C.c_uint32))
-        d.tex_h, d.tex_w = tex.shape
+        d.texture = tex.ctypes.data
+        d.tex_h, d.tex_w = tex.shape[:2]
     d.tex_filter, d.tex_edge = scene.tex_filter, scene.tex_edge
     d.uniforms = C.addressof(scene.uniforms)
     return d

@@ -132,8 +132,8 @@ sr_v4 run_fs(const Ctx& c, const CV& sv) {
     case FS_BLINN_PHONG_DIR:
         return sr_blinn_phong(U, v4(sv.k), v4(sv.k + 4), v4(U->color));
     case FS_TEXTURED_BLINN_PHONG: {
-        sr_v4 t = sr_sample_rgba8(c.d->texture, c.d->tex_w, c.d->tex_h, sv.k[8], sv.k[9],
-                                  (int)c.d->tex_filter, (int)c.d->tex_edge);
+        sr_v4 t = sr_sample(c.d->texture, c.d->tex_f32, c.d->tex_w, c.d->tex_h, sv.k[8], sv.k[9],
+                            (int)c.d->tex_filter, (int)c.d->tex_edge);
         t = sr_decode_gamma(t, U->gamma);
         return sr_blinn_phong(U, v4(sv.k), v4(sv.k + 4), t);
     }

@@ -39,8 +39,9 @@ typedef struct or_draw {
     uint32_t tile_w, tile_h;
     uint32_t stencil_ref;
     uint32_t stencil_test, stencil_op, stencil_wrap;
-    const uint32_t* texture;      /* RGBA8 texels, may be NULL               */
+    const void* texture;          /* RGBA8 or RGBA f32 texels, may be NULL   */
     uint32_t tex_w, tex_h, tex_filter, tex_edge;
+    uint32_t tex_f32;             /* 1: RGBA f32 texels                      */
     const sr_uniforms* uniforms;  /* derived fields must be filled           */
 } or_draw;
 

@@ -371,8 +371,44 @@ extern "C" SR_API int sr_texture_upload(const uint32_t* rgba8, uint32_t w, uint3
     return SR_OK;
 }
 
+extern "C" SR_API int sr_texture_upload_rgba32f(const float* rgba, uint32_t w, uint32_t h, sr_texture** out) {
+    if (!out || !rgba || w == 0 || h == 0) return SR_EINVAL;
+    *out = nullptr;
+    sr_texture* t = new (std::nothrow) sr_texture();
+    if (!t) return SR_ENOMEM;
+    t->w = w;
+    t->h = h;
+    t->f32 = 1;
+    cudaError_t e = cudaMalloc(&t->data, (size_t)w * h * 16);
+    if (e == cudaSuccess) e = cudaMemcpy(t->data, rgba, (size_t)w * h * 16, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        last_cuda_error() = e;
+        if (t->data) cudaFree(t->data);
+        delete t;
+        return e == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA;
+    }
+    *out = t;
+    return SR_OK;
+}
+
+extern "C" SR_API int sr_texture_view_framebuffer(sr_pipeline* p, sr_texture** out) {
+    if (!p || !out) return SR_EINVAL;
+    *out = nullptr;
+    if (!p->color || (p->fb.color_format != SR_COLOR_RGBA8 && p->fb.color_format != SR_COLOR_RGBA32F))
+        return SR_EINVAL;
+    sr_texture* t = new (std::nothrow) sr_texture();
+    if (!t) return SR_ENOMEM;
+    t->data = static_cast<uint32_t*>(p->color);
+    t->w = p->fb.width;
+    t->h = p->fb.height;
+    t->f32 = p->fb.color_format == SR_COLOR_RGBA32F ? 1u : 0u;
+    t->view = true;
+    *out = t;
+    return SR_OK;
+}
+
 extern "C" SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, uint32_t w, uint32_t h, void* stream) {
-    if (!t || !rgba8 || w != t->w || h != t->h) return SR_EINVAL;
+    if (!t || !rgba8 || w != t->w || h != t->h || t->f32 || t->view) return SR_EINVAL;
     cudaStream_t st = (cudaStream_t)stream;
     SR_CK(cudaMemcpyAsync(t->data, rgba8, (size_t)w * h * 4, cudaMemcpyHostToDevice, st));
     if (!stream) SR_CK(cudaStreamSynchronize(st));
@@ -380,15 +416,18 @@ extern "C" SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, ui
 }
 
 extern "C" SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t) {
-    if (!p || !t || p->fb.color_format != SR_COLOR_RGBA8 || !p->color) return SR_EINVAL;
+    if (!p || !t || t->view || !p->color) return SR_EINVAL;
+    const uint32_t f = p->fb.color_format;
+    if ((f != SR_COLOR_RGBA8 && f != SR_COLOR_RGBA32F) || t->f32 != (f == SR_COLOR_RGBA32F ? 1u : 0u)) return SR_EINVAL;
     if (t->w != p->fb.width || t->h != p->fb.height) return SR_EINVAL;
-    SR_CK(cudaMemcpyAsync(t->data, p->color, (size_t)t->w * t->h * 4, cudaMemcpyDeviceToDevice, p->stream));
+    SR_CK(cudaMemcpyAsync(t->data, p->color, (size_t)t->w * t->h * (t->f32 ? 16 : 4), cudaMemcpyDeviceToDevice,
+                          p->stream));
     return SR_OK;
 }
 
 extern "C" SR_API int sr_texture_free(sr_texture* t) {
     if (!t) return SR_EINVAL;
-    if (t->data) cudaFree(t->data);
+    if (t->data && !t->view) cudaFree(t->data);
     delete t;
     return SR_OK;
 }
@@ -420,7 +459,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
     P.color_format = p->fb.color_format;
     P.draw_id = draw_id;
     P.force_unsafe = p->force_unsafe ? 1u : 0u;
-    if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; }
+    if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; P.tex_f32 = d->texture->f32; }
     P.tex_filter = d->tex_filter; P.tex_edge = d->tex_edge;
     // stencil mode (src/stencil.rs; a missing attachment behaves as `()`)
     uint32_t test = pd.stencil_test, op = pd.stencil_op;
@@ -658,6 +697,8 @@ extern "C" SR_API int sr_render(sr_pipeline* p, const sr_draw* d) {
     if (m->n_planes < (uint32_t)vs_planes(d->vs)) return SR_EINVAL;
     if (vs_nk(d->vs) < fs_min_varyings(d->fs)) return SR_EINVAL;
     if (d->fs == FS_TEXTURED_BLINN_PHONG && !d->texture) return SR_EINVAL;
+    // a texture view may not read the colour plane this draw writes
+    if (d->texture && d->texture->view && d->texture->data == p->color) return SR_EINVAL;
     if (p->stencil && d->stencil_ref > 255) return SR_EINVAL;
     // duplicate(): the producing draw must be the previous one, over the same
     // mesh contents, vertex shader and viewport (and geometry stage)

@@ -816,6 +816,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         if (m->n_planes < (uint32_t)vs_planes(d->vs)) return SR_EINVAL;
         if (vs_nk(d->vs) < batch_min_varyings(d->fs)) return SR_EINVAL;
         if (d->fs == FS_TEXTURED_BLINN_PHONG && !d->texture) return SR_EINVAL;
+        if (d->texture && d->texture->view) return SR_EINVAL;   // another target of the batch may write it
         if (p->stencil && !(p->stencil_test == SR_STENCIL_ALWAYS && p->stencil_op == SR_STENCIL_KEEP)) return SR_EINVAL;
         const uint64_t npx = (uint64_t)p->fb.width * p->fb.height;
         slots += m->n_pad;
@@ -893,7 +894,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         P.color_format = p->fb.color_format;
         P.stencil_test = SR_STENCIL_ALWAYS; P.stencil_op = SR_STENCIL_KEEP; P.stencil_wrap = 1;
         P.force_unsafe = p->force_unsafe ? 1u : 0u;
-        if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; }
+        if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; P.tex_f32 = d->texture->f32; }
         P.tex_filter = d->tex_filter; P.tex_edge = d->tex_edge;
         P.bin_w_log2 = 5; P.bin_h_log2 = 5;
         P.bins_x = (W + 31) >> 5; P.bins_y = (H + 31) >> 5;

@@ -89,6 +89,7 @@ struct DrawParams {
     float vp[6];
     int vs, fs, blend;
     uint32_t tex_w, tex_h, tex_filter, tex_edge;
+    uint32_t tex_f32;             // the texture holds RGBA f32 texels
     uint32_t mode_b;              // exhaustive raster (stencil events gate fragments)
     uint32_t stencil_active;      // stencil plane changes during this draw
     uint32_t draw_id;             // sequence number of the draw since the last sync
@@ -222,8 +223,10 @@ struct sr_mesh {
 };
 
 struct sr_texture {
-    uint32_t* data;
+    uint32_t* data;       // RGBA8 texels, or RGBA f32 texels (4 floats each) when f32
     uint32_t w, h;
+    uint32_t f32;         // 1: RGBA f32 texels
+    bool view;            // reads a pipeline's colour plane in place (data not owned)
 };
 
 // ------------------------------------------------------- grid sizing (host)

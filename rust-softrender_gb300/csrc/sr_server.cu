@@ -264,6 +264,7 @@ extern "C" SR_API int sr_server_submit(sr_server* s, const sr_request* r, uint64
         return SR_EINVAL;
     if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT) return SR_EINVAL;
     if (d->fs == FS_TEXTURED_BLINN_PHONG && !d->texture) return SR_EINVAL;
+    if (d->texture && d->texture->view) return SR_EINVAL;   // batched with targets that may write it
     if (r->width == 0 || r->height == 0 || r->width > 32767 || r->height > 32767) return SR_EINVAL;
     if (r->color_format != SR_COLOR_RGBA8 && r->color_format != SR_COLOR_RGBA32F) return SR_EINVAL;
     Req* q = new (std::nothrow) Req();

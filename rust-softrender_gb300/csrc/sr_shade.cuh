@@ -18,7 +18,7 @@ __device__ __forceinline__ sr_v4 shade_fs(const sr_uniforms& U, const float* k, 
         return sr_blinn_phong(&U, sr_make_v4(k[0], k[1], k[2], k[3]), sr_make_v4(k[4], k[5], k[6], k[7]),
                               sr_make_v4(U.color[0], U.color[1], U.color[2], U.color[3]));
     if (FS == FS_TEXTURED_BLINN_PHONG) {
-        sr_v4 t = sr_sample_rgba8(tex, P.tex_w, P.tex_h, k[8], k[9], (int)P.tex_filter, (int)P.tex_edge);
+        sr_v4 t = sr_sample(tex, P.tex_f32, P.tex_w, P.tex_h, k[8], k[9], (int)P.tex_filter, (int)P.tex_edge);
         t = sr_decode_gamma(t, U.gamma);
         return sr_blinn_phong(&U, sr_make_v4(k[0], k[1], k[2], k[3]), sr_make_v4(k[4], k[5], k[6], k[7]), t);
     }
@@ -39,7 +39,7 @@ __device__ __forceinline__ uint32_t shade_fs_rgba8(const sr_uniforms& U, const f
         return sr_blinn_phong_rgba8(&U, sr_make_v4(k[0], k[1], k[2], k[3]), sr_make_v4(k[4], k[5], k[6], k[7]),
                                     sr_make_v4(U.color[0], U.color[1], U.color[2], U.color[3]));
     if (FS == FS_TEXTURED_BLINN_PHONG) {
-        const sr_v4 t = sr_sample_rgba8(tex, P.tex_w, P.tex_h, k[8], k[9], (int)P.tex_filter, (int)P.tex_edge);
+        const sr_v4 t = sr_sample(tex, P.tex_f32, P.tex_w, P.tex_h, k[8], k[9], (int)P.tex_filter, (int)P.tex_edge);
         return sr_textured_blinn_phong_rgba8(&U, sr_make_v4(k[0], k[1], k[2], k[3]),
                                              sr_make_v4(k[4], k[5], k[6], k[7]), t);
     }

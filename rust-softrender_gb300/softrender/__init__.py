@@ -108,12 +108,34 @@ class Mesh:
 
 
 class Texture:
-    def __init__(self, rgba8):
-        t = np.ascontiguousarray(rgba8, dtype=np.uint32)
+    """A texture read by the textured shaders: (h, w) uint32 RGBA8 texels, or
+    (h, w, 4) float32 RGBA texels."""
+
+    def __init__(self, texels):
         h = C.c_void_p()
-        check(lib().sr_texture_upload(t.ctypes.data, t.shape[1], t.shape[0], C.byref(h)), "sr_texture_upload")
+        if np.asarray(texels).dtype == np.float32:
+            t = np.ascontiguousarray(texels, dtype=np.float32)
+            if t.ndim != 3 or t.shape[2] != 4:
+                raise ValueError("RGBA f32 texels must have shape (h, w, 4)")
+            check(lib().sr_texture_upload_rgba32f(t.ctypes.data, t.shape[1], t.shape[0], C.byref(h)),
+                  "sr_texture_upload_rgba32f")
+        else:
+            t = np.ascontiguousarray(texels, dtype=np.uint32)
+            check(lib().sr_texture_upload(t.ctypes.data, t.shape[1], t.shape[0], C.byref(h)), "sr_texture_upload")
         self.handle = h
         self.width, self.height = t.shape[1], t.shape[0]
+
+    @classmethod
+    def view(cls, pipeline):
+        """The pipeline's colour attachment read in place as a texture
+        (texture-buffer framebuffers, src/framebuffer/texturebuffer.rs)."""
+        h = C.c_void_p()
+        check(lib().sr_texture_view_framebuffer(pipeline.handle, C.byref(h)), "sr_texture_view_framebuffer")
+        t = cls.__new__(cls)
+        t.handle = h
+        t.width, t.height = pipeline.framebuffer.width, pipeline.framebuffer.height
+        t._pipeline = pipeline   # the plane it reads lives as long as the pipeline
+        return t
 
     def update(self, rgba8, stream_ptr=None):
         t = np.ascontiguousarray(rgba8, dtype=np.uint32)

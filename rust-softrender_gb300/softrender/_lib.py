@@ -35,6 +35,8 @@ SIGNATURES = {
     "sr_texture_update": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]),
     "sr_texture_free": (C.c_int, [C.c_void_p]),
     "sr_texture_from_framebuffer": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "sr_texture_upload_rgba32f": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.POINTER(C.c_void_p)]),
+    "sr_texture_view_framebuffer": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p)]),
     "sr_shader_lookup": (C.c_int, [C.c_char_p, C.c_int, C.POINTER(C.c_int)]),
     "sr_draw_init": (None, [C.POINTER(A.SrDraw)]),
     "sr_render": (C.c_int, [C.c_void_p, C.POINTER(A.SrDraw)]),

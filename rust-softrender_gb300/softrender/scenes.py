@@ -130,7 +130,7 @@ class Scene:
     stencil_wrap: int = 1
     viewport: tuple = None
     uniforms: A.SrUniforms = None
-    texture: Optional[np.ndarray] = None      # (h, w) uint32 RGBA8
+    texture: Optional[np.ndarray] = None      # (h, w) uint32 RGBA8 or (h, w, 4) float32 RGBA
     tex_filter: int = A.SR_SAMPLE_BILINEAR
     tex_edge: int = A.SR_SAMPLE_CLAMP
     clear_color: tuple = (0.0, 0.0, 0.0, 1.0)

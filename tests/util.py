@@ -19,18 +19,24 @@ def ulp_diff_f32(a, b):
 
 
 def assert_bitexact(name, got, want):
+    """Bit for bit, except that for f32 data any NaN matches any NaN: IEEE 754
+    leaves the payload of a produced NaN open (the GPU writes the canonical
+    NaN, x86 keeps the sign and quiet bit of its default NaN)."""
     if got is None and want is None:
         return
     got = np.asarray(got)
     want = np.asarray(want)
     assert got.shape == want.shape, (name, got.shape, want.shape)
-    gb = got.view(np.uint8) if got.dtype != np.uint8 else got
-    wb = want.view(np.uint8) if want.dtype != np.uint8 else want
-    if not np.array_equal(gb, wb):
-        if got.dtype == np.float32:
-            bad = np.argwhere(ulp_diff_f32(got, want) != 0)
-        else:
-            bad = np.argwhere(got != want)
+    if got.dtype == np.float32 and want.dtype == np.float32:
+        got = np.ascontiguousarray(got)
+        want = np.ascontiguousarray(want)
+        differ = (got.view(np.uint32) != want.view(np.uint32)) & ~(np.isnan(got) & np.isnan(want))
+    else:
+        gb = got.view(np.uint8) if got.dtype != np.uint8 else got
+        wb = want.view(np.uint8) if want.dtype != np.uint8 else want
+        differ = None if np.array_equal(gb, wb) else (got != want)
+    if differ is not None and differ.any():
+        bad = np.argwhere(differ)
         first = tuple(bad[0]) if len(bad) else None
         raise AssertionError("%s differs at %d positions; first %s got %r want %r" % (
             name, len(bad), first, got[first] if first else None, want[first] if first else None))
