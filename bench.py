@@ -415,6 +415,44 @@ def run_frames():
     return out
 
 
+def profile_batched(args):
+    """The batched leg's draws alone, for launch lists and ncu captures: the
+    first N instances of the batched workload rendered as one batch with the
+    launch configuration the tuner picks for the full workload (32 primitives
+    per warp, large-primitive threshold 2048, 8 raster CTAs per SM)."""
+    import softrender as sr
+    from softrender import scenes
+    inst = scenes.batch_instances()[:args.profile_batched]
+    T = []
+    for sc in inst:
+        fb = sr.Framebuffer(sc.width, sc.height, sc.color_format, sc.depth, sc.stencil)
+        pl = sr.Pipeline.from_framebuffer(fb, sc.uniforms)
+        m = sr.Mesh(sc.planes, sc.indices)
+        T.append((pl, m, sr.draw_for_scene(sc, m), sc))
+    b = sr.Batch(use_graphs=False, autotune=False)
+    b.set_config(32, 2048, 8)
+    arr = b.items([(pl, d, sc.clear_bytes()) for pl, m, d, sc in T])
+    for _ in range(args.warmup):
+        if b.render_items(arr) != 0 or b.sync() != 0:
+            raise RuntimeError("batch failed")
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        if b.render_items(arr) != 0:
+            raise RuntimeError("batch failed")
+    if b.sync() != 0:
+        raise RuntimeError("batch failed")
+    ms = (time.perf_counter() - t0) / max(1, args.steps) * 1e3
+    st = b.stats()
+    print(json.dumps({"profile": "batched", "instances": len(inst), "ms_per_batch": round(ms, 3),
+                      "triangles": int(sum(sc.n_tris for sc in inst)),
+                      "pixels": int(sum(sc.width * sc.height for sc in inst)),
+                      "fragments": int(st["fragments"]), "kernel_launches": int(st["kernel_launches"])}))
+    b.destroy()
+    for pl, m, d, sc in T:
+        pl.destroy()
+        m.free()
+
+
 def _timed(fn):
     t0 = time.perf_counter()
     fn()
@@ -553,8 +591,14 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-draws measurement")
     ap.add_argument("--no-frames", action="store_true", help="skip the small and stress frame measurements")
     ap.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--profile-batched", type=int, default=0, metavar="N",
+                    help="profiling aid: render the first N batched instances (--warmup untimed and --steps timed "
+                         "batches, fixed launch configuration, no tuner, no graphs) and print their timing only")
     args = ap.parse_args()
     rank, world, local = dist_env()
+    if args.profile_batched:
+        profile_batched(args)
+        return
 
     if args.impl == "reference":
         run_reference(args, rank, world)
