@@ -99,6 +99,13 @@ __device__ __forceinline__ void out_tri(const Poly& P, int k, int& i0, int& i1, 
 
 __device__ __forceinline__ int n_out_tris(const Poly& P) { return P.n == 3 ? 1 : (P.n > 3 ? P.n - 2 : 0); }
 
+// A triangle inside every plane (all inside masks 0x3f): the push loop yields
+// the polygon b x6, c x6, a x6 and its fan from the last entry (a) the 16
+// triangles (a, P[k], P[k+1]); only k = 5, (a, b, c), is not degenerate.
+constexpr uint32_t ALL_INSIDE = 0x3fu;
+constexpr int INSIDE_OUT_TRIS = 16;
+__device__ __forceinline__ int inside_poly_vertex(int j) { return j < 6 ? 1 : (j < 12 ? 2 : 0); }
+
 __device__ __forceinline__ bool out_tri_degenerate(const Poly& P, int k) {
     int i0, i1, i2;
     out_tri(P, k, i0, i1, i2);
@@ -124,15 +131,20 @@ __global__ void __launch_bounds__(256) clip_count_kernel(uint32_t n_in, uint32_t
         uint32_t mk[3];
 #pragma unroll
         for (int j = 0; j < 3; ++j) mk[j] = inside_mask(__ldg(clip4 + __ldg(idx + 3 * t + j)));
-        Poly P;
-        build_poly(mk, P);
-        int nv = 0;
-        for (int i = 0; i < P.n; ++i) nv += (P.e[i] & 0x80) ? 1 : 0;
-        int no = n_out_tris(P);
-        int kept = 0;
-        for (int k = 0; k < no; ++k) kept += (keep_degenerate || !out_tri_degenerate(P, k)) ? 1 : 0;
-        counts[t] = ((unsigned long long)nv << 32) | (unsigned long long)kept;
-        gen = (unsigned long long)no;
+        if ((mk[0] & mk[1] & mk[2]) == ALL_INSIDE) {
+            counts[t] = keep_degenerate ? (unsigned long long)INSIDE_OUT_TRIS : 1ull;
+            gen = INSIDE_OUT_TRIS;
+        } else {
+            Poly P;
+            build_poly(mk, P);
+            int nv = 0;
+            for (int i = 0; i < P.n; ++i) nv += (P.e[i] & 0x80) ? 1 : 0;
+            int no = n_out_tris(P);
+            int kept = 0;
+            for (int k = 0; k < no; ++k) kept += (keep_degenerate || !out_tri_degenerate(P, k)) ? 1 : 0;
+            counts[t] = ((unsigned long long)nv << 32) | (unsigned long long)kept;
+            gen = (unsigned long long)no;
+        }
     }
     // block-reduce the number of generated primitives for the statistics
     __shared__ unsigned long long s_gen;
@@ -182,6 +194,24 @@ __global__ void __launch_bounds__(256) clip_emit_kernel(uint32_t n_in, uint32_t 
     for (int j = 0; j < 3; ++j) {
         c[j] = __ldg(clip4 + vi[j]);
         mk[j] = inside_mask(c[j]);
+    }
+    if ((mk[0] & mk[1] & mk[2]) == ALL_INSIDE) {   // no intersections; see inside_poly_vertex
+        if (!keep_degenerate) {
+            if (toff < gen_tri_cap) {
+                refs[3 * (size_t)toff + 0] = vi[0];
+                refs[3 * (size_t)toff + 1] = vi[1];
+                refs[3 * (size_t)toff + 2] = vi[2];
+            }
+            return;
+        }
+        for (int k = 0; k < INSIDE_OUT_TRIS; ++k) {
+            const uint32_t o = toff + (uint32_t)k;
+            if (o >= gen_tri_cap) break;
+            refs[3 * (size_t)o + 0] = vi[0];
+            refs[3 * (size_t)o + 1] = vi[inside_poly_vertex(k)];
+            refs[3 * (size_t)o + 2] = vi[inside_poly_vertex(k + 1)];
+        }
+        return;
     }
     Poly P;
     build_poly(mk, P);

@@ -116,6 +116,21 @@ def test_stencil_exhaustive(built_lib, oracle_mod, test_op):
     check(sc, oracle_mod, initial=(None, None, st0))
 
 
+@pytest.mark.parametrize("which", ["icosphere", "gridsphere"])
+def test_clip_keeps_degenerate_under_stencil(built_lib, oracle_mod, which):
+    """Clip geometry shader with stencil counting: the 15 degenerate fan
+    triangles of each inside triangle stay (their bbox pixels are stencil
+    events).  The icosphere lies inside every plane; the grid-sphere camera
+    makes a share of the triangles cross planes."""
+    kw = dict(stencil=True, stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT, stencil_wrap=1)
+    if which == "icosphere":
+        sc = scenes.icosphere_scene(160, 120, subdiv=2, gs_mode=A.SR_GS_CLIP, tile=(40, 32), **kw)
+    else:
+        sc = scenes.grid_sphere_scene(width=192, height=108, n_lat=16, n_lon=32, tex_size=32, tile=(48, 40), **kw)
+    stats, ostats = check(sc, oracle_mod)
+    assert stats["triangles_generated"] == ostats["triangles_generated"]
+
+
 def test_blend_over_f32(built_lib, oracle_mod):
     sc = scenes.stress_scene(n_tiny=1500, n_large=20, size=128, tile=(48, 40))
     sc.color_format = A.SR_COLOR_RGBA32F
