@@ -81,34 +81,42 @@ __global__ void scan_blocks_kernel(T* block_sums, uint32_t nb) {
     if (threadIdx.x == 0) block_sums[nb] = tot;
 }
 
-// out[j] = exclusive prefix of in; out[n] = total.  Elements are assigned
-// blocked-per-thread so each thread scans SCAN_ITEMS consecutive values.
+// Shared-memory slot of tile element e, padded by one element per 128 bytes
+// so that the blocked-per-thread accesses (thread t reads elements
+// t * SCAN_ITEMS ..) fall into distinct banks.
+template <typename T>
+__device__ __forceinline__ int scan_slot(int e) { return e + (e >> (sizeof(T) == 8 ? 4 : 5)); }
+template <typename T>
+constexpr int scan_tile_slots() { return SCAN_TILE + (SCAN_TILE >> (sizeof(T) == 8 ? 4 : 5)); }
+
+// out[j] = exclusive prefix of in; out[n] = total.  Loads and stores are
+// coalesced; in between, each thread scans SCAN_ITEMS consecutive values.
 template <typename T>
 __global__ void scan_apply_kernel(const T* __restrict__ in, uint64_t n, const T* __restrict__ block_sums,
                                   uint32_t nb, T* __restrict__ out) {
-    __shared__ T tile[SCAN_TILE];
+    __shared__ T tile[scan_tile_slots<T>()];
     uint64_t base = (uint64_t)blockIdx.x * SCAN_TILE;
     for (int i = 0; i < SCAN_ITEMS; ++i) {
         uint64_t j = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
-        tile[i * SCAN_THREADS + threadIdx.x] = j < n ? in[j] : T(0);
+        tile[scan_slot<T>(i * SCAN_THREADS + threadIdx.x)] = j < n ? in[j] : T(0);
     }
     __syncthreads();
     T v[SCAN_ITEMS];
     T s = 0;
     for (int i = 0; i < SCAN_ITEMS; ++i) {
-        v[i] = tile[threadIdx.x * SCAN_ITEMS + i];
+        v[i] = tile[scan_slot<T>(threadIdx.x * SCAN_ITEMS + i)];
         s += v[i];
     }
     T tot;
     T ex = block_exclusive_scan<T, SCAN_THREADS>(s, &tot) + block_sums[blockIdx.x];
     for (int i = 0; i < SCAN_ITEMS; ++i) {
-        tile[threadIdx.x * SCAN_ITEMS + i] = ex;
+        tile[scan_slot<T>(threadIdx.x * SCAN_ITEMS + i)] = ex;
         ex += v[i];
     }
     __syncthreads();
     for (int i = 0; i < SCAN_ITEMS; ++i) {
         uint64_t j = base + (uint64_t)i * SCAN_THREADS + threadIdx.x;
-        if (j < n) out[j] = tile[i * SCAN_THREADS + threadIdx.x];
+        if (j < n) out[j] = tile[scan_slot<T>(i * SCAN_THREADS + threadIdx.x)];
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = block_sums[nb];
 }
