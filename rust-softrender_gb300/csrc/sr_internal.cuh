@@ -208,6 +208,38 @@ __device__ __forceinline__ bool segment_cleared(float4 r0, float4 r1, uint32_t x
     return cw;
 }
 
+// The same sign test over the pixel rectangle [x0, x1] x [y0, y1]: the
+// numerators and det - N_u - N_v are affine and their error bounds S convex,
+// so the four corners decide (each bound taken at its largest corner).
+__device__ __forceinline__ bool rect_cleared(float4 r0, float4 r1, int x0, int y0, int x1, int y1) {
+    const float g = 5.0e-7f;
+    const float eps = 6.0e-8f;
+    const float det = r1.z;
+    const float s = det > 0.0f ? 1.0f : -1.0f;
+    float nu[4], nv[4], su = 0.0f, sv = 0.0f, mu = 0.0f, mv = 0.0f;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const float dx = ((float)((e & 1) ? x1 : x0) + 0.5f) - r1.x;
+        const float dy = ((float)((e & 2) ? y1 : y0) + 0.5f) - r1.y;
+        nu[e] = r0.x * dx + r0.y * dy;
+        nv[e] = r0.z * dx + r0.w * dy;
+        su = fmaxf(su, fabsf(r0.x) * fabsf(dx) + fabsf(r0.y) * fabsf(dy));
+        sv = fmaxf(sv, fabsf(r0.z) * fabsf(dx) + fabsf(r0.w) * fabsf(dy));
+        mu = fmaxf(mu, fabsf(nu[e]));
+        mv = fmaxf(mv, fabsf(nv[e]));
+    }
+    const float tiny = fabsf(det) * 1.0e-30f;
+    bool cu = true, cv = true, cw = true;
+    const float mw = 2.0f * g * (su + sv) + 16.0f * eps * (fabsf(det) + mu + mv);
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        cu = cu && (s * nu[e] + g * su + tiny < 0.0f);
+        cv = cv && (s * nv[e] + g * sv + tiny < 0.0f);
+        cw = cw && (s * (det - nu[e] - nv[e]) + mw < 0.0f);
+    }
+    return cu || cv || cw;
+}
+
 }  // namespace sr
 
 // Opaque handles of the C ABI

@@ -157,8 +157,15 @@ __global__ void __launch_bounds__(ORD_THREADS) raster_ordered_kernel(
                     const int bx0 = (int)(bx * BW), by0 = (int)(by * BH);
                     const int x0 = max(__float_as_int(r3.x), bx0), x1 = min(__float_as_int(r3.z), bx0 + (int)BW - 1);
                     const int y0 = max(__float_as_int(r3.y), by0), y1 = min(__float_as_int(r3.w), by0 + (int)BH - 1);
-                    if (P.mode_b || (fl & REC_UNSAFE) || (x1 - x0 + 1) * (y1 - y0 + 1) > 16) {
+                    if (P.mode_b || (fl & REC_UNSAFE)) {
                         atomicOr(&lmask[wi], bit);
+                    } else if ((x1 - x0 + 1) * (y1 - y0 + 1) > 16) {
+                        // a safe primitive touches only covered pixels of its
+                        // bbox here (stencil events are counted apart unless in
+                        // mode B): one whose sign test clears the bin part of
+                        // its bbox is dropped for the whole bin
+                        if (!rect_cleared(rec[threadIdx.x][0], rec[threadIdx.x][1], x0, y0, x1, y1))
+                            atomicOr(&lmask[wi], bit);
                     } else if (x0 <= x1 && y0 <= y1) {
                         for (int yy = y0; yy <= y1; ++yy)
                             for (int xx = x0; xx <= x1; ++xx)
