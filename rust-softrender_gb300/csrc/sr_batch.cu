@@ -802,7 +802,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
     if (n > (1u << 20)) return SR_EINVAL;
     // ---- validation (nothing is enqueued unless every item is acceptable)
     std::unordered_set<const sr_pipeline*> seen;
-    uint64_t slots = 0, tris = 0, quads = 0, blocks = 0, chunks = 0, px = 0;
+    uint64_t slots = 0, tris = 0, quads = 0, blocks = 0, clear_blocks = 0, px = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const sr_batch_item& it = items[i];
         const sr_pipeline* p = it.target;
@@ -827,10 +827,10 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         tris += m->n_indices / 3;
         quads += (m->n_verts + 3) / 4;
         blocks += (uint64_t)((p->fb.width + 31) / 32) * ((p->fb.height + 31) / 32);
-        if (it.clear) chunks += (uint64_t)((p->fb.width + 31) / 32) * ((p->fb.height + 31) / 32);
+        if (it.clear) clear_blocks += (uint64_t)((p->fb.width + 31) / 32) * ((p->fb.height + 31) / 32);
         px += npx;
     }
-    if (slots >= (1ull << 31) || tris >= (1ull << 31) || blocks >= (1ull << 31) || chunks >= (1ull << 31))
+    if (slots >= (1ull << 31) || tris >= (1ull << 31) || blocks >= (1ull << 31) || clear_blocks >= (1ull << 31))
         return SR_EINVAL;
     // the host table is reused: the previous batch must have consumed it
     if (b->in_flight) {
