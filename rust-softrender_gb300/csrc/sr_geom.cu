@@ -161,7 +161,7 @@ __global__ void __launch_bounds__(256) clip_count_kernel(uint32_t n_in, uint32_t
 __device__ __forceinline__ float lerp1(float t, float x1, float x2) { return (1.0f - t) * x1 + t * x2; }
 
 __global__ void __launch_bounds__(256) clip_emit_kernel(uint32_t n_in, uint32_t n_verts, uint32_t keep_degenerate,
-                                                        uint32_t draw_id,
+                                                        uint32_t draw_id, int nkq,
                                                         VpMatrix vpm,
                                                         uint32_t gen_base, uint32_t gen_tri_cap,
                                                         uint32_t gen_vert_cap,
@@ -247,7 +247,7 @@ __global__ void __launch_bounds__(256) clip_emit_kernel(uint32_t n_in, uint32_t 
         const float4* kb = reinterpret_cast<const float4*>(vary + (size_t)vi[pi] * VSTRIDE);
         float4* ko = reinterpret_cast<float4*>(vary + (size_t)(gen_base + g) * VSTRIDE);
 #pragma unroll
-        for (int q = 0; q < VSTRIDE / 4; ++q) {
+        for (int q = 0; q < nkq; ++q) {   // the vertex shader's varyings
             float4 x = ka[q], y = kb[q];
             ko[q] = make_float4(lerp1(tt, x.x, y.x), lerp1(tt, x.y, y.y), lerp1(tt, x.z, y.z), lerp1(tt, x.w, y.w));
         }
@@ -274,7 +274,8 @@ void launch_clip(const DrawParams& P, const sr_mesh* m, VertexStore vs, unsigned
     clip_count_kernel<<<grid, block, 0, st>>>(n, P.n_verts, P.keep_degenerate, m->indices, vs.clip4, counts, flags);
     exclusive_scan<unsigned long long>(counts, n, offsets, scan_tmp, st);
     VpMatrix vpm = viewport_matrix(P.vp);
-    clip_emit_kernel<<<grid, block, 0, st>>>(n, P.n_verts, P.keep_degenerate, P.draw_id, vpm, P.gen_base, P.gen_tri_cap, P.gen_vert_cap,
+    clip_emit_kernel<<<grid, block, 0, st>>>(n, P.n_verts, P.keep_degenerate, P.draw_id, (vs_nk(P.vs) + 3) / 4, vpm,
+                                             P.gen_base, P.gen_tri_cap, P.gen_vert_cap,
                                              m->indices, vs.clip4, vs.scr4, vs.vary, offsets, refs, flags);
 }
 

@@ -36,7 +36,7 @@ enum BlendId { BLEND_REPLACE = 0, BLEND_OVER = 1, BLEND_COUNT };
 enum GsId { GS_CLIP = 0, GS_VERTEX_NORMALS = 1, GS_FACE_NORMALS = 2, GS_COUNT };
 
 __host__ __device__ inline int vs_planes(int vs) { return vs == VS_MVP_POS_NRM ? 6 : vs == VS_CLIP_RGBA8 ? 4 : 8; }
-__host__ __device__ inline int vs_nk(int vs) { return vs == VS_MVP_POS_NRM ? 8 : vs == VS_MVP_POS_NRM_UV ? 10 : 4; }
+__host__ __device__ constexpr int vs_nk(int vs) { return vs == VS_MVP_POS_NRM ? 8 : vs == VS_MVP_POS_NRM_UV ? 10 : 4; }
 
 // Device error / counter block (one per pipeline).  The first part persists
 // until sr_sync; the statistics part is zeroed at the start of every draw.

@@ -28,6 +28,8 @@ struct LPV {
     float4 k0, k1, k2;   // varyings
 };
 
+// All three varying quads of a vertex slot; those beyond the vertex shader's
+// varyings are not written by the vertex stage and are carried along unused.
 __device__ __forceinline__ void load_k(const float* __restrict__ vary, uint32_t slot, float4& a, float4& b, float4& c) {
     const float4* q = reinterpret_cast<const float4*>(vary + (size_t)slot * VSTRIDE);
     a = __ldg(q);

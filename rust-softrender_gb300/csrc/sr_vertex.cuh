@@ -49,10 +49,13 @@ __device__ __forceinline__ void vertex_quad(uint32_t q, uint32_t n_verts, uint32
         if (clip4) clip4[v] = make_float4(c.x, c.y, c.z, c.w);
         sr_v4 s = normalize_pos(c, vpm.m);
         scr4[v] = make_float4(s.x, s.y, s.z, s.w);
+        // only the shader's varyings are written (readers never go beyond
+        // them: each fragment shader's are validated against the vertex shader's)
+        constexpr int NKQ = (vs_nk(VS) + 3) / 4;
         float4* vo = reinterpret_cast<float4*>(vary + (size_t)v * VSTRIDE);
         vo[0] = make_float4(k[0], k[1], k[2], k[3]);
-        vo[1] = make_float4(k[4], k[5], k[6], k[7]);
-        vo[2] = make_float4(k[8], k[9], k[10], k[11]);
+        if (NKQ > 1) vo[1] = make_float4(k[4], k[5], k[6], k[7]);
+        if (NKQ > 2) vo[2] = make_float4(k[8], k[9], k[10], k[11]);
     }
 }
 
