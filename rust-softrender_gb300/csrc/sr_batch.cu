@@ -3,7 +3,7 @@
 // rendered by one launch per stage instead of one set of launches per draw.
 //
 // Every stage is a persistent kernel (a fixed grid sized to the GPU) that
-// pulls work items from the flattened (instance, item) space: vertex quads,
+// pulls work items from the flattened (instance, item) space: vertices,
 // primitives, 32x32 resolve blocks and 32x32 clear blocks.  An item's
 // instance is found by binary search over per-instance exclusive prefix sums
 // (once per warp where a warp's items are consecutive).  A cleared target is
@@ -58,7 +58,7 @@ struct BTables {
     const uint32_t* n;            // number of draws in this batch
     const BInst* inst;
     const sr_uniforms* U;
-    const uint32_t* qbase;        // exclusive prefix of vertex quads        (NB + 1)
+    const uint32_t* qbase;        // exclusive prefix of vertices            (NB + 1)
     const uint32_t* tbase;        // exclusive prefix of primitives          (NB + 1)
     const uint32_t* bbase;        // exclusive prefix of 32x32 resolve blocks (NB + 1)
     const uint32_t* cbase;        // exclusive prefix of 32x32 clear blocks  (NB + 1)
@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(128) batch_vertex_kernel(BTables T, float4* __
     const uint32_t n = *T.n;
     const uint32_t total = __ldg(T.qbase + n);
     const uint32_t lane = threadIdx.x & 31;
-    // a warp takes 32 consecutive quads per round; lane 0 finds the draw
+    // a warp takes 32 consecutive vertices per round; lane 0 finds the draw
     for (uint32_t jw = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); jw < total; jw += gridDim.x * blockDim.x) {
         uint32_t i0 = 0;
         if (lane == 0) i0 = owner_of(T.qbase, n, jw);
@@ -140,14 +140,14 @@ __global__ void __launch_bounds__(128) batch_vertex_kernel(BTables T, float4* __
         if (j >= total) continue;
         const uint32_t i = owner_from(T.qbase, n, i0, j);
         const BInst& I = T.inst[i];
-        const uint32_t q = j - __ldg(T.qbase + i);
+        const uint32_t v = j - __ldg(T.qbase + i);
         float4* s4 = scr4 + I.vbase;
         float* vy = vary + (size_t)I.vbase * VSTRIDE;
         switch (I.P.vs) {
-        case VS_MVP_POS_NRM: vertex_quad<VS_MVP_POS_NRM>(q, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
-        case VS_MVP_POS_NRM_UV: vertex_quad<VS_MVP_POS_NRM_UV>(q, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
-        case VS_CLIP_COLOR: vertex_quad<VS_CLIP_COLOR>(q, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
-        default: vertex_quad<VS_CLIP_RGBA8>(q, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
+        case VS_MVP_POS_NRM: vertex_one<VS_MVP_POS_NRM>(v, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
+        case VS_MVP_POS_NRM_UV: vertex_one<VS_MVP_POS_NRM_UV>(v, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
+        case VS_CLIP_COLOR: vertex_one<VS_CLIP_COLOR>(v, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
+        default: vertex_one<VS_CLIP_RGBA8>(v, I.P.n_verts, I.n_pad, T.U[i], I.vpm, I.planes, nullptr, s4, vy); break;
         }
     }
 }
@@ -802,7 +802,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
     if (n > (1u << 20)) return SR_EINVAL;
     // ---- validation (nothing is enqueued unless every item is acceptable)
     std::unordered_set<const sr_pipeline*> seen;
-    uint64_t slots = 0, tris = 0, quads = 0, blocks = 0, clear_blocks = 0, px = 0;
+    uint64_t slots = 0, tris = 0, blocks = 0, clear_blocks = 0, px = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const sr_batch_item& it = items[i];
         const sr_pipeline* p = it.target;
@@ -825,7 +825,6 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         const uint64_t npx = (uint64_t)p->fb.width * p->fb.height;
         slots += m->n_pad;
         tris += m->n_indices / 3;
-        quads += (m->n_verts + 3) / 4;
         blocks += (uint64_t)((p->fb.width + 31) / 32) * ((p->fb.height + 31) / 32);
         if (it.clear) clear_blocks += (uint64_t)((p->fb.width + 31) / 32) * ((p->fb.height + 31) / 32);
         px += npx;
@@ -931,7 +930,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         hu[i] = p->U;
         if (!nothing) combos |= 1u << (d->fs * 3 + (int)p->fb.color_format);
         vbase += m->n_pad;
-        qb[i + 1] = qb[i] + (nothing ? 0u : (m->n_verts + 3) / 4);
+        qb[i + 1] = qb[i] + (nothing ? 0u : m->n_verts);
         tb[i + 1] = tb[i] + nt;
         bb[i + 1] = bb[i] + (nothing ? 0u : (uint32_t)nblk);
         cb[i + 1] = cb[i] + (it.clear ? (uint32_t)nblk : 0u);

@@ -21,14 +21,13 @@ template <int VS>
 __global__ void __launch_bounds__(128) vertex_kernel(uint32_t n_verts, uint32_t n_pad, sr_uniforms U, VpMatrix vpm,
                                                      const float* __restrict__ planes, float4* __restrict__ clip4,
                                                      float4* __restrict__ scr4, float* __restrict__ vary) {
-    vertex_quad<VS>(blockIdx.x * blockDim.x + threadIdx.x, n_verts, n_pad, U, vpm, planes, clip4, scr4, vary);
+    vertex_one<VS>(blockIdx.x * blockDim.x + threadIdx.x, n_verts, n_pad, U, vpm, planes, clip4, scr4, vary);
 }
 
 void launch_vertex(const DrawParams& P, const sr_uniforms& U, const sr_mesh* m, VertexStore vs,
                    bool write_clip, cudaStream_t st) {
-    uint32_t quads = (m->n_verts + 3) / 4;
-    if (quads == 0) return;
-    dim3 grid((quads + 127) / 128), block(128);
+    if (m->n_verts == 0) return;
+    dim3 grid((m->n_verts + 127) / 128), block(128);
     VpMatrix vpm = viewport_matrix(P.vp);
     float4* c4 = write_clip ? vs.clip4 : nullptr;
     switch (P.vs) {

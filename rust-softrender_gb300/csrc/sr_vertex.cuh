@@ -22,41 +22,33 @@ __device__ __forceinline__ sr_v4 run_vs(const sr_uniforms* U, const float* a, fl
     return sr_vs_clip_rgba8(U, a, k);
 }
 
-// One thread's work of the vertex stage: vertices 4q .. 4q+3 (one 128-bit
-// load per attribute plane), shaded, normalised, written to the store.
+// One thread's work of the vertex stage: vertex v, shaded, normalised and
+// written to the store.  Consecutive threads take consecutive vertices, so
+// the plane loads and the position / varying stores are contiguous per warp.
 template <int VS>
-__device__ __forceinline__ void vertex_quad(uint32_t q, uint32_t n_verts, uint32_t n_pad, const sr_uniforms& U,
-                                            const VpMatrix& vpm, const float* __restrict__ planes,
-                                            float4* __restrict__ clip4, float4* __restrict__ scr4,
-                                            float* __restrict__ vary) {
+__device__ __forceinline__ void vertex_one(uint32_t v, uint32_t n_verts, uint32_t n_pad, const sr_uniforms& U,
+                                           const VpMatrix& vpm, const float* __restrict__ planes,
+                                           float4* __restrict__ clip4, float4* __restrict__ scr4,
+                                           float* __restrict__ vary) {
     constexpr int NP = VS == VS_MVP_POS_NRM ? 6 : VS == VS_CLIP_RGBA8 ? 4 : 8;
-    uint32_t v0 = q * 4;
-    if (v0 >= n_verts) return;
-    float4 in[NP];
+    if (v >= n_verts) return;
+    float a[8];
 #pragma unroll
-    for (int j = 0; j < NP; ++j) in[j] = __ldg(reinterpret_cast<const float4*>(planes + (size_t)j * n_pad) + q);
+    for (int j = 0; j < NP; ++j) a[j] = __ldg(planes + (size_t)j * n_pad + v);
+    float k[VSTRIDE];
 #pragma unroll
-    for (int l = 0; l < 4; ++l) {
-        uint32_t v = v0 + l;
-        if (v >= n_verts) break;
-        float a[8];
-#pragma unroll
-        for (int j = 0; j < NP; ++j) a[j] = l == 0 ? in[j].x : l == 1 ? in[j].y : l == 2 ? in[j].z : in[j].w;
-        float k[VSTRIDE];
-#pragma unroll
-        for (int i = 0; i < VSTRIDE; ++i) k[i] = 0.0f;
-        sr_v4 c = run_vs<VS>(&U, a, k);
-        if (clip4) clip4[v] = make_float4(c.x, c.y, c.z, c.w);
-        sr_v4 s = normalize_pos(c, vpm.m);
-        scr4[v] = make_float4(s.x, s.y, s.z, s.w);
-        // only the shader's varyings are written (readers never go beyond
-        // them: each fragment shader's are validated against the vertex shader's)
-        constexpr int NKQ = (vs_nk(VS) + 3) / 4;
-        float4* vo = reinterpret_cast<float4*>(vary + (size_t)v * VSTRIDE);
-        vo[0] = make_float4(k[0], k[1], k[2], k[3]);
-        if (NKQ > 1) vo[1] = make_float4(k[4], k[5], k[6], k[7]);
-        if (NKQ > 2) vo[2] = make_float4(k[8], k[9], k[10], k[11]);
-    }
+    for (int i = 0; i < VSTRIDE; ++i) k[i] = 0.0f;
+    sr_v4 c = run_vs<VS>(&U, a, k);
+    if (clip4) clip4[v] = make_float4(c.x, c.y, c.z, c.w);
+    sr_v4 s = normalize_pos(c, vpm.m);
+    scr4[v] = make_float4(s.x, s.y, s.z, s.w);
+    // only the shader's varyings are written (readers never go beyond them:
+    // each fragment shader's are validated against the vertex shader's)
+    constexpr int NKQ = (vs_nk(VS) + 3) / 4;
+    float4* vo = reinterpret_cast<float4*>(vary + (size_t)v * VSTRIDE);
+    vo[0] = make_float4(k[0], k[1], k[2], k[3]);
+    if (NKQ > 1) vo[1] = make_float4(k[4], k[5], k[6], k[7]);
+    if (NKQ > 2) vo[2] = make_float4(k[8], k[9], k[10], k[11]);
 }
 
 inline VpMatrix viewport_matrix(const float* vp) {
