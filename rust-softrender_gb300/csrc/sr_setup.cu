@@ -174,18 +174,16 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
             if (lane == 0 && m) atomicAdd(S.globals + k, (unsigned long long)__popc(m));
         }
     }
-    // statistics
-    for (int o = 16; o > 0; o >>= 1) {
-        n_raster += __shfl_down_sync(0xffffffffu, n_raster, o);
-        n_unsafe += __shfl_down_sync(0xffffffffu, n_unsafe, o);
-        n_entries += __shfl_down_sync(0xffffffffu, n_entries, o);
-        nan_cnt += __shfl_down_sync(0xffffffffu, nan_cnt, o);
-    }
+    // statistics: per-warp sums (one primitive per thread, so they fit 32 bits)
+    const uint32_t w_raster = __reduce_add_sync(0xffffffffu, (uint32_t)n_raster);
+    const uint32_t w_unsafe = __reduce_add_sync(0xffffffffu, (uint32_t)n_unsafe);
+    const uint32_t w_entries = __reduce_add_sync(0xffffffffu, (uint32_t)n_entries);
+    const uint32_t w_nan = __reduce_add_sync(0xffffffffu, nan_cnt);
     if (lane == 0) {
-        if (n_raster) atomicAdd(&flags->triangles_raster, n_raster);
-        if (n_unsafe) atomicAdd(&flags->unsafe, n_unsafe);
-        if (n_entries) atomicAdd(&flags->entries, n_entries);
-        if (nan_cnt) { atomicAdd(&flags->nan_bbox, nan_cnt); atomicAdd(&flags->nan_total, nan_cnt); }
+        if (w_raster) atomicAdd(&flags->triangles_raster, (unsigned long long)w_raster);
+        if (w_unsafe) atomicAdd(&flags->unsafe, (unsigned long long)w_unsafe);
+        if (w_entries) atomicAdd(&flags->entries, (unsigned long long)w_entries);
+        if (w_nan) { atomicAdd(&flags->nan_bbox, w_nan); atomicAdd(&flags->nan_total, w_nan); }
     }
 }
 
