@@ -673,7 +673,7 @@ def run_reference(args, rank, world):
         cpu_frame_estimate(scene, every=64, tiles=4, tile_begin=4 * i)
     frames, sample, threads = [], "", os.cpu_count()
     for i in range(args.steps):
-        f, sample, threads = cpu_frame_estimate(scene, every=2, tiles=128, tile_begin=128 * i)
+        f, sample, threads = cpu_frame_estimate(scene, every=2, tiles=64, tile_begin=64 * i)
         frames.append(f)
     frame_s = float(np.mean(frames))
     value = n_tris / frame_s / 1e6
