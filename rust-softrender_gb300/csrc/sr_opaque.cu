@@ -217,11 +217,11 @@ static void launch_resolve_fs(const DrawParams& P, const sr_uniforms& U, const O
 // launches: raster_small, raster_big, ext_direct, resolve
 int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A, cudaStream_t st) {
     // primitives per warp: 32, halved while that would leave fewer warps than
-    // the GPU holds (152 SMs x 48 resident warps); clipped draws estimate the
+    // the GPU holds (48 resident warps per SM); clipped draws estimate the
     // primitive count by the input count
     const uint32_t n_est = P.n_raster_host ? P.n_raster_host : P.n_in;
     uint32_t G = 32;
-    while (G > 1 && n_est / G < 152u * 48u) G >>= 1;
+    while (G > 1 && n_est / G < (uint32_t)sm_count() * 48u) G >>= 1;
 #define SR_RS(g) raster_small_kernel<g><<<resident_grid(raster_small_kernel<g>, RG_THREADS, 8), RG_THREADS, 0, st>>>( \
         P, A.setup, A.area, A.gkeys, A.bitmap, \
                                                                       A.stencil, A.gate, A.big_list, A.flags)
