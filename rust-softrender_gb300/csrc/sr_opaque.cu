@@ -42,10 +42,10 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
     uint32_t gate_with_stencil, uint32_t* __restrict__ big_list, DeviceFlags* flags) {
     __shared__ float4 srec[RG_THREADS / 32][32][3];
     __shared__ uint32_t sxy[RG_THREADS / 32][32];           // x0 | y0 << 16
-    __shared__ uint32_t sw[RG_THREADS / 32][32];            // bbox width
+    __shared__ uint32_t sw[RG_THREADS / 32][32];            // pairs per row | bbox width << 16
     __shared__ uint32_t sst[RG_THREADS / 32][32];           // first item
     __shared__ uint32_t st[RG_THREADS / 32][32];            // primitive index
-    __shared__ unsigned long long smag[RG_THREADS / 32][32]; // ceil(2^32 / width)
+    __shared__ unsigned long long smag[RG_THREADS / 32][32]; // ceil(2^32 / pairs per row)
     if (flags->poison) return;
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
     const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
@@ -59,11 +59,20 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
         t0 = __shfl_sync(0xffffffffu, t0, 0);
         if (t0 >= N) break;
         const uint32_t t = t0 + lane;
-        uint32_t a = 0;
+        // items: horizontal pairs of bbox pixels, ceil(w / 2) per bbox row
+        uint32_t a = 0, x0 = 0, y0 = 0, x1 = 0, y1 = 0;
         if (lane < G && t < N) {
             const unsigned long long at = area[t];
-            if (at > RG_BIG) big_list[atomicAdd(&flags->n_big, 1ull)] = t;
-            else a = (uint32_t)at;
+            if (at > RG_BIG) {
+                big_list[atomicAdd(&flags->n_big, 1ull)] = t;
+            } else if (at) {
+                const float4 r3 = __ldg(setup + 4 * (size_t)t + 3);
+                x0 = (uint32_t)max(__float_as_int(r3.x), 0);
+                y0 = (uint32_t)max(__float_as_int(r3.y), 0);
+                x1 = (uint32_t)min(__float_as_int(r3.z), (int)P.W - 1);
+                y1 = (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1);
+                a = (y1 - y0 + 1) * ((x1 - x0 + 2) >> 1);
+            }
         }
         const uint32_t inc = warp_inclusive_scan(a);
         const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
@@ -76,19 +85,14 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
             srec[wl][c][0] = __ldg(r);
             srec[wl][c][1] = __ldg(r + 1);
             srec[wl][c][2] = __ldg(r + 2);
-            const float4 r3 = __ldg(r + 3);
-            const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
-            const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
-            const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)P.W - 1);
-            const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1);
-            const uint32_t w = x1 - x0 + 1;
+            const uint32_t w = x1 - x0 + 1, wp = (w + 1) >> 1;
             mark_rect(bitmap, blocks_x, x0, y0, x1, y1);
             const uint32_t sb = seam_bits(x0, y0, x1, y1, P.W, P.H, P.tile_w, P.tile_h);
             sxy[wl][c] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
-            sw[wl][c] = w;
+            sw[wl][c] = wp | (w << 16);
             sst[wl][c] = ex;
             st[wl][c] = t;
-            smag[wl][c] = ((1ull << 32) + w - 1) / w;
+            smag[wl][c] = ((1ull << 32) + wp - 1) / wp;
         }
         __syncwarp();
         const uint32_t le = (2u << lane) - 1u;   // lanes 0..lane
@@ -101,12 +105,18 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
             before += __popc(starts);
             if (q < total) {
                 const uint32_t local = q - sst[wl][o];
-                const uint32_t w = sw[wl][o];
-                const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][o]) >> 32);  // local / w
+                const uint32_t wpw = sw[wl][o], wp = wpw & 0xffffu;
+                const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][o]) >> 32);  // local / wp
+                const uint32_t col = 2 * (local - row * wp);
                 const uint32_t xy = sxy[wl][o];
-                rg_fragment(P, srec[wl][o][0], srec[wl][o][1], srec[wl][o][2], st[wl][o],
-                            (xy & 0x7fffu) + (local - row * w), ((xy >> 16) & 0x7fffu) + row, N, gkeys, bitmap,
-                            stencil, gate_with_stencil, mx, my, ((xy >> 15) & 1u) | ((xy >> 30) & 2u), frags);
+                const float4 r0 = srec[wl][o][0], r1 = srec[wl][o][1], r2 = srec[wl][o][2];
+                const uint32_t px = (xy & 0x7fffu) + col, py = ((xy >> 16) & 0x7fffu) + row, tt = st[wl][o];
+                const uint32_t seams = ((xy >> 15) & 1u) | ((xy >> 30) & 2u);
+                rg_fragment(P, r0, r1, r2, tt, px, py, N, gkeys, bitmap, stencil, gate_with_stencil, mx, my, seams,
+                            frags);
+                if (col + 1 < (wpw >> 16))
+                    rg_fragment(P, r0, r1, r2, tt, px + 1, py, N, gkeys, bitmap, stencil, gate_with_stencil, mx, my,
+                                seams, frags);
             }
         }
         __syncwarp();
