@@ -287,7 +287,8 @@ __global__ void __launch_bounds__(256, 6) batch_raster_small_kernel(BTables T, c
         if (t0 >= total) break;
         i0 = __shfl_sync(0xffffffffu, i0, 0);
         const uint32_t g = t0 + lane;
-        uint32_t a = 0;
+        // items: horizontal pairs of bbox pixels, ceil(w / 2) per bbox row
+        uint32_t a = 0, i = 0, x0 = 0, y0 = 0, x1 = 0, y1 = 0;
         if (lane < G && g < total) {
             const unsigned long long at = area[g];
             if (at > big_threshold) {
@@ -296,8 +297,14 @@ __global__ void __launch_bounds__(256, 6) batch_raster_small_kernel(BTables T, c
                 const unsigned long long old = atomicAdd(queues + Q_BIG, (1ull << 40) | nch);
                 big_list[old >> 40] = g;
                 big_base[old >> 40] = (uint32_t)(old & ((1ull << 40) - 1));
-            } else {
-                a = (uint32_t)at;
+            } else if (at) {
+                i = owner_from(T.tbase, n, i0, g);
+                const float4 r3 = __ldg(setup + 4 * (size_t)g + 3);
+                x0 = (uint32_t)max(__float_as_int(r3.x), 0);
+                y0 = (uint32_t)max(__float_as_int(r3.y), 0);
+                x1 = (uint32_t)min(__float_as_int(r3.z), (int)T.inst[i].P.W - 1);
+                y1 = (uint32_t)min(__float_as_int(r3.w), (int)T.inst[i].P.H - 1);
+                a = (y1 - y0 + 1) * ((x1 - x0 + 2) >> 1);
             }
         }
         const uint32_t inc = warp_inclusive_scan(a);
@@ -307,23 +314,17 @@ __global__ void __launch_bounds__(256, 6) batch_raster_small_kernel(BTables T, c
         if (a) {
             // compacted slot: the rank of this primitive among the non-empty ones
             const uint32_t lane_c = __popc(nonempty & ((1u << lane) - 1u));
-            const uint32_t i = owner_from(T.tbase, n, i0, g);
             const BInst& I = T.inst[i];
             const float4* r = setup + 4 * (size_t)g;
             srec[wl][lane_c][0] = __ldg(r);
             srec[wl][lane_c][1] = __ldg(r + 1);
             srec[wl][lane_c][2] = __ldg(r + 2);
-            const float4 r3 = __ldg(r + 3);
             const uint32_t W = I.P.W, H = I.P.H;
-            const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), 0);
-            const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), 0);
-            const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)W - 1);
-            const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)H - 1);
-            const uint32_t w = x1 - x0 + 1;
+            const uint32_t w = x1 - x0 + 1, wp = (w + 1) >> 1;
             mark_rect(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1);
             const uint32_t sb = seam_bits(x0, y0, x1, y1, W, H, I.P.tile_w, I.P.tile_h);
             sxy[wl][lane_c] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
-            sw[wl][lane_c] = w;
+            sw[wl][lane_c] = wp | (w << 16);
             Slot S;
             S.wh = W | (H << 16);
             S.tiles = I.P.tile_w | (I.P.tile_h << 16);
@@ -334,7 +335,7 @@ __global__ void __launch_bounds__(256, 6) batch_raster_small_kernel(BTables T, c
             S.gkeys = I.gkeys;
             sslot[wl][lane_c] = S;
             sst[wl][lane_c] = ex;
-            smag[wl][lane_c] = ((1ull << 32) + w - 1) / w;
+            smag[wl][lane_c] = ((1ull << 32) + wp - 1) / wp;
         }
         __syncwarp();
         const uint32_t le = (2u << lane) - 1u;   // lanes 0..lane
@@ -347,15 +348,21 @@ __global__ void __launch_bounds__(256, 6) batch_raster_small_kernel(BTables T, c
             before += __popc(starts);
             if (q < tot) {
                 const uint32_t local = q - sst[wl][lo];
-                const uint32_t w = sw[wl][lo];
-                const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][lo]) >> 32);  // local / w
+                const uint32_t wpw = sw[wl][lo], wp = wpw & 0xffffu;
+                const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][lo]) >> 32);  // local / wp
+                const uint32_t col = 2 * (local - row * wp);
                 const uint32_t xy = sxy[wl][lo];
                 const Slot& S = sslot[wl][lo];
-                frag_emit(S.wh & 0xffffu, S.wh >> 16, S.tiles & 0xffffu, S.tiles >> 16, S.mx, S.my,
-                          ((xy >> 15) & 1u) | ((xy >> 30) & 2u), (S.n_depth >> 31) != 0, srec[wl][lo][0],
-                          srec[wl][lo][1], srec[wl][lo][2], S.t, (xy & 0x7fffu) + (local - row * w),
-                          ((xy >> 16) & 0x7fffu) + row, S.n_depth & 0x7fffffffu, S.gkeys,
+                const float4 r0 = srec[wl][lo][0], r1 = srec[wl][lo][1], r2 = srec[wl][lo][2];
+                const uint32_t px = (xy & 0x7fffu) + col, py = ((xy >> 16) & 0x7fffu) + row;
+                const uint32_t seams = ((xy >> 15) & 1u) | ((xy >> 30) & 2u);
+                frag_emit(S.wh & 0xffffu, S.wh >> 16, S.tiles & 0xffffu, S.tiles >> 16, S.mx, S.my, seams,
+                          (S.n_depth >> 31) != 0, r0, r1, r2, S.t, px, py, S.n_depth & 0x7fffffffu, S.gkeys,
                           nullptr, 0u, 0u, 0u, frags);
+                if (col + 1 < (wpw >> 16))
+                    frag_emit(S.wh & 0xffffu, S.wh >> 16, S.tiles & 0xffffu, S.tiles >> 16, S.mx, S.my, seams,
+                              (S.n_depth >> 31) != 0, r0, r1, r2, S.t, px + 1, py, S.n_depth & 0x7fffffffu, S.gkeys,
+                              nullptr, 0u, 0u, 0u, frags);
             }
         }
         __syncwarp();
