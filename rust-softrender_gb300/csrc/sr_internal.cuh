@@ -2,7 +2,7 @@
 //
 // Device data layout (all in HBM, owned by the pipeline / mesh objects):
 //   mesh planes      SoA f32, each plane padded to a multiple of 4 vertices
-//                    (16-byte aligned, read with 128-bit loads)
+//                    (16-byte aligned planes)
 //   mesh indices     u32, 3 per triangle
 //   vertex store     clip4[v]  AoS float4 clip-space position (clip GS only)
 //                    scr4[v]   AoS float4 screen position (x, y, z, 1/w)
@@ -179,8 +179,8 @@ __device__ __forceinline__ bool clamp_axis(int i0, int i1, uint32_t p, uint32_t 
 // Sound segment test of the extension pass (see sr_setup.cu): true when one of
 // the reference's u, v, w is certainly negative on the whole clamped segment
 // [x0, x1] x [y0, y1] (one of the two ranges is a single coordinate).
-__device__ __forceinline__ bool segment_cleared(float4 r0, float4 r1, uint32_t x0, uint32_t y0, uint32_t x1,
-                                                uint32_t y1) {
+__host__ __device__ __forceinline__ bool segment_cleared(float4 r0, float4 r1, uint32_t x0, uint32_t y0, uint32_t x1,
+                                                         uint32_t y1) {
     const float g = 5.0e-7f;
     const float eps = 6.0e-8f;
     const float det = r1.z;
@@ -211,7 +211,7 @@ __device__ __forceinline__ bool segment_cleared(float4 r0, float4 r1, uint32_t x
 // The same sign test over the pixel rectangle [x0, x1] x [y0, y1]: the
 // numerators and det - N_u - N_v are affine and their error bounds S convex,
 // so the four corners decide (each bound taken at its largest corner).
-__device__ __forceinline__ bool rect_cleared(float4 r0, float4 r1, int x0, int y0, int x1, int y1) {
+__host__ __device__ __forceinline__ bool rect_cleared(float4 r0, float4 r1, int x0, int y0, int x1, int y1) {
     const float g = 5.0e-7f;
     const float eps = 6.0e-8f;
     const float det = r1.z;
