@@ -86,3 +86,77 @@ def test_invalid_arguments_rejected_on_host(built_lib):
     idx = np.array([0, 1, 5], dtype=np.uint32)
     arr = (C.c_void_p * 1)(plane.ctypes.data)
     assert lib.sr_mesh_upload(arr, 1, 3, idx.ctypes.data, 3, C.byref(h)) == A.SR_EINVAL
+
+
+# ---------------------------------------------------------------- the Rust binding shown to integrators
+_C2RUST = {"uint32_t": "u32", "int32_t": "i32", "uint64_t": "u64", "uint8_t": "u8", "float": "f32",
+           "double": "f64", "size_t": "usize", "int": "c_int", "char": "c_char", "void": "c_void"}
+
+
+def _rust_type(c_decl):
+    """The Rust spelling of a C type: `const float* const*` -> `*const *const f32`.
+    A `const` before a `*` qualifies what that `*` points to."""
+    toks = re.findall(r"\w+|\*", c_decl)
+    base, pointee_const, levels = None, False, []
+    for t in toks:
+        if t == "const":
+            pointee_const = True
+        elif t == "*":
+            levels.append(pointee_const)
+            pointee_const = False
+        else:
+            base = t
+    ty = _C2RUST.get(base, base)
+    for c in levels:
+        ty = ("*const " if c else "*mut ") + ty
+    return ty
+
+
+def _header_text():
+    txt = open(os.path.join(ROOT, "include", "sr.h")).read()
+    return re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+
+
+def _rust_block():
+    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    return "\n".join(b for b in re.findall(r"```rust\n(.*?)```", txt, flags=re.S) if "extern \"C\"" in b)
+
+
+def test_rust_binding_functions_match_header():
+    hdr, rust = _header_text(), _rust_block()
+    want = {}
+    for ret, name, args in re.findall(r"SR_API\s+([\w\s\*]+?)\b(sr_\w+)\s*\(([^)]*)\)\s*;", hdr):
+        params = [] if args.strip() in ("", "void") else args.split(",")
+        # drop the parameter name, keep its type
+        types = [_rust_type(re.sub(r"\b\w+\s*$", "", p)) for p in params]
+        r = _rust_type(ret).strip()
+        want[name] = (types, None if r == "c_void" else r)
+    got = {}
+    for name, args, ret in re.findall(r"pub fn (sr_\w+)\(([^)]*)\)\s*(?:->\s*([^;]+))?;", rust):
+        types = [" ".join(a.split(":", 1)[1].split()) for a in args.split(",") if a.strip()]
+        got[name] = (types, ret.strip() if ret else None)
+    assert set(got) == set(want), set(got) ^ set(want)
+    bad = {n: (want[n], got[n]) for n in want if want[n] != got[n]}
+    assert not bad, bad
+
+
+def test_rust_binding_structs_match_header():
+    hdr, rust = _header_text(), _rust_block()
+    rust_structs = {n: [(f, " ".join(t.split())) for f, t in re.findall(r"pub (\w+): ([^,]+)", body)]
+                    for n, body in re.findall(r"pub struct (sr_\w+) \{(.*?)\}", rust, flags=re.S)}
+    checked = 0
+    for body, name in re.findall(r"typedef struct \w+ \{(.*?)\} (sr_\w+);", hdr, flags=re.S):
+        fields = []
+        for decl in (d.strip() for d in body.split(";")):
+            if not decl:
+                continue
+            m = re.match(r"((?:const\s+)?\w+\s*\**)\s*(.*)$", decl, flags=re.S)
+            for item in m.group(2).split(","):
+                item = item.strip()
+                arr = re.match(r"(\w+)\[(\d+)\]", item)
+                ty = _rust_type(m.group(1))
+                fields.append((arr.group(1), f"[{ty}; {arr.group(2)}]") if arr else (item, ty))
+        assert name in rust_structs, name
+        assert rust_structs[name] == fields, (name, rust_structs[name], fields)
+        checked += 1
+    assert checked >= 8
