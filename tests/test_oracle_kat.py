@@ -7,7 +7,9 @@ computed here independently of the oracle's code: tile walks from the loop
 in fragment.rs:188-216, viewport products from clipvertex.rs:89-127, the
 clip push order of geometry.rs:264-299, coverage from triangle.rs:104-126
 evaluated with numpy float32 (IEEE single, no contraction), the f32::MIN
-depth clear, ties passing `>=`, stencil events per tile pass, and the
+depth clear, ties passing `>=`, stencil events per tile pass (clamped onto
+tile edges, counted behind the depth test), the NaN coverage of a
+zero-area triangle, seam pixels blended once per tile pass, and the
 accuracy of the pow used by the shaders.  No GPU needed."""
 import ctypes as C
 import math
@@ -223,3 +225,95 @@ def test_pow_special_cases(oracle_mod):
 def test_byte_to_unit_exact(oracle_mod):
     for c in range(256):
         assert oracle_mod.u8_unit(c) == F(c) / F(255)
+
+
+def _clamp_as_int(v, lo, hi):
+    # triangle.rs:66-78: below the tile -> its low edge, above -> its high edge, else trunc
+    return lo if v < lo else hi if v > hi else int(math.trunc(v))
+
+
+def _stencil_events_by_hand(tri_xy, W, H, tw, th):
+    """Stencil events of one triangle (triangle.rs:82-99): every pixel of its
+    bbox clamped to each semantic tile, once per tile, covered or not."""
+    xs, ys = [float(p[0]) for p in tri_xy], [float(p[1]) for p in tri_xy]
+    want = np.zeros((H, W), np.uint8)
+    for (x0, y0, x1, y1) in _tiles_by_hand(W, H, tw, th):
+        mnx, mxx = _clamp_as_int(min(xs), x0, x1), _clamp_as_int(max(xs), x0, x1)
+        mny, mxy = _clamp_as_int(min(ys), y0, y1), _clamp_as_int(max(ys), y0, y1)
+        want[mny:mxy + 1, mnx:mxx + 1] += 1
+    return want
+
+
+def test_degenerate_triangle_nan_path(oracle_mod):
+    """A triangle with det = 0 (triangle.rs:64): at a pixel centre on its line
+    both numerators are 0, so u = v = w = NaN and the pixel counts as covered
+    (triangle.rs:113); the interpolated depth is NaN too, so `pos.z < 0`
+    fails (triangle.rs:120) and nothing is shaded.  The stencil, applied per
+    bbox pixel before the coverage test (triangle.rs:90-99), still counts, and
+    its bbox clamped onto a tile it misses collapses onto that tile's edge row."""
+    W = H = 8
+    sc = _one_triangle_scene([(1.5, 2.5), (5.5, 2.5), (3.5, 2.5)], W, H, stencil=True,
+                             stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT)
+    tri = oracle_mod.raster_tris(sc)[0]
+    xy = [(tri[j][0], tri[j][1]) for j in range(3)]
+    assert all(p[1] == F(2.5) for p in xy)            # the line runs exactly through row 2's centres
+    with np.errstate(divide="ignore", invalid="ignore"):
+        m = _coverage_by_hand(xy, W, H)
+    # covered through NaN: every centre of row 2 lies on the line (the bbox
+    # limits the visited ones to x = 1..5)
+    assert m.sum() == W and m[2].all()
+    fb, st, status = oracle_mod.render(sc)
+    assert status == 0 and st["fragments"] == 0
+    assert (fb.color == 0).all()
+    assert (fb.depth == F(-3.4028235e38)).all()
+    want = _stencil_events_by_hand(xy, W, H, 4, 4)
+    assert want[4].any()                              # events on the edge row of the tiles below
+    assert np.array_equal(fb.stencil, want)
+
+
+def test_seam_pixels_blend_once_per_tile_pass(oracle_mod):
+    """Adjacent semantic tiles share a row or column (fragment.rs:188-216) and
+    every primitive is visited in every tile (fragment.rs:240-318), so with a
+    blend a seam pixel is blended once per tile holding it, and ties pass the
+    depth test (`>=`, triangle.rs:120-126) each time.  Checked per pixel: one
+    draw with 4x4 tiles equals the same triangle drawn, with one tile over the
+    whole frame, as many times as 4x4 tiles hold that pixel (1, 2 or 4)."""
+    W = H = 9
+    kw = dict(rgba=(200, 100, 50, 128), blend="over", clear_color=(0.0, 0.0, 1.0, 1.0))
+    tri = [(-5.0, -5.0), (30.0, -5.0), (-5.0, 30.0)]
+    tiled, _, status = oracle_mod.render(_one_triangle_scene(tri, W, H, **kw))
+    assert status == 0
+    whole = _one_triangle_scene(tri, W, H, tile=(128, 128), **kw)
+    assert len(_tiles_by_hand(W, H, 128, 128)) == 1
+    fb = oracle_mod.framebuffer_for(whole)
+    after = {}
+    for k in range(1, 5):
+        fb, _, _ = oracle_mod.render(whole, fb=fb)
+        after[k] = fb.color.view(np.uint32).reshape(H, W).copy()
+    count = np.zeros((H, W), int)
+    for (x0, y0, x1, y1) in _tiles_by_hand(W, H, 4, 4):
+        count[y0:y1 + 1, x0:x1 + 1] += 1
+    assert sorted(set(count.ravel().tolist())) == [1, 2, 4]
+    want = np.choose(count - 1, [after[1], after[2], after[3], after[4]])
+    got = tiled.color.view(np.uint32).reshape(H, W)
+    assert np.array_equal(got, want)
+    assert (after[2] != after[1]).all()              # each extra blend changes the pixel
+
+
+def test_stencil_counts_pixels_failing_depth(oracle_mod):
+    """The stencil op runs before the depth test (triangle.rs:90-99 then
+    :120-126): a triangle behind the depth already written still counts its
+    events, and leaves colour and depth as they were."""
+    W = H = 9
+    tri = [(-5.0, -5.0), (30.0, -5.0), (-5.0, 30.0)]
+    front = _one_triangle_scene(tri, W, H, z=-0.25, stencil=True,
+                                stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT)
+    back = _one_triangle_scene(tri, W, H, z=-0.75, rgba=(0, 255, 0, 255), stencil=True,
+                               stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT)
+    fb, _, _ = oracle_mod.render(front)
+    color, depth = fb.color.copy(), fb.depth.copy()
+    fb, st, status = oracle_mod.render(back, fb=fb)
+    assert status == 0 and st["fragments"] > 0                     # covered, reaching the depth test
+    assert np.array_equal(fb.color, color) and np.array_equal(fb.depth, depth)
+    xy = [(v[0], v[1]) for v in oracle_mod.raster_tris(front)[0]]
+    assert np.array_equal(fb.stencil, 2 * _stencil_events_by_hand(xy, W, H, 4, 4))
