@@ -234,7 +234,9 @@ SR_API int sr_framebuffer_device_ptrs(sr_pipeline* p, void** color, float** dept
 
 /* Mesh<V> (src/mesh.rs:38-64) uploaded as SoA f32 attribute planes (each
  * n_verts floats; the vertex shader fixes their meaning) plus u32 indices.
- * Host buffers are copied before return; the mesh is immutable afterwards. */
+ * Host buffers are copied before return; the mesh is immutable afterwards.
+ * At most 2^31 vertices (SR_EINVAL beyond): vertex references are u32 and
+ * the geometry stage adds up to 2^30 generated vertices after the mesh's. */
 SR_API int sr_mesh_upload(const float* const* planes, uint32_t n_planes, uint32_t n_verts,
                           const uint32_t* indices, uint64_t n_indices, sr_mesh** out);
 /* Replaces the contents of an uploaded mesh with new host data of the same
@@ -291,7 +293,11 @@ SR_API void sr_draw_init(sr_draw* d);
  * the pipeline's stream (see sr_draw). */
 SR_API int sr_render(sr_pipeline* p, const sr_draw* d);
 /* Waits for the pipeline's stream; returns the first device-recorded error of
- * the draws since the previous sync (SR_ENAN, SR_EOVERFLOW) or SR_ECUDA. */
+ * the draws since the previous sync (SR_ENAN, SR_EOVERFLOW) or SR_ECUDA.
+ * Scratch buffers that a draw outgrew are enlarged and the draws from the
+ * first affected one replayed (up to 8 rounds); SR_EOVERFLOW means the frame
+ * is incomplete: a draw needed more than 2^30 primitives or vertices out of
+ * the geometry stage, or more than 2^32 - 1 (bin, primitive) pairs. */
 SR_API int sr_sync(sr_pipeline* p);
 /* Counters of the most recent sr_render (valid after sr_sync). */
 SR_API int sr_get_stats(sr_pipeline* p, sr_stats* out);

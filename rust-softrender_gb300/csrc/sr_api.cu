@@ -297,6 +297,9 @@ extern "C" SR_API int sr_mesh_upload(const float* const* planes, uint32_t n_plan
                                      const uint32_t* indices, uint64_t n_indices, sr_mesh** out) {
     if (!out || (n_planes && !planes) || n_planes > (uint32_t)MAX_PLANES || (n_indices && !indices)) return SR_EINVAL;
     *out = nullptr;
+    // vertex references are u32: the padded planes plus the geometry stage's
+    // generated vertices (at most 2^30) stay below 2^32
+    if (n_verts > (1u << 31)) return SR_EINVAL;
     for (uint64_t i = 0; i < n_indices; ++i)
         if (indices[i] >= n_verts) return SR_EINVAL;
     if (n_indices / 3 > (1ull << 30)) return SR_EINVAL;
@@ -756,12 +759,14 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
     if (!p) return SR_EINVAL;
     int status = SR_OK;
     bool replayed = false;
+    bool settled = false;   // the flags read clean after the last enqueue or replay
     for (int attempt = 0; attempt < 8; ++attempt) {
         SR_CK(cudaMemcpyAsync(p->hflags, p->flags, sizeof(DeviceFlags), cudaMemcpyDeviceToHost, p->stream));
         cudaError_t e = cudaStreamSynchronize(p->stream);
         if (e != cudaSuccess) { last_cuda_error() = e; return SR_ECUDA; }
         DeviceFlags f = *p->hflags;
         if (!f.poison) {
+            settled = true;
             if (p->pending.empty()) break;
             std::memset(&p->last_stats, 0, sizeof(p->last_stats));
             p->last_stats.triangles_generated = f.triangles_generated;
@@ -788,6 +793,11 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
         if (f.overflow_bits & OVF_GEN_VERTS) p->gen_vert_cap = f.need_gen_verts + f.need_gen_verts / 4 + 1024;
         if (f.overflow_bits & OVF_ENTRIES) p->entry_cap = f.need_entries + f.need_entries / 4 + 1024;
         if (f.overflow_bits & OVF_SORT) { status = SR_EOVERFLOW; }
+        // the capacities are clamped when a draw is enqueued (2^30 generated
+        // triangles and vertices, 2^32 - 1 bin entries): a draw needing more
+        // overflows again on every replay
+        if (f.need_gen_tris > (1ull << 30) || f.need_gen_verts > (1ull << 30) || f.need_entries > 0xffffffffull)
+            status = SR_EOVERFLOW;
         uint32_t from = f.poison_draw;
         DeviceFlags z;
         std::memset(&z, 0, sizeof(z));
@@ -803,6 +813,9 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
         replayed = true;
         if (status != SR_OK) break;
     }
+    // out of attempts with the last replay unchecked, or poisoned without a draw
+    // to replay: the frame is incomplete
+    if (!settled && status == SR_OK) status = SR_EOVERFLOW;
     // asynchronous reads copied a framebuffer that replayed draws changed
     if (replayed)
         for (const auto& r : p->pending_reads) {

@@ -86,6 +86,9 @@ def test_invalid_arguments_rejected_on_host(built_lib):
     idx = np.array([0, 1, 5], dtype=np.uint32)
     arr = (C.c_void_p * 1)(plane.ctypes.data)
     assert lib.sr_mesh_upload(arr, 1, 3, idx.ctypes.data, 3, C.byref(h)) == A.SR_EINVAL
+    # more vertices than u32 vertex references leave room for (checked before any copy)
+    assert lib.sr_mesh_upload(None, 0, (1 << 31) + 1, None, 0, C.byref(h)) == A.SR_EINVAL
+    assert h.value is None
 
 
 # ---------------------------------------------------------------- the Rust binding shown to integrators
