@@ -696,6 +696,7 @@ extern "C" SR_API int sr_render(sr_pipeline* p, const sr_draw* d) {
     // the normal shaders read world position and normal from varyings 0..7
     if (d->gs_mode == SR_GS_NAMED && d->gs != GS_CLIP && vs_nk(d->vs) < 8) return SR_EINVAL;
     if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
+    if (d->tex_filter > SR_SAMPLE_BILINEAR || d->tex_edge > SR_SAMPLE_BORDER) return SR_EINVAL;
     if (d->cull > SR_CULL_COUNTER_CLOCKWISE) return SR_EINVAL;
     if (m->n_planes < (uint32_t)vs_planes(d->vs)) return SR_EINVAL;
     if (vs_nk(d->vs) < fs_min_varyings(d->fs)) return SR_EINVAL;

@@ -823,6 +823,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         if (m->n_indices % 3 != 0) return SR_EINVAL;                        // mod.rs:148
         if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT) return SR_EINVAL;
         if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
+        if (d->tex_filter > SR_SAMPLE_BILINEAR || d->tex_edge > SR_SAMPLE_BORDER) return SR_EINVAL;
         if (d->cull > SR_CULL_COUNTER_CLOCKWISE) return SR_EINVAL;
         if (m->n_planes < (uint32_t)vs_planes(d->vs)) return SR_EINVAL;
         if (vs_nk(d->vs) < batch_min_varyings(d->fs)) return SR_EINVAL;

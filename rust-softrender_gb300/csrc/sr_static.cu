@@ -107,6 +107,7 @@ extern "C" SR_API int sr_render_static(const sr_draw* d, const void* uniforms, s
     if (d->reuse != SR_REUSE_NONE) return SR_EINVAL;           // no previous draw to refer to
     if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT) return SR_EINVAL;
     if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
+    if (d->tex_filter > SR_SAMPLE_BILINEAR || d->tex_edge > SR_SAMPLE_BORDER) return SR_EINVAL;
     if (d->cull > SR_CULL_COUNTER_CLOCKWISE) return SR_EINVAL;
     if (vs_nk(d->vs) < min_varyings(d->fs)) return SR_EINVAL;
     if (fb->width == 0 || fb->height == 0 || fb->width > 32767 || fb->height > 32767) return SR_EINVAL;

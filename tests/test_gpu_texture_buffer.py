@@ -129,3 +129,36 @@ def test_texture_views_rejected(built_lib):
         view.free()
         pl.destroy()
         mesh.free()
+
+
+def test_unknown_sampler_modes_rejected(built_lib):
+    """sr_filter has two values and sr_edge three; any other value is refused
+    by sr_render, sr_batch_render and sr_render_static alike."""
+    import softrender as sr
+    sc = scenes.grid_sphere_scene(32, 32, n_lat=4, n_lon=8, tex_size=8, gs_mode=A.SR_GS_NONE,
+                                  color_format=A.SR_COLOR_RGBA8)
+    pl, mesh, tex = sr.prepare_scene(sc)
+    L = sr.lib()
+    b = sr.Batch(use_graphs=False, autotune=False)
+    try:
+        for field, bad in (("tex_filter", A.SR_SAMPLE_BILINEAR + 1), ("tex_edge", A.SR_SAMPLE_BORDER + 1)):
+            d = sr.draw_for_scene(sc, mesh, tex)
+            setattr(d, field, bad)
+            assert L.sr_render(pl.handle, C.byref(d)) == A.SR_EINVAL
+            assert b.render_items(b.items([(pl, d, None)])) == A.SR_EINVAL
+            ds = A.SrDraw()
+            L.sr_draw_init(C.byref(ds))
+            setattr(ds, field, bad)
+            fb = A.SrFbDesc(32, 32, A.SR_COLOR_RGBA8, 1, 0)
+            # refused while checking the draw, before any buffer is looked at
+            assert L.sr_render_static(C.byref(ds), C.byref(sc.uniforms), C.sizeof(sc.uniforms), None, 0, 0, 0,
+                                      None, 0, None, 0, 0, C.byref(fb), None, None, None) == A.SR_EINVAL
+        d = sr.draw_for_scene(sc, mesh, tex)
+        assert L.sr_render(pl.handle, C.byref(d)) == A.SR_OK
+        assert pl.sync() == A.SR_OK
+    finally:
+        b.destroy()
+        pl.destroy()
+        mesh.free()
+        if tex is not None:
+            tex.free()
