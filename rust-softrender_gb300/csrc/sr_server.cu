@@ -1,6 +1,7 @@
 // sr_server.cu — the serving loop (continuous batching) over sr_batch.
 //
-// A worker thread owns every CUDA call of the server.  Submitted requests
+// A worker thread makes every rendering call of the server (the copies of a
+// result run on the thread that reads it).  Submitted requests
 // wait in a FIFO; whenever a batch slot is free and the head of the FIFO fits
 // the HBM budget, the worker takes every queued request that fits (up to
 // max_batch, in arrival order) and renders them as one batch on that slot's
@@ -10,7 +11,10 @@
 // slot's stream stamps the completion time of its requests.
 //
 // Targets (pipelines: colour, depth, per-pixel keys) are pooled by size and
-// format and stay resident until the caller reads or releases the result.
+// format and stay resident until the caller reads or releases the result;
+// the pool then keeps them for reuse.  Pooled targets count against the HBM
+// budget with the admitted requests, and are freed when admitted work needs
+// their room.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -58,10 +62,13 @@ uint64_t px_class(uint32_t w, uint32_t h) {
     return c;
 }
 
-uint64_t target_bytes(uint32_t w, uint32_t h, uint32_t fmt) {
-    const uint64_t px = px_class(w, h);
+// Device bytes of a pooled target of pixel class `px`: colour, depth and
+// per-pixel keys, the touched-block bitmap, flags.
+uint64_t class_bytes(uint64_t px, uint32_t fmt) {
     return px * ((fmt == SR_COLOR_RGBA32F ? 16 : 4) + 4 + 8) + px / 256 + 4096;
 }
+
+uint64_t target_bytes(uint32_t w, uint32_t h, uint32_t fmt) { return class_bytes(px_class(w, h), fmt); }
 
 uint64_t request_bytes(const sr_request& r) {
     const sr_mesh* m = r.draw.mesh;
@@ -82,6 +89,7 @@ struct sr_server {
     std::multimap<std::pair<uint64_t, uint32_t>, sr_pipeline*> pool;   // (pixel class, format)
     uint64_t next_ticket = 1;
     uint64_t in_use = 0, peak = 0;
+    uint64_t pool_bytes = 0;    // targets held in the pool for reuse
     uint32_t inflight = 0;
     bool stop = false;
     int device = 0;
@@ -124,14 +132,24 @@ void CUDART_CB batch_done(void* p) {
 sr_pipeline* take_target(sr_server* s, uint32_t w, uint32_t h, uint32_t fmt) {
     const uint64_t cls = px_class(w, h);
     sr_pipeline* p = nullptr;
+    std::vector<sr_pipeline*> evict;
     {
         std::lock_guard<std::mutex> lk(s->mu);
         auto it = s->pool.find(std::make_pair(cls, fmt));
         if (it != s->pool.end()) {
             p = it->second;
             s->pool.erase(it);
+            s->pool_bytes -= class_bytes(cls, fmt);
+        }
+        // the pool counts against the budget too: while the admitted requests
+        // and the pooled targets together exceed it, pooled targets go
+        for (auto e = s->pool.begin(); e != s->pool.end() && s->in_use + s->pool_bytes > s->cfg.hbm_budget;) {
+            s->pool_bytes -= class_bytes(e->first.first, e->first.second);
+            evict.push_back(e->second);
+            e = s->pool.erase(e);
         }
     }
+    for (sr_pipeline* e : evict) sr_pipeline_destroy(e);
     if (!p) {
         sr_fb_desc fb{w, h, fmt, 1, 0};
         if (pipeline_create_cap(&fb, cls, &p) != SR_OK) return nullptr;
@@ -291,11 +309,17 @@ extern "C" SR_API int sr_server_submit(sr_server* s, const sr_request* r, uint64
 extern "C" SR_API int sr_server_wait(sr_server* s, uint64_t ticket, uint32_t timeout_ms) {
     if (!s) return SR_EINVAL;
     std::unique_lock<std::mutex> lk(s->mu);
-    auto it = s->reqs.find(ticket);
-    if (it == s->reqs.end()) return SR_EINVAL;
-    Req* q = it->second;
-    if (!s->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return q->done; })) return SR_ETIMEOUT;
-    return q->status;
+    if (s->reqs.find(ticket) == s->reqs.end()) return SR_EINVAL;
+    // looked up again on every wake-up: another thread may read (and free)
+    // the request meanwhile
+    Req* q = nullptr;
+    const bool ok = s->cv.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] {
+        auto it = s->reqs.find(ticket);
+        q = it == s->reqs.end() ? nullptr : it->second;
+        return !q || q->done;
+    });
+    if (!ok) return SR_ETIMEOUT;
+    return q ? q->status : SR_EINVAL;
 }
 
 namespace {
@@ -313,7 +337,11 @@ int finish(sr_server* s, uint64_t ticket, void* color, float* depth) {
     if (q->target && (color || depth) && st == SR_OK) st = sr_framebuffer_read(q->target, color, depth, nullptr);
     {
         std::lock_guard<std::mutex> lk(s->mu);
-        if (q->target) s->pool.emplace(std::make_pair(px_class(q->r.width, q->r.height), q->r.color_format), q->target);
+        if (q->target) {
+            const uint64_t cls = px_class(q->r.width, q->r.height);
+            s->pool.emplace(std::make_pair(cls, q->r.color_format), q->target);
+            s->pool_bytes += class_bytes(cls, q->r.color_format);
+        }
         s->in_use -= q->bytes;
     }
     s->cv.notify_all();
