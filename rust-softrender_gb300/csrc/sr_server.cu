@@ -21,6 +21,7 @@
 #include <condition_variable>
 #include <cstring>
 #include <deque>
+#include <iterator>
 #include <map>
 #include <mutex>
 #include <thread>
@@ -142,11 +143,13 @@ sr_pipeline* take_target(sr_server* s, uint32_t w, uint32_t h, uint32_t fmt) {
             s->pool_bytes -= class_bytes(cls, fmt);
         }
         // the pool counts against the budget too: while the admitted requests
-        // and the pooled targets together exceed it, pooled targets go
-        for (auto e = s->pool.begin(); e != s->pool.end() && s->in_use + s->pool_bytes > s->cfg.hbm_budget;) {
+        // and the pooled targets together exceed it, pooled targets go,
+        // largest first (fewest frees)
+        while (!s->pool.empty() && s->in_use + s->pool_bytes > s->cfg.hbm_budget) {
+            const auto e = std::prev(s->pool.end());
             s->pool_bytes -= class_bytes(e->first.first, e->first.second);
             evict.push_back(e->second);
-            e = s->pool.erase(e);
+            s->pool.erase(e);
         }
     }
     for (sr_pipeline* e : evict) sr_pipeline_destroy(e);
