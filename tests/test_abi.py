@@ -163,3 +163,34 @@ def test_rust_binding_structs_match_header():
         assert rust_structs[name] == fields, (name, rust_structs[name], fields)
         checked += 1
     assert checked >= 8
+
+
+def test_ctypes_struct_layouts_match_header(tmp_path):
+    """Every ctypes structure of softrender._abi has the size, and each of its
+    fields the offset, that a C++ compiler gives the struct of include/sr.h /
+    include/sr_shaders.h of the same name (a mismatch would corrupt every call
+    that passes the struct).  Host compiler only, no GPU."""
+    import shutil
+    import subprocess
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    classes = {"sr_uniforms": A.SrUniforms, "sr_fb_desc": A.SrFbDesc, "sr_viewport": A.SrViewport,
+               "sr_draw": A.SrDraw, "sr_stats": A.SrStats, "sr_batch_item": A.SrBatchItem,
+               "sr_server_config": A.SrServerConfig, "sr_request": A.SrRequest,
+               "sr_server_stats": A.SrServerStats}
+    lines = ["#include <cstddef>", "#include <cstdio>", '#include "sr.h"', '#include "sr_shaders.h"',
+             "int main() {"]
+    want = []
+    for cname, cls in classes.items():
+        lines.append(f'    std::printf("{cname} %zu\\n", sizeof({cname}));')
+        want.append(f"{cname} {C.sizeof(cls)}")
+        for fname, _ in cls._fields_:
+            lines.append(f'    std::printf("{cname}.{fname} %zu\\n", offsetof({cname}, {fname}));')
+            want.append(f"{cname}.{fname} {getattr(cls, fname).offset}")
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.cpp"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    subprocess.check_call(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe])
+    got = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
+    assert [g for g in got if g] == want
