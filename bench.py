@@ -140,40 +140,38 @@ def subsample_scene(scene, every):
 
 def cpu_frame_estimate(scene, every, tiles, tile_begin=0, threads=None):
     """Times the oracle (the reference path restated, all host threads) on a
-    bounded sample and extrapolates to one full frame:
-      t_vs    vertex stage over all vertices (no primitives)
-      t_geo   vertex + geometry stage on every `every`-th triangle
-      t_ras   rasterisation of that sample over `tiles` of the frame's tiles
-    frame = t_vs + every * (t_geo - t_vs) + every * t_ras * n_tiles / tiles
+    bounded sample and extrapolates to one full frame, from the stage times
+    the oracle measures inside one render call:
+      vertex    vertex stage over all vertices
+      geometry  geometry stage (clip GS + finish) on every `every`-th triangle
+      raster    fragment stage of that sample over `tiles` of the frame's
+                tiles, spread over the frame (1 in n_tiles // tiles, the
+                offset rotating with tile_begin)
+    frame = vertex + every * geometry + every * raster * n_tiles / tiles
     (the reference's geometry cost and its per-tile cost are linear in the
-    primitive count: every tile visits every primitive)."""
+    primitive count: every tile visits every primitive; screen content is
+    uneven, so a contiguous run of tiles would extrapolate its own density
+    to the frame)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
     threads = threads or os.cpu_count()
-    empty = subsample_scene(scene, 1)
-    empty.indices = np.zeros(0, dtype=np.uint32)
-    t0 = time.perf_counter()
-    oracle.render(empty, n_threads=threads, tile_end=0)
-    t_vs = time.perf_counter() - t0
     sc = subsample_scene(scene, every)
-    t0 = time.perf_counter()
-    _, st, _ = oracle.render(sc, n_threads=threads, tile_end=0)
-    t_geo = time.perf_counter() - t0
-    n_tiles = int(st["tiles"])
+    n_tiles = len(oracle.tiles(scene.width, scene.height, *scene.tile))
     tiles = min(tiles, n_tiles)
-    tb = tile_begin % max(1, n_tiles - tiles + 1)
+    step = max(1, n_tiles // tiles)
+    first = tile_begin % step
+    picked = range(first, min(n_tiles, first + step * tiles), step)
     t0 = time.perf_counter()
-    oracle.render(sc, n_threads=threads, tile_begin=tb, tile_end=tb + tiles)
-    t_all = time.perf_counter() - t0
-    t_ras = max(0.0, t_all - t_geo)
-    frame = t_vs + every * max(0.0, t_geo - t_vs) + every * t_ras * n_tiles / tiles
-    if every == 1 and tiles == n_tiles:
+    _, st, _ = oracle.render(sc, n_threads=threads, tile_begin=first, tile_end=picked.stop, tile_step=step)
+    wall = time.perf_counter() - t0
+    frame = st["vertex_s"] + every * st["geometry_s"] + every * st["raster_s"] * n_tiles / len(picked)
+    if every == 1 and len(picked) == n_tiles:
         sample = ("one full frame: all %d triangles through vertex+clip GS, rasterised over all %d tiles; "
-                  "%.1f s of CPU wall time" % (scene.n_tris, n_tiles, t_vs + t_geo + t_all))
+                  "%.1f s of CPU wall time" % (scene.n_tris, n_tiles, wall))
     else:
-        sample = ("every %d-th of %d triangles through vertex+clip GS, rasterised over %d of %d tiles, "
-                  "extrapolated linearly to the frame; %.1f s of CPU wall time" % (
-                      every, scene.n_tris, tiles, n_tiles, t_vs + t_geo + t_all))
+        sample = ("1 in %d of %d triangles through vertex+clip GS, rasterised over %d of %d tiles "
+                  "(1 in %d, spread over the frame), stage times extrapolated linearly to the frame; "
+                  "%.1f s of CPU wall time" % (every, scene.n_tris, len(picked), n_tiles, step, wall))
     return frame, sample, threads
 
 
@@ -672,8 +670,14 @@ def run_reference(args, rank, world):
     for i in range(args.warmup):
         cpu_frame_estimate(scene, every=64, tiles=4, tile_begin=4 * i)
     frames, sample, threads = [], "", os.cpu_count()
+    # one step samples 1 in 2 triangles over 64 tiles (about 7 s on 8 cores);
+    # beyond 20 steps each step samples up to 3x less (1 in 6 triangles over
+    # 21 tiles still estimates the frame within a few percent), so that long
+    # runs stay within a few minutes
+    shrink = min(3, max(1, -(-args.steps // 20)))
+    tiles = 64 // shrink
     for i in range(args.steps):
-        f, sample, threads = cpu_frame_estimate(scene, every=2, tiles=64, tile_begin=64 * i)
+        f, sample, threads = cpu_frame_estimate(scene, every=2 * shrink, tiles=tiles, tile_begin=i)
         frames.append(f)
     frame_s = float(np.mean(frames))
     value = n_tris / frame_s / 1e6

@@ -48,7 +48,8 @@ class OrFb(C.Structure):
 
 class OrStats(C.Structure):
     _fields_ = [("triangles_generated", C.c_uint64), ("fragments", C.c_uint64),
-                ("tiles", C.c_uint64), ("nan_bbox", C.c_uint32), ("status", C.c_uint32)]
+                ("tiles", C.c_uint64), ("nan_bbox", C.c_uint32), ("status", C.c_uint32),
+                ("vertex_s", C.c_double), ("geometry_s", C.c_double), ("raster_s", C.c_double)]
 
 
 def lib():
@@ -59,6 +60,9 @@ def lib():
         L.or_render.argtypes = [C.POINTER(OrDraw), C.POINTER(OrFb), C.c_int, C.c_uint32,
                                 C.c_uint32, C.POINTER(OrStats)]
         L.or_render.restype = C.c_int
+        L.or_render_strided.argtypes = [C.POINTER(OrDraw), C.POINTER(OrFb), C.c_int, C.c_uint32, C.c_uint32,
+                                        C.c_uint32, C.POINTER(OrStats)]
+        L.or_render_strided.restype = C.c_int
         L.or_clear.argtypes = [C.POINTER(OrFb), C.c_void_p]
         L.or_tiles.argtypes = [C.c_uint32] * 4 + [C.POINTER(C.c_uint32), C.c_uint32,
                                                   C.POINTER(C.c_uint32)]
@@ -169,18 +173,26 @@ def raster_tris(scene):
     return out[:n.value]
 
 
-def render(scene, fb=None, n_threads=1, tile_begin=0, tile_end=0xFFFFFFFF):
+def render(scene, fb=None, n_threads=1, tile_begin=0, tile_end=0xFFFFFFFF, tile_step=1):
     """Renders `scene` (softrender.scenes.Scene) into fb (a new cleared one if
-    None); returns (fb, stats dict, status)."""
+    None); returns (fb, stats dict, status).  Only tiles tile_begin,
+    tile_begin + tile_step, ... below tile_end are rasterised (all by default;
+    a stride gives timing samples spread over the frame)."""
     if fb is None:
         fb = framebuffer_for(scene)
     keep = []
     d = _draw(scene, keep)
     st = OrStats()
     cfb = fb._c()
-    status = lib().or_render(C.byref(d), C.byref(cfb), n_threads, tile_begin, tile_end, C.byref(st))
+    if tile_step == 1:
+        status = lib().or_render(C.byref(d), C.byref(cfb), n_threads, tile_begin, tile_end, C.byref(st))
+    else:
+        n = max(0, -(-(min(tile_end, 0xFFFFFFFF) - tile_begin) // tile_step))
+        status = lib().or_render_strided(C.byref(d), C.byref(cfb), n_threads, tile_begin, tile_step,
+                                         min(n, 0xFFFFFFFF), C.byref(st))
     stats = dict(triangles_generated=st.triangles_generated, fragments=st.fragments,
-                 tiles=st.tiles, nan_bbox=st.nan_bbox)
+                 tiles=st.tiles, nan_bbox=st.nan_bbox, vertex_s=st.vertex_s, geometry_s=st.geometry_s,
+                 raster_s=st.raster_s)
     return fb, stats, status
 
 

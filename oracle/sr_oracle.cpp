@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -642,11 +643,19 @@ void or_coordinate_from_index(uint64_t index, uint32_t width, uint32_t* x, uint3
 }
 
 int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, uint32_t tile_end,
-                   or_stats* stats, float* tris_out, uint64_t tris_cap, uint64_t* n_tris_out);
+                   uint32_t tile_step, or_stats* stats, float* tris_out, uint64_t tris_cap, uint64_t* n_tris_out);
 
 int or_render(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, uint32_t tile_end,
               or_stats* stats) {
-    return or_render_impl(d, fb, n_threads, tile_begin, tile_end, stats, nullptr, 0, nullptr);
+    return or_render_impl(d, fb, n_threads, tile_begin, tile_end, 1, stats, nullptr, 0, nullptr);
+}
+
+int or_render_strided(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_first, uint32_t tile_step,
+                      uint32_t n, or_stats* stats) {
+    if (tile_step == 0) return 1;
+    const uint64_t end = (uint64_t)tile_first + (uint64_t)tile_step * n;
+    return or_render_impl(d, fb, n_threads, tile_first, (uint32_t)std::min<uint64_t>(end, 0xffffffffu), tile_step,
+                          stats, nullptr, 0, nullptr);
 }
 
 int or_raster_tris(const or_draw* d, uint32_t width, uint32_t height, float* out, uint64_t cap, uint64_t* n) {
@@ -654,11 +663,11 @@ int or_raster_tris(const or_draw* d, uint32_t width, uint32_t height, float* out
     std::memset(&fb, 0, sizeof(fb));
     fb.width = width;
     fb.height = height;
-    return or_render_impl(d, &fb, 1, 0, 0, nullptr, out, cap, n);
+    return or_render_impl(d, &fb, 1, 0, 0, 1, nullptr, out, cap, n);
 }
 
 int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, uint32_t tile_end,
-                   or_stats* stats, float* tris_out, uint64_t tris_cap, uint64_t* n_tris_out) {
+                   uint32_t tile_step, or_stats* stats, float* tris_out, uint64_t tris_cap, uint64_t* n_tris_out) {
     Ctx c;
     c.d = d;
     c.U = d->uniforms;
@@ -685,6 +694,9 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
     int nt = n_threads < 1 ? 1 : n_threads;
     const size_t vfetch = 64 * (size_t)(vs_planes(c.vs) * 4);
 
+    using clk = std::chrono::steady_clock;
+    const clk::time_point t_start = clk::now();
+
     /* vertex stage (vertex.rs:87-160) */
     std::vector<CV> verts(d->n_verts);
     if (d->gs_mode == 0) {
@@ -692,6 +704,8 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
     } else {
         mapper(d->n_verts, vfetch, nt, [&](size_t i) { verts[i] = run_vs(c, (uint32_t)i); });
     }
+
+    const clk::time_point t_vertex = clk::now();
 
     /* geometry stage (geometry.rs:132-258): each worker claims one primitive
      * per fetch_add and appends to its own storage; storages are merged in
@@ -737,6 +751,8 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
         norm_all(gen_points);
     }
 
+    const clk::time_point t_geometry = clk::now();
+
     if (tris_out || n_tris_out) {
         /* screen positions of the triangles the fragment stage rasterises */
         uint64_t k = 0;
@@ -758,14 +774,18 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
 
     /* fragment stage (fragment.rs:168-319) */
     std::vector<Tile> tiles = make_tiles(c.W, c.H, d->tile_w, d->tile_h);
+    // the tiles to rasterise, in row-major order: all of [tile_begin, tile_end)
+    // for or_render, every tile_step-th of them for timing samples
     uint32_t tb = std::min<uint32_t>(tile_begin, (uint32_t)tiles.size());
     uint32_t te = std::min<uint32_t>(tile_end, (uint32_t)tiles.size());
-    std::atomic<uint32_t> tile_counter{tb};
+    std::vector<uint32_t> sel;
+    for (uint64_t t = tb; t < te; t += std::max(1u, tile_step)) sel.push_back((uint32_t)t);
+    std::atomic<size_t> tile_counter{0};
     run_threads(nt, [&]() {
         for (;;) {
-            uint32_t ti = tile_counter.fetch_add(1, std::memory_order_relaxed);
-            if (ti >= te) break;
-            const Tile& tile = tiles[ti];
+            const size_t k = tile_counter.fetch_add(1, std::memory_order_relaxed);
+            if (k >= sel.size()) break;
+            const Tile& tile = tiles[sel[k]];
             if (pn == 3 && indexed)
                 for (uint64_t i = 0; i < d->n_indices; i += 3)
                     rasterize_triangle(c, tile, verts[d->indices[i]], verts[d->indices[i + 1]], verts[d->indices[i + 2]]);
@@ -784,7 +804,12 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
         }
     });
 
+    const clk::time_point t_raster = clk::now();
+
     if (stats) {
+        stats->vertex_s = std::chrono::duration<double>(t_vertex - t_start).count();
+        stats->geometry_s = std::chrono::duration<double>(t_geometry - t_vertex).count();
+        stats->raster_s = std::chrono::duration<double>(t_raster - t_geometry).count();
         stats->triangles_generated = gen_tris.size() / 3 + gen_lines.size() / 2 + gen_points.size();
         stats->fragments = c.fragments.load();
         stats->tiles = tiles.size();

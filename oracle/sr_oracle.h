@@ -59,6 +59,9 @@ typedef struct or_stats {
     uint64_t tiles;               /* semantic tiles in the frame             */
     uint32_t nan_bbox;            /* primitives with an all-NaN bbox         */
     uint32_t status;              /* 0 ok, else an sr_status code            */
+    double vertex_s;              /* wall time of the vertex stage           */
+    double geometry_s;            /* geometry stage + finish (clip GS only)  */
+    double raster_s;              /* fragment stage over the tiles rendered  */
 } or_stats;
 
 /* Renders one draw into fb.  n_threads == 1 is the normative (deterministic)
@@ -68,6 +71,11 @@ typedef struct or_stats {
  * tile list are rasterised (tile_end = UINT32_MAX for all). */
 int or_render(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, uint32_t tile_end,
               or_stats* stats);
+/* As or_render, rasterising only the n tiles tile_first, tile_first +
+ * tile_step, ... (those inside the tile list): a timing sample spread over
+ * the whole frame.  tile_step = 0 returns 1. */
+int or_render_strided(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_first, uint32_t tile_step,
+                      uint32_t n, or_stats* stats);
 
 /* Screen-space positions (x, y, z, 1/w per vertex, 12 floats per triangle)
  * of the triangles the fragment stage rasterises, after the vertex and

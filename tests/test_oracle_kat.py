@@ -317,3 +317,32 @@ def test_stencil_counts_pixels_failing_depth(oracle_mod):
     assert np.array_equal(fb.color, color) and np.array_equal(fb.depth, depth)
     xy = [(v[0], v[1]) for v in oracle_mod.raster_tris(front)[0]]
     assert np.array_equal(fb.stencil, 2 * _stencil_events_by_hand(xy, W, H, 4, 4))
+
+
+def test_strided_tiles_partition_the_frame(oracle_mod):
+    """The tile stride used for timing samples selects exactly every k-th tile:
+    for an opaque draw with a counting stencil (neither depends on the order
+    of tile passes) the even tiles then the odd tiles into one framebuffer
+    give the full frame, colour, depth and stencil, and their fragment
+    counts add up."""
+    sc = scenes.icosphere_scene(40, 30, subdiv=2, color_format=A.SR_COLOR_RGBA8)
+    sc.tile = (8, 8)
+    sc.stencil = True
+    sc.stencil_test, sc.stencil_op = A.SR_STENCIL_ALWAYS, A.SR_STENCIL_INCREMENT
+    full, st_full, s0 = oracle_mod.render(sc)
+    n = int(st_full["tiles"])
+    assert s0 == 0 and n == 20
+    fb = oracle_mod.framebuffer_for(sc)
+    frags = 0
+    for first in (0, 1):
+        fb, st, s = oracle_mod.render(sc, fb=fb, tile_begin=first, tile_step=2)
+        assert s == 0
+        frags += st["fragments"]
+    assert np.array_equal(fb.color, full.color)
+    assert np.array_equal(fb.depth.view(np.uint32), full.depth.view(np.uint32))
+    assert np.array_equal(fb.stencil, full.stencil)
+    assert frags == st_full["fragments"] > 0
+    # a window of 3 tiles with stride 7 rasterises tiles 2, 9, 16 only
+    _, st3, _ = oracle_mod.render(sc, tile_begin=2, tile_end=2 + 7 * 3, tile_step=7)
+    one = sum(oracle_mod.render(sc, tile_begin=t, tile_end=t + 1)[1]["fragments"] for t in (2, 9, 16))
+    assert st3["fragments"] == one
