@@ -247,6 +247,10 @@ SR_API int sr_mesh_upload(const float* const* planes, uint32_t n_planes, uint32_
  * on the device and the next sr_sync returns SR_EINVAL. */
 SR_API int sr_mesh_update(sr_mesh* m, const float* const* planes, uint32_t n_planes, uint32_t n_verts,
                           const uint32_t* indices, uint64_t n_indices, void* stream);
+/* Releases the caller's handle.  Meshes are shared like the reference's
+ * Arc<Mesh> (src/pipeline/mod.rs:146): a draw still pending on a pipeline
+ * (until its sr_sync, which may replay it) and a server request not yet read
+ * or released keep the mesh alive, and the last of them frees it. */
 SR_API int sr_mesh_free(sr_mesh* m);
 /* Device bytes held by a mesh (for HBM budgeting). */
 SR_API uint64_t sr_mesh_bytes(const sr_mesh* m);
@@ -256,6 +260,8 @@ SR_API int sr_texture_upload(const uint32_t* rgba8, uint32_t width, uint32_t hei
 /* Replaces the texels of an uploaded texture of the same size, ordered on
  * `stream` (NULL: synchronous). */
 SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, uint32_t width, uint32_t height, void* stream);
+/* Releases the caller's handle; pending draws and queued server requests
+ * keep the texture alive as sr_mesh_free describes. */
 SR_API int sr_texture_free(sr_texture* t);
 /* An RGBA f32 texture (four floats per texel, r first), sampled by the
  * textured shaders like the RGBA8 ones but without the /255 conversion. */

@@ -183,6 +183,11 @@ int sr::pipeline_retarget(sr_pipeline* p, uint32_t width, uint32_t height) {
 extern "C" SR_API int sr_pipeline_destroy(sr_pipeline* p) {
     if (!p) return SR_EINVAL;
     if (p->stream) cudaStreamSynchronize(p->stream);
+    for (const auto& pd : p->pending) {
+        mesh_unref(pd.d.mesh);
+        texture_unref(pd.d.texture);
+    }
+    p->pending.clear();
     if (p->color) cudaFree(p->color);
     if (p->depth) cudaFree(p->depth);
     if (p->stencil) cudaFree(p->stencil);
@@ -345,11 +350,19 @@ extern "C" SR_API int sr_mesh_update(sr_mesh* m, const float* const* planes, uin
     return SR_OK;
 }
 
-extern "C" SR_API int sr_mesh_free(sr_mesh* m) {
-    if (!m) return SR_EINVAL;
+void sr::mesh_unref(const sr_mesh* cm) {
+    sr_mesh* m = const_cast<sr_mesh*>(cm);
+    if (!m || m->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
     if (m->planes) cudaFree(m->planes);
     if (m->indices) cudaFree(m->indices);
     delete m;
+}
+
+// Releases the caller's reference; draws still pending on a pipeline (until
+// its sr_sync) and queued server requests keep the mesh alive.
+extern "C" SR_API int sr_mesh_free(sr_mesh* m) {
+    if (!m) return SR_EINVAL;
+    mesh_unref(m);
     return SR_OK;
 }
 
@@ -428,10 +441,16 @@ extern "C" SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t)
     return SR_OK;
 }
 
-extern "C" SR_API int sr_texture_free(sr_texture* t) {
-    if (!t) return SR_EINVAL;
+void sr::texture_unref(const sr_texture* ct) {
+    sr_texture* t = const_cast<sr_texture*>(ct);
+    if (!t || t->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
     if (t->data && !t->view) cudaFree(t->data);
     delete t;
+}
+
+extern "C" SR_API int sr_texture_free(sr_texture* t) {
+    if (!t) return SR_EINVAL;
+    texture_unref(t);
     return SR_OK;
 }
 
@@ -734,6 +753,9 @@ extern "C" SR_API int sr_render(sr_pipeline* p, const sr_draw* d) {
         p->outputs_intact = false;
         return rc;
     }
+    // the draw may be replayed from its descriptor until the next sr_sync
+    mesh_ref(pd.d.mesh);
+    texture_ref(pd.d.texture);
     p->prev = pd;
     p->have_prev = true;
     return SR_OK;
@@ -824,6 +846,10 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
             if (rc != SR_OK && status == SR_OK) status = rc;
         }
     p->pending_reads.clear();
+    for (const auto& pd : p->pending) {
+        mesh_unref(pd.d.mesh);
+        texture_unref(pd.d.texture);
+    }
     p->pending.clear();
     DeviceFlags z;
     std::memset(&z, 0, sizeof(z));

@@ -102,6 +102,16 @@ struct sr_pipeline {
 };
 
 namespace sr {
+// References to meshes and textures held by work that may still read them;
+// the release of the last one frees the object (see sr_mesh).
+inline void mesh_ref(const sr_mesh* m) {
+    if (m) const_cast<sr_mesh*>(m)->refs.fetch_add(1, std::memory_order_relaxed);
+}
+inline void texture_ref(const sr_texture* t) {
+    if (t) const_cast<sr_texture*>(t)->refs.fetch_add(1, std::memory_order_relaxed);
+}
+void mesh_unref(const sr_mesh* m);
+void texture_unref(const sr_texture* t);
 // Creates a pipeline whose planes hold cap_px pixels (>= width * height), so
 // that pipeline_retarget can later give it any frame of at most cap_px pixels.
 int pipeline_create_cap(const sr_fb_desc* fb, size_t cap_px, sr_pipeline** out);

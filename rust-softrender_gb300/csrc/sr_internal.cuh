@@ -18,10 +18,18 @@
 
 #include <cuda_runtime.h>
 #include <stddef.h>
+#include <atomic>
 #include <stdint.h>
 
 #include "sr.h"
 #include "sr_shaders.h"
+
+// `#pragma unroll` in functions the host compiles too (the device pass only)
+#ifdef __CUDA_ARCH__
+#define SR_UNROLL _Pragma("unroll")
+#else
+#define SR_UNROLL
+#endif
 
 namespace sr {
 
@@ -187,7 +195,7 @@ __host__ __device__ __forceinline__ bool segment_cleared(float4 r0, float4 r1, u
     const float s = det > 0.0f ? 1.0f : -1.0f;
     float nu[2], nv[2], Su[2], Sv[2];
     uint32_t xs[2] = {x0, x1}, ys[2] = {y0, y1};
-#pragma unroll
+SR_UNROLL
     for (int e = 0; e < 2; ++e) {
         float dx = ((float)xs[e] + 0.5f) - r1.x;
         float dy = ((float)ys[e] + 0.5f) - r1.y;
@@ -217,7 +225,7 @@ __host__ __device__ __forceinline__ bool rect_cleared(float4 r0, float4 r1, int 
     const float det = r1.z;
     const float s = det > 0.0f ? 1.0f : -1.0f;
     float nu[4], nv[4], su = 0.0f, sv = 0.0f, mu = 0.0f, mv = 0.0f;
-#pragma unroll
+SR_UNROLL
     for (int e = 0; e < 4; ++e) {
         const float dx = ((float)((e & 1) ? x1 : x0) + 0.5f) - r1.x;
         const float dy = ((float)((e & 2) ? y1 : y0) + 0.5f) - r1.y;
@@ -231,7 +239,7 @@ __host__ __device__ __forceinline__ bool rect_cleared(float4 r0, float4 r1, int 
     const float tiny = fabsf(det) * 1.0e-30f;
     bool cu = true, cv = true, cw = true;
     const float mw = 2.0f * g * (su + sv) + 16.0f * eps * (fabsf(det) + mu + mv);
-#pragma unroll
+SR_UNROLL
     for (int e = 0; e < 4; ++e) {
         cu = cu && (s * nu[e] + g * su + tiny < 0.0f);
         cv = cv && (s * nv[e] + g * sv + tiny < 0.0f);
@@ -243,22 +251,28 @@ __host__ __device__ __forceinline__ bool rect_cleared(float4 r0, float4 r1, int 
 }  // namespace sr
 
 // Opaque handles of the C ABI
+// Meshes and textures are shared like the reference's Arc<Mesh>
+// (src/pipeline/mod.rs:146): the caller's handle holds one reference, and so
+// does every draw that may still read the object (a pending draw until sync,
+// a queued server request until read); the last release frees it.
 struct sr_mesh {
-    float* planes;        // n_planes planes of n_pad floats
-    uint32_t n_planes;
-    uint32_t n_verts;
-    uint32_t n_pad;
-    uint32_t* indices;
-    uint64_t n_indices;
-    uint64_t bytes;
-    uint64_t version;     // bumped by every sr_mesh_update
+    float* planes = nullptr;        // n_planes planes of n_pad floats
+    uint32_t n_planes = 0;
+    uint32_t n_verts = 0;
+    uint32_t n_pad = 0;
+    uint32_t* indices = nullptr;
+    uint64_t n_indices = 0;
+    uint64_t bytes = 0;
+    uint64_t version = 0;           // bumped by every sr_mesh_update
+    std::atomic<uint32_t> refs{1};
 };
 
 struct sr_texture {
-    uint32_t* data;       // RGBA8 texels, or RGBA f32 texels (4 floats each) when f32
-    uint32_t w, h;
-    uint32_t f32;         // 1: RGBA f32 texels
-    bool view;            // reads a pipeline's colour plane in place (data not owned)
+    uint32_t* data = nullptr;       // RGBA8 texels, or RGBA f32 texels (4 floats each) when f32
+    uint32_t w = 0, h = 0;
+    uint32_t f32 = 0;               // 1: RGBA f32 texels
+    bool view = false;              // reads a pipeline's colour plane in place (data not owned)
+    std::atomic<uint32_t> refs{1};
 };
 
 // ------------------------------------------------------- grid sizing (host)

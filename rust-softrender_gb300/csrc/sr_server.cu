@@ -295,6 +295,9 @@ extern "C" SR_API int sr_server_submit(sr_server* s, const sr_request* r, uint64
     q->r.uniforms = nullptr;
     q->bytes = request_bytes(*r);
     if (q->bytes > s->cfg.hbm_budget) { delete q; return SR_EBUDGET; }
+    // the request reads its mesh and texture until it is read or released
+    mesh_ref(d->mesh);
+    texture_ref(d->texture);
     {
         std::lock_guard<std::mutex> lk(s->mu);
         q->ticket = s->next_ticket++;
@@ -348,6 +351,8 @@ int finish(sr_server* s, uint64_t ticket, void* color, float* depth) {
         s->in_use -= q->bytes;
     }
     s->cv.notify_all();
+    mesh_unref(q->r.draw.mesh);
+    texture_unref(q->r.draw.texture);
     delete q;
     return st == SR_ENAN ? SR_OK : st;
 }
@@ -428,6 +433,8 @@ extern "C" SR_API int sr_server_destroy(sr_server* s) {
     }
     for (auto& kv : s->reqs) {
         if (kv.second->target) sr_pipeline_destroy(kv.second->target);
+        mesh_unref(kv.second->r.draw.mesh);
+        texture_unref(kv.second->r.draw.texture);
         delete kv.second;
     }
     for (auto& kv : s->pool) sr_pipeline_destroy(kv.second);

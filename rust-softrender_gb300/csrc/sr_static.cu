@@ -186,8 +186,7 @@ extern "C" SR_API int sr_render_static(const sr_draw* d, const void* uniforms, s
         cudaMemsetAsync(bitmap, 0, ((nblk + 31) / 32) * sizeof(uint32_t), st) != cudaSuccess)
         return SR_ECUDA;
 
-    sr_mesh m;   // a view of the caller's buffers (owns nothing)
-    std::memset(&m, 0, sizeof(m));
+    sr_mesh m{};   // a view of the caller's buffers (owns nothing)
     m.planes = const_cast<float*>(planes);
     m.n_planes = n_planes;
     m.n_verts = n_verts;

@@ -122,3 +122,30 @@ def test_index_out_of_range(built_lib, oracle_mod):
     fb, _, _ = oracle_mod.render(sc)
     assert np.array_equal(color, fb.color.view(np.uint32).reshape(32, 32))
     assert np.array_equal(depth.view(np.uint32), fb.depth.view(np.uint32))
+
+
+def test_mesh_and_texture_freed_before_sync(built_lib, oracle_mod):
+    """Meshes and textures are shared like the reference's Arc<Mesh>
+    (src/pipeline/mod.rs:146): freeing the caller's handles right after
+    sr_render leaves them alive for the pending draw.  The first clipped draw
+    on a fresh pipeline outgrows its clip-output buffers (sized 2 x inputs +
+    4096), so sr_sync replays it from its descriptor after the handles are
+    gone; the frame still equals the oracle's."""
+    import softrender as sr
+    from util import compare_frame
+    sc = scenes.grid_sphere_scene(64, 48, n_lat=16, n_lon=32, tex_size=16, color_format=A.SR_COLOR_RGBA8)
+    assert sc.gs_mode == A.SR_GS_CLIP
+    pl, mesh, tex = sr.prepare_scene(sc)
+    try:
+        d = sr.draw_for_scene(sc, mesh, tex)
+        assert sr.lib().sr_render(pl.handle, C.byref(d)) == A.SR_OK
+        mesh.free()
+        tex.free()
+        assert pl.sync() == A.SR_OK
+        n_in = sc.indices.shape[0] // 3
+        assert pl.stats()["triangles_generated"] > 2 * n_in + 4096       # the draw was replayed
+        got = pl.read()
+    finally:
+        pl.destroy()
+    fb, _, _ = oracle_mod.render(sc)
+    compare_frame(got, fb)
