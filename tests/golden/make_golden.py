@@ -39,6 +39,12 @@ def golden_scenes():
         "points_70": scenes.lines_scene(n=800, size=70, seed=7, prim=A.SR_PRIM_POINT),
         "face_normals_96x64": scenes.icosphere_scene(96, 64, subdiv=2, gs_mode=A.SR_GS_NAMED, gs="face_normals",
                                                      fs="constant_color", tile=(32, 32)),
+        "vertex_normals_96x64": scenes.icosphere_scene(96, 64, subdiv=2, gs_mode=A.SR_GS_NAMED,
+                                                       gs="vertex_normals", fs="constant_color", tile=(32, 32)),
+        "icosphere_aces_rgba32f_96x72": scenes.icosphere_scene(96, 72, subdiv=3, fs="aces_lights"),
+        "icosphere_clip_aces_rgba8_80x64": scenes.icosphere_scene(80, 64, subdiv=2, gs_mode=A.SR_GS_CLIP,
+                                                                  color_format=A.SR_COLOR_RGBA8, fs="aces_lights",
+                                                                  cull=A.SR_CULL_COUNTER_CLOCKWISE, tile=(16, 16)),
     }
 
 

@@ -222,3 +222,14 @@ def test_ordered_bins_longer_than_16k(built_lib, oracle_mod):
     sc = scenes.stress_scene(n_tiny=64, n_large=40000, size=64, seed=3, seed_large=5)
     stats, _ = check(sc, oracle_mod)
     assert stats["bin_entries"] > 16 * 16384
+
+
+@pytest.mark.parametrize("fmt", [A.SR_COLOR_RGBA32F, A.SR_COLOR_RGBA8])
+@pytest.mark.parametrize("gs_mode", [A.SR_GS_NONE, A.SR_GS_CLIP])
+def test_aces_lights(built_lib, oracle_mod, fmt, gs_mode):
+    """The 4-point-light Blinn-Phong with the ACES tonemap
+    (full_example/src/shaders.rs:108-163)."""
+    sc = scenes.icosphere_scene(200, 150, subdiv=3, fs="aces_lights", color_format=fmt, gs_mode=gs_mode,
+                                tile=(64, 48))
+    stats, _ = check(sc, oracle_mod)
+    assert stats["fragments"] > 0
