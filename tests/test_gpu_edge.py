@@ -129,11 +129,14 @@ def test_mesh_and_texture_freed_before_sync(built_lib, oracle_mod):
     (src/pipeline/mod.rs:146): freeing the caller's handles right after
     sr_render leaves them alive for the pending draw.  The first clipped draw
     on a fresh pipeline outgrows its clip-output buffers (sized 2 x inputs +
-    4096), so sr_sync replays it from its descriptor after the handles are
+    4096; with stencil counting every inside triangle keeps its 16 fan
+    outputs), so sr_sync replays it from its descriptor after the handles are
     gone; the frame still equals the oracle's."""
     import softrender as sr
     from util import compare_frame
-    sc = scenes.grid_sphere_scene(64, 48, n_lat=16, n_lon=32, tex_size=16, color_format=A.SR_COLOR_RGBA8)
+    sc = scenes.grid_sphere_scene(64, 48, n_lat=16, n_lon=32, tex_size=16, color_format=A.SR_COLOR_RGBA8,
+                                  stencil=True, stencil_test=A.SR_STENCIL_ALWAYS,
+                                  stencil_op=A.SR_STENCIL_INCREMENT, stencil_wrap=1)
     assert sc.gs_mode == A.SR_GS_CLIP
     pl, mesh, tex = sr.prepare_scene(sc)
     try:
