@@ -191,7 +191,6 @@ void launch_setup_bin(const DrawParams& P, const uint32_t* vidx, VertexStore vs,
                       uint32_t* bin_counts, uint32_t* bin_off, uint32_t* bin_cursor, uint32_t* entries,
                       uint32_t* scan_tmp, uint32_t* unsafe_list, unsigned long long* area, const StencilCountArgs& S,
                       DeviceFlags* flags, cudaStream_t st) {
-    uint32_t n_bins = P.bins_x * P.bins_y;
     uint32_t n_host = P.n_raster_host;
     uint32_t n_launch = n_host ? n_host : P.gen_tri_cap;
     dim3 block(256), grid((n_launch + 255) / 256 ? (n_launch + 255) / 256 : 1);
@@ -203,7 +202,7 @@ void launch_setup_bin(const DrawParams& P, const uint32_t* vidx, VertexStore vs,
     // ordered path: setup only; bins are built by launch_bins (sr_bins.cu)
     setup_kernel<<<grid, block, 0, st>>>(P, n_host, vidx, vs.scr4, setup, reinterpret_cast<uint2*>(binrect),
                                          nullptr, unsafe_list, nullptr, S, flags);
-    (void)n_bins; (void)bin_off; (void)bin_cursor; (void)entries; (void)scan_tmp;
+    (void)bin_off; (void)bin_cursor; (void)entries; (void)scan_tmp;
 }
 
 }  // namespace sr
