@@ -933,8 +933,8 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
             std::memcpy(&c, it.clear_color, 4);
             I.clear_color = make_uint4(c, c, c, c);
         }
-        I.mx = (uint32_t)((0x100000000ull + d->tile_w - 1) / d->tile_w);
-        I.my = (uint32_t)((0x100000000ull + d->tile_h - 1) / d->tile_h);
+        I.mx = div_magic(d->tile_w);
+        I.my = div_magic(d->tile_h);
         hu[i] = p->U;
         if (!nothing) combos |= 1u << (d->fs * 3 + (int)p->fb.color_format);
         vbase += m->n_pad;

@@ -167,7 +167,7 @@ struct TileSpan {
     int first;   // first tile index containing the pixel
     int count;   // 1 or 2
 };
-__device__ __forceinline__ TileSpan tiles_of(uint32_t p, uint32_t t, uint32_t n, uint32_t last) {
+__host__ __device__ __forceinline__ TileSpan tiles_of(uint32_t p, uint32_t t, uint32_t n, uint32_t last) {
     TileSpan s;
     if (p > 0 && p < last && (p % t) == 0) { s.first = (int)(p / t) - 1; s.count = 2; }
     else { uint32_t c = p / t; if (c > n - 1) c = n - 1; s.first = (int)c; s.count = 1; }

@@ -18,11 +18,24 @@ __device__ __forceinline__ void mark_touched(uint32_t* bitmap, uint32_t blocks_x
     if (!(bitmap[b >> 5] & bit)) atomicOr(bitmap + (b >> 5), bit);
 }
 
-// ceil(2^32 / t): floor(p / t) == __umulhi(p, m) for p, t < 2^16
-__device__ __forceinline__ uint32_t div_magic(uint32_t t) { return (uint32_t)((0x100000000ull + t - 1) / t); }
+// high 32 bits of a 32 x 32-bit product
+__host__ __device__ __forceinline__ uint32_t umulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+// m = ceil(2^32 / t), so that floor(p / t) == umulhi32(p, m) for p < 2^15 and
+// 2 <= t < 2^16 (m = (2^32 + e) / t with e < t: the excess p e / (t 2^32)
+// stays below 1 / t).  For t == 1 it wraps to 0, which seam_count reads as
+// "every coordinate is a multiple of t".
+__host__ __device__ __forceinline__ uint32_t div_magic(uint32_t t) {
+    return (uint32_t)((0x100000000ull + t - 1) / t);
+}
 // number of semantic tiles along one axis containing coordinate p (1 or 2)
-__device__ __forceinline__ int seam_count(uint32_t p, uint32_t t, uint32_t m, uint32_t last) {
-    return (p > 0 && p < last && __umulhi(p, m) * t == p) ? 2 : 1;
+__host__ __device__ __forceinline__ int seam_count(uint32_t p, uint32_t t, uint32_t m, uint32_t last) {
+    return (p > 0 && p < last && (m == 0 || umulhi32(p, m) * t == p)) ? 2 : 1;
 }
 // mark the 32x32 blocks of a clamped bbox as touched
 __device__ __forceinline__ void mark_rect(uint32_t* bitmap, uint32_t blocks_x, uint32_t x0, uint32_t y0, uint32_t x1,

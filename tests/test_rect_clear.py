@@ -7,28 +7,19 @@ tests/rect_clear_check.cu calls the same header functions the kernels use,
 compiled by nvcc as host code, on random, sliver, sub-pixel and
 far-from-origin triangles, and evaluates every pixel of each cleared
 rectangle in f32 without contraction.  Needs nvcc, no GPU."""
-import os
 import re
-import shutil
 import subprocess
 
 import pytest
 
-HERE = os.path.dirname(os.path.abspath(__file__))
-ROOT = os.path.dirname(HERE)
-NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
+from util import build_host_check
 
 
 @pytest.fixture(scope="module")
 def checker(tmp_path_factory):
-    if not (os.path.exists(NVCC) or shutil.which("nvcc")):
+    exe = build_host_check("rect_clear_check.cu", tmp_path_factory.mktemp("rect_clear"))
+    if exe is None:
         pytest.skip("nvcc not available")
-    nvcc = NVCC if os.path.exists(NVCC) else shutil.which("nvcc")
-    exe = str(tmp_path_factory.mktemp("rect_clear") / "check")
-    subprocess.check_call([nvcc, "-std=c++17", "-O2", "-fmad=false", "-gencode", "arch=compute_103a,code=sm_103a",
-                           "-Xcompiler", "-ffp-contract=off,-fno-fast-math",
-                           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "rust-softrender_gb300", "csrc"),
-                           os.path.join(HERE, "rect_clear_check.cu"), "-o", exe])
     return exe
 
 

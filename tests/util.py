@@ -1,5 +1,30 @@
-"""Comparison helpers shared by the parity tests."""
+"""Comparison helpers shared by the parity tests, and the build of the host
+programs that check device helpers on the CPU."""
+import os
+import shutil
+import subprocess
+
 import numpy as np
+
+TESTS = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(TESTS)
+
+
+def build_host_check(src, out_dir):
+    """Compiles tests/<src> (a .cu file that calls __host__ __device__ helpers
+    of the library's headers) with nvcc as a host program and returns its path;
+    None when nvcc is not available."""
+    nvcc = "/usr/local/cuda/bin/nvcc"
+    if not os.path.exists(nvcc):
+        nvcc = shutil.which("nvcc")
+    if not nvcc:
+        return None
+    exe = os.path.join(str(out_dir), os.path.splitext(src)[0])
+    subprocess.check_call([nvcc, "-std=c++17", "-O2", "-fmad=false", "-gencode", "arch=compute_103a,code=sm_103a",
+                           "-Xcompiler", "-ffp-contract=off,-fno-fast-math",
+                           "-I", os.path.join(ROOT, "include"), "-I", os.path.join(ROOT, "rust-softrender_gb300", "csrc"),
+                           os.path.join(TESTS, src), "-o", exe])
+    return exe
 
 
 def ulp_diff_f32(a, b):
