@@ -40,3 +40,53 @@ def test_png_round_trip(tmp_path):
     sio.save_png(str(p), img)
     back = sio.load_png(str(p))
     assert back.dtype == np.uint32 and np.array_equal(back, img)
+
+
+def _reference_asset(rel):
+    """A file of the reference checkout (SOFTRENDER_REFERENCE, else the
+    checkout this repository was built beside); None where it is absent."""
+    import os
+    base = os.environ.get("SOFTRENDER_REFERENCE", "/root/reference")
+    p = os.path.join(base, rel)
+    return p if os.path.exists(p) else None
+
+
+def test_obj_reference_suzanne(oracle_mod):
+    """The reference example's mesh (examples/assets/suzanne.obj, loaded by
+    tobj in examples/suzanne.rs:24-47): 468 quads and 32 triangles become 968
+    triangles; every corner carries the position and normal its face names;
+    the mesh renders through the oracle with the example's shading."""
+    import math
+    import pytest
+    from softrender import _abi as A
+    from softrender import scenes
+    path = _reference_asset("examples/assets/suzanne.obj")
+    if path is None:
+        pytest.skip("the reference checkout is not present")
+    text = open(path).read()
+    pos, nrm, uv, idx = sio.load_obj(path)
+    assert idx.shape == (3 * 968,) and idx.max() < pos.shape[0]
+    assert nrm is not None and uv is not None and nrm.shape == pos.shape
+    # an independent reading of the corners, face by face, fan-triangulated
+    v = [tuple(map(float, l.split()[1:4])) for l in text.splitlines() if l.startswith("v ")]
+    vn = [tuple(map(float, l.split()[1:4])) for l in text.splitlines() if l.startswith("vn ")]
+    want_p, want_n = [], []
+    for l in text.splitlines():
+        if l.startswith("f "):
+            c = [tuple(int(x) for x in tok.split("/")) for tok in l.split()[1:]]
+            for i in range(1, len(c) - 1):
+                for k in (c[0], c[i], c[i + 1]):
+                    want_p.append(v[k[0] - 1])
+                    want_n.append(vn[k[2] - 1])
+    assert np.array_equal(pos[idx], np.asarray(want_p, np.float32))
+    assert np.array_equal(nrm[idx], np.asarray(want_n, np.float32))
+    # Blinn-Phong with one directional light, camera at distance 3 (examples/suzanne.rs)
+    W = H = 96
+    cam = (0.0, 0.0, 3.0)
+    u = scenes.make_uniforms(view=scenes.look_at_rh(cam, (0, 0, 0), (0, 1, 0)),
+                             projection=scenes.perspective(1.0, math.radians(60.0), 0.1, 100.0), camera=cam)
+    sc = scenes.Scene(planes=scenes._planes(pos, nrm), indices=idx, width=W, height=H,
+                      color_format=A.SR_COLOR_RGBA8, vs="mvp_pos_nrm", fs="blinn_phong_dir", uniforms=u,
+                      tile=(32, 32))
+    fb, st, status = oracle_mod.render(sc)
+    assert status == 0 and st["fragments"] > 1000
