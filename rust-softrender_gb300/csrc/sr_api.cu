@@ -614,7 +614,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
         if ((rc = p->pcount.ensure(n_raster_cap + 1)) || (rc = p->poff.ensure(n_raster_cap + 1)) ||
             (rc = p->pkeys0.ensure(p->entry_cap)) || (rc = p->pkeys1.ensure(p->entry_cap)) ||
             (rc = p->pvals0.ensure(p->entry_cap)) || (rc = p->pvals1.ensure(p->entry_cap)) ||
-            (rc = p->hist.ensure(256 * nblk)) || (rc = p->hist_off.ensure(256 * nblk)) ||
+            (rc = p->hist.ensure(256 * nblk)) || (rc = p->hist_off.ensure(256 * nblk + 1)) ||   // + the scan's total
             (rc = p->ranges.ensure(2 * (size_t)n_bins)) || (rc = p->bin_tmp.ensure(tmp)))
             return rc;
         B = BinBuffers{p->pcount.p, p->poff.p, p->bin_tmp.p, {p->pkeys0.p, p->pkeys1.p}, {p->pvals0.p, p->pvals1.p},

@@ -11,7 +11,7 @@ namespace sr {
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_ITEMS = 16;
 constexpr int SCAN_TILE = SCAN_THREADS * SCAN_ITEMS;   // 4096 elements per block
-constexpr int SCAN_MAX_BLOCKS = 8192;                    // 33.5M elements per scan
+constexpr int SCAN_MAX_BLOCKS = 8192;                    // block sums scanned in registers (33.5M elements)
 
 template <typename T>
 __device__ __forceinline__ T warp_inclusive_scan(T v) {
@@ -81,6 +81,33 @@ __global__ void scan_blocks_kernel(T* block_sums, uint32_t nb) {
     if (threadIdx.x == 0) block_sums[nb] = tot;
 }
 
+// The same for any number of block sums (scans of more than SCAN_MAX_BLOCKS
+// tiles): each thread takes a contiguous run of ceil(nb / 1024) sums and reads
+// it twice from global memory instead of holding it in registers.  The block
+// scan's barriers order every read before the first write.
+template <typename T>
+__global__ void scan_blocks_large_kernel(T* block_sums, uint32_t nb) {
+    constexpr int NT = 1024;
+    const uint32_t per = (nb + NT - 1) / NT;
+    const uint64_t j0 = (uint64_t)threadIdx.x * per;
+    T s = 0;
+    for (uint32_t i = 0; i < per; ++i) {
+        const uint64_t j = j0 + i;
+        if (j < nb) s += block_sums[j];
+    }
+    T tot;
+    T ex = block_exclusive_scan<T, NT>(s, &tot);
+    for (uint32_t i = 0; i < per; ++i) {
+        const uint64_t j = j0 + i;
+        if (j < nb) {
+            const T v = block_sums[j];
+            block_sums[j] = ex;
+            ex += v;
+        }
+    }
+    if (threadIdx.x == 0) block_sums[nb] = tot;
+}
+
 // Shared-memory slot of tile element e, padded by one element per 128 bytes
 // so that the blocked-per-thread accesses (thread t reads elements
 // t * SCAN_ITEMS ..) fall into distinct banks.
@@ -124,14 +151,17 @@ __global__ void scan_apply_kernel(const T* __restrict__ in, uint64_t n, const T*
 inline uint32_t scan_blocks(uint64_t n) { return (uint32_t)((n + SCAN_TILE - 1) / SCAN_TILE); }
 
 // tmp must hold scan_blocks(n) + 1 elements; out must hold n + 1.
-// Returns false if n exceeds the supported size.
+// Returns false if n exceeds the supported size (2^40 elements).
 template <typename T>
 inline bool exclusive_scan(const T* in, uint64_t n, T* out, T* tmp, cudaStream_t st) {
+    if (n > (1ull << 40)) return false;
     uint32_t nb = scan_blocks(n);
-    if (nb > (uint32_t)SCAN_MAX_BLOCKS) return false;
     if (nb == 0) nb = 1;
     scan_reduce_kernel<T><<<nb, SCAN_THREADS, 0, st>>>(in, n, tmp);
-    scan_blocks_kernel<T><<<1, 1024, 0, st>>>(tmp, nb);
+    if (nb <= (uint32_t)SCAN_MAX_BLOCKS)
+        scan_blocks_kernel<T><<<1, 1024, 0, st>>>(tmp, nb);
+    else
+        scan_blocks_large_kernel<T><<<1, 1024, 0, st>>>(tmp, nb);
     scan_apply_kernel<T><<<nb, SCAN_THREADS, 0, st>>>(in, n, tmp, nb, out);
     return true;
 }
