@@ -457,7 +457,7 @@ def _timed(fn):
     return time.perf_counter() - t0
 
 
-def run_served(rate=2000.0, duration=5.0, sat_duration=1.0):
+def run_served(rate=2000.0, duration=10.0, sat_duration=1.0):
     """Poisson request stream against the serving loop and against the plain
     per-request loop (same server code, one request at a time through
     sr_render + sr_sync): p50/p99 latency and throughput at `rate`, the plain

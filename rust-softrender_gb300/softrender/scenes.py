@@ -457,7 +457,7 @@ def batch_instances(n=256, seed=4, tri_lo=500, tri_hi=200000,
     return out
 
 
-def served_workload(rate=2000.0, duration=5.0, seed=5, pool=12, tri_lo=1000, tri_hi=500000,
+def served_workload(rate=2000.0, duration=10.0, seed=5, pool=12, tri_lo=1000, tri_hi=500000,
                     res_lo=(128, 128), res_hi=(1920, 1080)):
     """Request stream of the serving benchmark: a pool of resident seeded
     sphere meshes (triangle counts log-uniform in [tri_lo, tri_hi]) and
