@@ -374,14 +374,19 @@ def run_frames():
     pipeline (icosphere 5,120 tris, 1024^2 RGBA f32 + f32 depth, Blinn-Phong)
     and the ordering/tiny-triangle stress (16,777,216 tiny tris + 4,096 alpha
     tris, 2048^2 RGBA8 + f32 depth + u8 stencil, over-blend, stencil
-    increment)."""
+    increment, wrapping and saturating)."""
     import torch
     import softrender as sr
     from softrender import _abi as A
     from softrender import scenes
+    import copy
     out = {}
+    stress = scenes.stress_scene()                 # stencil Increment, wrapping
+    stress_sat = copy.copy(stress)                 # the same frame, Increment saturating
+    stress_sat.stencil_wrap = 0
     for key, sc, n in (("icosphere_5120tri_1024x1024_rgba32f", scenes.icosphere_scene(1024, 1024), 20),
-                       ("stress_16777216tiny_4096alpha_2048x2048_stencil", scenes.stress_scene(), 3)):
+                       ("stress_16777216tiny_4096alpha_2048x2048_stencil", stress, 3),
+                       ("stress_16777216tiny_4096alpha_2048x2048_stencil_saturate", stress_sat, 3)):
         pl, mesh, tex = sr.prepare_scene(sc)
         stream = torch.cuda.Stream()
         pl.set_stream(stream.cuda_stream)
