@@ -506,6 +506,14 @@ void rasterize_line(Ctx& c, const Tile& tile, const CV& st, const CV& en) {
                       (float)tile.x1, (float)tile.y1, o))
         return;
     float x1 = o[0], y1 = o[1], x2 = o[2], y2 = o[3];
+    /* a NaN clipped end point (a NaN or infinite vertex): cast(x1).unwrap()
+     * to i64 panics for Bresenham (line.rs:111-116), and Xiaolin Wu's
+     * `as i64` of NaN (line.rs:163) was undefined when the reference was
+     * written; the line is skipped and the draw reports status 7 */
+    if (std::isnan(x1) || std::isnan(y1) || std::isnan(x2) || std::isnan(y2)) {
+        c.nan_bbox.fetch_add(1, std::memory_order_relaxed);
+        return;
+    }
     float dlen = hypotf_(x1 - x2, y1 - y2);
     auto plot = [&](int64_t x, int64_t y, double a) { line_fragment(c, tile, st, en, x1, y1, dlen, x, y, a); };
     if (c.d->aa_lines) {

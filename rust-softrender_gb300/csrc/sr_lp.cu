@@ -428,6 +428,17 @@ __global__ void __launch_bounds__(32) raster_lp_kernel(DrawParams P, sr_uniforms
                 const float4 a = v[2 * (size_t)i].p, b = v[2 * (size_t)i + 1].p;
                 hit = liang_barsky(a.x, a.y, b.x, b.y, (float)tile.x0, (float)tile.y0, (float)tile.x1,
                                    (float)tile.y1, o);
+                // a NaN clipped end point (a NaN or infinite vertex): the
+                // reference's cast to i64 panics for Bresenham (line.rs:111-116)
+                // and is undefined for Xiaolin Wu (`as i64` of NaN, line.rs:163,
+                // before Rust 1.45); the line is skipped and the draw reports
+                // SR_ENAN (plotting it at 0 from every tile would also race
+                // between tiles of one phase)
+                if (hit && (isnan(o[0]) || isnan(o[1]) || isnan(o[2]) || isnan(o[3]))) {
+                    hit = false;
+                    atomicAdd(&flags->nan_total, 1u);
+                    atomicAdd(&flags->nan_bbox, 1u);
+                }
             } else {
                 const float4 a = v[i].p;
                 hit = (float)tile.x0 <= a.x && a.x < (float)tile.x1 && (float)tile.y0 <= a.y && a.y < (float)tile.y1;

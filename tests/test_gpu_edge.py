@@ -152,3 +152,17 @@ def test_mesh_and_texture_freed_before_sync(built_lib, oracle_mod):
         pl.destroy()
     fb, _, _ = oracle_mod.render(sc)
     compare_frame(got, fb)
+
+
+@pytest.mark.parametrize("aa", [False, True])
+def test_nan_line_end_point(built_lib, oracle_mod, aa):
+    """A line with a NaN vertex under stencil counting, Bresenham and Xiaolin
+    Wu: skipped with SR_ENAN where the reference's cast to i64 panics or is
+    undefined (line.rs:111-116, 163); the rest of the frame equals the
+    oracle's."""
+    sc = scenes.lines_scene(n=60, size=64, seed=21, tile=(16, 16), stencil=True, stencil_test=A.SR_STENCIL_ALWAYS,
+                            stencil_op=A.SR_STENCIL_INCREMENT, aa_lines=aa)
+    sc.planes[0] = sc.planes[0].copy()
+    sc.planes[0][2 * 7] = np.float32("nan")
+    stats, ostats = check(sc, oracle_mod)
+    assert stats["fragments"] > 0

@@ -346,3 +346,29 @@ def test_strided_tiles_partition_the_frame(oracle_mod):
     _, st3, _ = oracle_mod.render(sc, tile_begin=2, tile_end=2 + 7 * 3, tile_step=7)
     one = sum(oracle_mod.render(sc, tile_begin=t, tile_end=t + 1)[1]["fragments"] for t in (2, 9, 16))
     assert st3["fragments"] == one
+
+
+@pytest.mark.parametrize("aa", [False, True])
+def test_nan_line_end_point(oracle_mod, aa):
+    """A line with a NaN vertex: Liang-Barsky (line.rs:22-52) passes NaN end
+    points through; Bresenham's cast to i64 then panics in the reference
+    (line.rs:111-116) and Xiaolin Wu's `as i64` of NaN (line.rs:163) was
+    undefined when it was written, so the oracle skips the line and reports
+    status 7 -- the frame equals the scene without that line, stencil events
+    included."""
+    kw = dict(stencil=True, stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT, aa_lines=aa)
+    sc = scenes.lines_scene(n=60, size=64, seed=21, tile=(16, 16), **kw)
+    sc.planes[0] = sc.planes[0].copy()
+    sc.planes[0][2 * 7] = np.float32("nan")                      # line 7's first vertex
+    fb, st, status = oracle_mod.render(sc)
+    assert status == 7
+    keep = np.ones(sc.indices.shape[0], bool)
+    keep[14:16] = False
+    dropped = scenes.lines_scene(n=60, size=64, seed=21, tile=(16, 16), **kw)
+    dropped.indices = sc.indices[keep]
+    fb2, st2, status2 = oracle_mod.render(dropped)
+    assert status2 == 0
+    assert np.array_equal(fb.color, fb2.color)
+    assert np.array_equal(fb.depth.view(np.uint32), fb2.depth.view(np.uint32))
+    assert np.array_equal(fb.stencil, fb2.stencil)
+    assert st["fragments"] == st2["fragments"] > 0
