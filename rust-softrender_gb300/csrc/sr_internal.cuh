@@ -173,6 +173,20 @@ __host__ __device__ __forceinline__ TileSpan tiles_of(uint32_t p, uint32_t t, ui
     else { uint32_t c = p / t; if (c > n - 1) c = n - 1; s.first = (int)c; s.count = 1; }
     return s;
 }
+// Schedule of the line / point raster: tile (c, r) runs in phase c + K r, the
+// phases one after another and the tiles of a phase concurrently.  Tiles that
+// can write a common pixel (seams; Xiaolin Wu lines also plot one pixel beyond
+// their tile) are at most D tile columns apart, D = 1 + floor(2 / tile_w) for
+// Wu lines and 1 otherwise; K = D + 1 keeps any two of them in distinct
+// phases, in the row-major order the reference visits them.
+__host__ __device__ __forceinline__ uint32_t lp_phase_step(bool wu_lines, uint32_t tile_w) {
+    return (wu_lines && tile_w < 3) ? (tile_w == 2 ? 3u : 4u) : 2u;
+}
+// first tile row of phase `phase` (its column phase - K r is below ncols)
+__host__ __device__ __forceinline__ uint32_t lp_phase_first_row(uint32_t phase, uint32_t ncols, uint32_t kstep) {
+    return phase + 1 > ncols ? (phase - ncols + kstep) / kstep : 0u;
+}
+
 // Is coordinate p inside the projection of [i0, i1] clamped to tile index c?
 // (clamp_as_int of triangle.rs:66-78, with floor-rounded bbox ends)
 __device__ __forceinline__ bool clamp_axis(int i0, int i1, uint32_t p, uint32_t c, uint32_t t, uint32_t last) {

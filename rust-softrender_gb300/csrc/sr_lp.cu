@@ -400,17 +400,17 @@ __device__ void rasterize_line(const DrawParams& P, const sr_uniforms& U, const 
 #undef SR_PLOT
 }
 
-// One warp per semantic tile of phase `phase` (tile (r, c) with c + 2r ==
-// phase); primitives in submission order.
+// One warp per semantic tile of phase `phase` (tile (r, c) with
+// c + kstep * r == phase); primitives in submission order.
 template <int FS, int FMT, int BLEND>
-__global__ void __launch_bounds__(32) raster_lp_kernel(DrawParams P, sr_uniforms U, uint32_t phase,
+__global__ void __launch_bounds__(32) raster_lp_kernel(DrawParams P, sr_uniforms U, uint32_t phase, uint32_t kstep,
                                                        const LPV* __restrict__ v, const uint8_t* __restrict__ valid,
                                                        uint32_t n_prims, uint32_t prim_n, const uint32_t* tex,
                                                        void* color, float* depth, uint8_t* stencil,
                                                        DeviceFlags* flags) {
-    const int r_lo = phase + 1 > P.ncols ? (int)(phase - P.ncols + 2) / 2 : 0;
+    const int r_lo = (int)lp_phase_first_row(phase, P.ncols, kstep);
     const int r = r_lo + (int)blockIdx.x;
-    const int c = (int)phase - 2 * r;
+    const int c = (int)phase - (int)kstep * r;
     if (r >= (int)P.nrows || c < 0 || c >= (int)P.ncols) return;
     LPTile tile;
     tile.x0 = (uint32_t)c * P.tile_w;
@@ -497,10 +497,11 @@ template <int FS, int FMT, int BLEND>
 static void launch_lp_phases(const DrawParams& P, const sr_uniforms& U, const LPV* v, const uint8_t* valid,
                              uint32_t n_prims, uint32_t prim_n, const uint32_t* tex, void* color, float* depth,
                              uint8_t* stencil, DeviceFlags* flags, cudaStream_t st) {
-    const uint32_t phases = (P.ncols - 1) + 2 * (P.nrows - 1) + 1;
+    const uint32_t kstep = lp_phase_step(P.aa_lines && prim_n == 2, P.tile_w);
+    const uint32_t phases = (P.ncols - 1) + kstep * (P.nrows - 1) + 1;
     for (uint32_t ph = 0; ph < phases; ++ph)
-        raster_lp_kernel<FS, FMT, BLEND><<<P.nrows, 32, 0, st>>>(P, U, ph, v, valid, n_prims, prim_n, tex, color,
-                                                                 depth, stencil, flags);
+        raster_lp_kernel<FS, FMT, BLEND><<<P.nrows, 32, 0, st>>>(P, U, ph, kstep, v, valid, n_prims, prim_n, tex,
+                                                                 color, depth, stencil, flags);
 }
 
 uint32_t launch_lp_raster(const DrawParams& P, const sr_uniforms& U, const LPV* v, const uint8_t* valid,

@@ -91,3 +91,14 @@ def test_render_to_texture(built_lib, oracle_mod):
         pl.destroy()
         mesh.free()
         tex.free()
+
+
+@pytest.mark.parametrize("tile", [(1, 1), (2, 2), (1, 3), (2, 5)])
+def test_wu_lines_tiny_tiles(built_lib, oracle_mod, tile):
+    """Xiaolin Wu lines plot one pixel beyond their semantic tile; with tiles
+    1 or 2 pixels wide such pixels belong to tiles two columns away, which the
+    raster schedule keeps in later phases (over-blend and stencil counting
+    make the order visible)."""
+    sc = scenes.lines_scene(n=150, size=40, seed=31, aa_lines=True, blend="over", tile=tile, stencil=True,
+                            stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT)
+    check(sc, oracle_mod)
