@@ -46,9 +46,11 @@ typedef enum sr_status {
     SR_EOVERFLOW = 4,  /* a fixed-capacity device buffer overflowed             */
     SR_ETIMEOUT = 5,   /* a bounded device or host wait gave up                 */
     SR_ECUDA = 6,      /* a CUDA runtime call failed                            */
-    SR_ENAN = 7,       /* a primitive had an all-NaN bounding box; the reference
-                          panics in clamp_as_int (triangle.rs:66-78); here the
-                          primitive is skipped and the draw reports this code   */
+    SR_ENAN = 7,       /* a triangle had an all-NaN bounding box, or a line NaN
+                          end points after clipping; the reference panics in
+                          clamp_as_int (triangle.rs:66-78) or in the i64 cast of
+                          the end points (line.rs:111-116); here the primitive
+                          is skipped and the draw reports this code             */
     SR_ENOTFOUND = 8,  /* unknown shader name                                   */
     SR_EBUSY = 9       /* resource in use                                       */
 } sr_status;
