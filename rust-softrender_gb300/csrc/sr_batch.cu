@@ -803,6 +803,26 @@ extern "C" SR_API int sr_batch_get_config(sr_batch* b, uint32_t* ppw, uint32_t* 
     return SR_OK;
 }
 
+// The checks of one draw that sr_batch_render makes independently of its
+// target; the server makes them when a request is submitted, so that an
+// ineligible request is refused alone instead of failing its whole batch.
+int sr::batch_draw_check(const sr_draw* d) {
+    const sr_mesh* m = d ? d->mesh : nullptr;
+    if (!m) return SR_EINVAL;
+    if (d->prim != SR_PRIM_TRIANGLE || d->gs_mode != SR_GS_NONE || d->blend != BLEND_REPLACE) return SR_EINVAL;
+    if (d->reuse != SR_REUSE_NONE) return SR_EINVAL;
+    if (m->n_indices % 3 != 0) return SR_EINVAL;                            // mod.rs:148
+    if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT) return SR_EINVAL;
+    if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
+    if (d->tex_filter > SR_SAMPLE_BILINEAR || d->tex_edge > SR_SAMPLE_BORDER) return SR_EINVAL;
+    if (d->cull > SR_CULL_COUNTER_CLOCKWISE) return SR_EINVAL;
+    if (m->n_planes < (uint32_t)vs_planes(d->vs)) return SR_EINVAL;
+    if (vs_nk(d->vs) < batch_min_varyings(d->fs)) return SR_EINVAL;
+    if (d->fs == FS_TEXTURED_BLINN_PHONG && !d->texture) return SR_EINVAL;
+    if (d->texture && d->texture->view) return SR_EINVAL;   // another target of the batch may write it
+    return SR_OK;
+}
+
 extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, uint32_t n) {
     if (!b || (n && !items)) return SR_EINVAL;
     if (n == 0) return SR_OK;
@@ -818,17 +838,8 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         if (!p || !m) return SR_EINVAL;
         if (!p->pending.empty()) return SR_EBUSY;
         if (!seen.insert(p).second) return SR_EINVAL;                       // targets must be distinct
-        if (d->prim != SR_PRIM_TRIANGLE || d->gs_mode != SR_GS_NONE || d->blend != BLEND_REPLACE) return SR_EINVAL;
-        if (d->reuse != SR_REUSE_NONE) return SR_EINVAL;
-        if (m->n_indices % 3 != 0) return SR_EINVAL;                        // mod.rs:148
-        if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT) return SR_EINVAL;
-        if (d->tile_w == 0 || d->tile_h == 0 || d->tile_w > 65535 || d->tile_h > 65535) return SR_EINVAL;
-        if (d->tex_filter > SR_SAMPLE_BILINEAR || d->tex_edge > SR_SAMPLE_BORDER) return SR_EINVAL;
-        if (d->cull > SR_CULL_COUNTER_CLOCKWISE) return SR_EINVAL;
-        if (m->n_planes < (uint32_t)vs_planes(d->vs)) return SR_EINVAL;
-        if (vs_nk(d->vs) < batch_min_varyings(d->fs)) return SR_EINVAL;
-        if (d->fs == FS_TEXTURED_BLINN_PHONG && !d->texture) return SR_EINVAL;
-        if (d->texture && d->texture->view) return SR_EINVAL;   // another target of the batch may write it
+        const int rc = batch_draw_check(d);
+        if (rc != SR_OK) return rc;
         if (p->stencil && !(p->stencil_test == SR_STENCIL_ALWAYS && p->stencil_op == SR_STENCIL_KEEP)) return SR_EINVAL;
         const uint64_t npx = (uint64_t)p->fb.width * p->fb.height;
         slots += m->n_pad;

@@ -112,6 +112,9 @@ inline void texture_ref(const sr_texture* t) {
 }
 void mesh_unref(const sr_mesh* m);
 void texture_unref(const sr_texture* t);
+// Target-independent eligibility of a draw for sr_batch_render (SR_OK or
+// SR_EINVAL), shared with the server's submission checks.
+int batch_draw_check(const sr_draw* d);
 // Creates a pipeline whose planes hold cap_px pixels (>= width * height), so
 // that pipeline_retarget can later give it any frame of at most cap_px pixels.
 int pipeline_create_cap(const sr_fb_desc* fb, size_t cap_px, sr_pipeline** out);

@@ -280,12 +280,10 @@ extern "C" SR_API int sr_server_create(const sr_server_config* cfg, sr_server** 
 extern "C" SR_API int sr_server_submit(sr_server* s, const sr_request* r, uint64_t* ticket) {
     if (!s || !r || !ticket || !r->uniforms || r->uniforms_size != sizeof(sr_uniforms)) return SR_EINVAL;
     const sr_draw* d = &r->draw;
-    if (!d->mesh || d->prim != SR_PRIM_TRIANGLE || d->gs_mode != SR_GS_NONE || d->blend != BLEND_REPLACE ||
-        d->reuse != SR_REUSE_NONE)
-        return SR_EINVAL;
-    if (d->vs < 0 || d->vs >= VS_COUNT || d->fs < 0 || d->fs >= FS_COUNT) return SR_EINVAL;
-    if (d->fs == FS_TEXTURED_BLINN_PHONG && !d->texture) return SR_EINVAL;
-    if (d->texture && d->texture->view) return SR_EINVAL;   // batched with targets that may write it
+    // everything sr_batch_render checks of the draw alone: a request it would
+    // refuse is refused here, not with the batch it was folded into
+    const int rc = batch_draw_check(d);
+    if (rc != SR_OK) return rc;
     if (r->width == 0 || r->height == 0 || r->width > 32767 || r->height > 32767) return SR_EINVAL;
     if (r->color_format != SR_COLOR_RGBA8 && r->color_format != SR_COLOR_RGBA32F) return SR_EINVAL;
     Req* q = new (std::nothrow) Req();

@@ -98,3 +98,35 @@ def test_server_budget_admission(built_lib):
         srv.destroy()
         for m in meshes:
             m.free()
+
+
+def test_server_refuses_ineligible_request_alone(built_lib):
+    """A request sr_batch_render would refuse (a zero semantic tile width, an
+    unknown cull or texture edge mode) is refused when it is submitted, so it
+    cannot fail the batch it would have been folded into; the requests
+    around it are served and equal their renders alone."""
+    import softrender as sr
+    from softrender import _abi as A
+    scs, meshes, reqs = _requests(n=8, seed=23)
+    want = _alone(scs)
+    srv = sr.Server(max_inflight=1, max_batch=8)
+    try:
+        tickets = []
+        for k, r in enumerate(reqs):
+            if k == 4:
+                for field, val in (("tile_w", 0), ("cull", 9), ("tex_edge", 7)):
+                    bad = A.SrRequest.from_buffer_copy(reqs[0])
+                    setattr(bad.draw, field, val)
+                    st, _ = srv.submit(bad)
+                    assert st == A.SR_EINVAL, field
+            st, t = srv.submit(r)
+            assert st == 0
+            tickets.append(t)
+        for k, (t, sc) in enumerate(zip(tickets, scs)):
+            assert srv.wait(t) == 0
+            _check(srv.read(t, sc.width, sc.height, sc.color_format), want[k], k)
+        assert srv.stats()["submitted"] == len(reqs)
+    finally:
+        srv.destroy()
+        for m in meshes:
+            m.free()
