@@ -194,3 +194,30 @@ def test_ctypes_struct_layouts_match_header(tmp_path):
     subprocess.check_call(["g++", "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe])
     got = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split("\n")
     assert [g for g in got if g] == want
+
+
+def test_header_is_plain_c_and_links(built_lib, tmp_path):
+    """include/sr.h is a C header (the C ABI a Rust `-sys` crate, cgo or any
+    C caller binds): a C99 program compiles against it with -pedantic
+    -Werror, links against the library and calls its host-only entry points."""
+    import shutil
+    import subprocess
+    if not shutil.which("gcc"):
+        pytest.skip("gcc not available")
+    src = tmp_path / "c_abi.c"
+    src.write_text(
+        '#include <stdio.h>\n#include "sr.h"\n'
+        "int main(void) {\n"
+        "    sr_draw d;\n"
+        "    sr_draw_init(&d);\n"
+        '    printf("%s|%u|%u|%s\\n", sr_version(), d.tile_w, d.tile_h, sr_status_string(SR_ENAN));\n'
+        "    return 0;\n"
+        "}\n")
+    exe = str(tmp_path / "c_abi")
+    libdir = os.path.dirname(built_lib)
+    subprocess.check_call(["gcc", "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                           "-I", os.path.join(ROOT, "include"), str(src), "-o", exe,
+                           "-L", libdir, "-lsoftrender_gb300", "-Wl,-rpath," + libdir])
+    out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout.strip()
+    version, tw, th, name = out.split("|")
+    assert version.startswith("softrender-gb300") and (tw, th) == ("128", "128") and name == "SR_ENAN"
