@@ -34,7 +34,6 @@ the data path).
 """
 import argparse
 import json
-import math
 import os
 import subprocess
 import sys
@@ -254,7 +253,6 @@ def run_ours(args, rank, world, local):
             t = torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
             keep.append(t)
             return t.numpy()
-        import ctypes as C
         from softrender._lib import lib
         h_planes = [pinned(p) for p in scene.planes]
         h_idx = pinned(scene.indices)

@@ -5,7 +5,6 @@ CPU-baseline leg of bench.py, never by the product library.
 """
 import ctypes as C
 import os
-import sys
 
 import numpy as np
 

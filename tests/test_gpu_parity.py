@@ -198,7 +198,6 @@ def test_dense_bins_depth_ties(built_lib, oracle_mod):
 def test_read_async_matches_read(built_lib):
     """sr_framebuffer_read_async enqueues the copies; after sr_sync the host
     buffers equal a synchronous read."""
-    import ctypes as C
     import numpy as np
     from softrender._lib import lib
     sc = scenes.icosphere_scene(160, 120, color_format=A.SR_COLOR_RGBA8)
