@@ -215,7 +215,8 @@ SR_API int sr_pipeline_set_profiling(sr_pipeline* p, int enable);
 
 /* Framebuffer::clear (src/framebuffer/mod.rs:36, renderbuffer/mod.rs:125-133):
  * colour <- *color (float[4] for RGBA32F, uint8[4] for RGBA8), depth <- f32::MIN,
- * stencil <- 0. */
+ * stencil <- 0, ordered on the stream after the draws enqueued so far (and
+ * repeated in sequence if sr_sync has to replay them). */
 SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color);
 /* PixelRead / UnsafeFramebuffer getters (src/pixels/mod.rs:46-77): copy planes
  * to host memory (any pointer may be NULL); synchronises the pipeline stream. */
@@ -226,7 +227,9 @@ SR_API int sr_framebuffer_read(sr_pipeline* p, void* color, float* depth, uint8_
  * the frame after the next sr_sync, which redoes the copies if it had to
  * replay draws. */
 SR_API int sr_framebuffer_read_async(sr_pipeline* p, void* color, float* depth, uint8_t* stencil);
-/* PixelWrite / UnsafeFramebuffer setters: host planes -> device (NULL skips). */
+/* PixelWrite / UnsafeFramebuffer setters: host planes -> device (NULL skips).
+ * Draws still pending are settled first, as sr_sync does; their status is
+ * returned by the next sr_sync. */
 SR_API int sr_framebuffer_write(sr_pipeline* p, const void* color, const float* depth,
                                 const uint8_t* stencil);
 /* Device addresses of the planes (for device-resident consumers). */

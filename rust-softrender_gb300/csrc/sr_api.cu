@@ -238,8 +238,7 @@ extern "C" SR_API int sr_pipeline_set_stream(sr_pipeline* p, void* stream) {
 }
 
 // ============================================================ framebuffer
-extern "C" SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color) {
-    if (!p || !color) return SR_EINVAL;
+static int enqueue_clear(sr_pipeline* p, const void* color) {
     size_t n = (size_t)p->fb.width * p->fb.height;
     uint4 cv = make_uint4(0, 0, 0, 0);
     size_t cn = 0;
@@ -266,6 +265,21 @@ extern "C" SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color) {
     return SR_OK;
 }
 
+// Framebuffer::clear.  A clear between draws that sr_sync has not settled yet
+// is recorded with them: a replay after an overflow re-runs it in sequence.
+extern "C" SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color) {
+    if (!p || !color) return SR_EINVAL;
+    const int rc = enqueue_clear(p, color);
+    if (rc == SR_OK && !p->pending.empty()) {
+        PendingDraw pc{};
+        pc.clear = 1;
+        const uint32_t f = p->fb.color_format;
+        std::memcpy(pc.clear_color, color, f == SR_COLOR_RGBA32F ? 16 : f == SR_COLOR_RGBA8 ? 4 : 0);
+        p->pending.push_back(pc);
+    }
+    return rc;
+}
+
 extern "C" SR_API int sr_sync(sr_pipeline* p);
 
 extern "C" SR_API int sr_framebuffer_read(sr_pipeline* p, void* color, float* depth, uint8_t* stencil) {
@@ -281,6 +295,12 @@ extern "C" SR_API int sr_framebuffer_read(sr_pipeline* p, void* color, float* de
 
 extern "C" SR_API int sr_framebuffer_write(sr_pipeline* p, const void* color, const float* depth, const uint8_t* stencil) {
     if (!p) return SR_EINVAL;
+    // the host planes cannot be replayed later: settle the pending draws
+    // first (their status is kept for the next sr_sync)
+    if (!p->pending.empty()) {
+        const int st = sr_sync(p);
+        if (st != SR_OK && p->deferred_status == SR_OK) p->deferred_status = st;
+    }
     size_t n = (size_t)p->fb.width * p->fb.height;
     if (color && p->color) SR_CK(cudaMemcpyAsync(p->color, color, n * bytes_per_color(p->fb.color_format), cudaMemcpyHostToDevice, p->stream));
     if (depth && p->depth) SR_CK(cudaMemcpyAsync(p->depth, depth, n * 4, cudaMemcpyHostToDevice, p->stream));
@@ -799,8 +819,11 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
             p->last_stats.fragments = f.fragments;
             p->last_stats.nan_bbox = f.nan_bbox;
             p->last_stats.overflow = f.overflow_bits;
-            const sr_mesh* m = p->pending.back().d.mesh;
-            p->last_stats.triangles_in = m ? m->n_indices / std::max(1u, p->pending.back().d.prim) : 0;
+            const PendingDraw* last = nullptr;   // the last draw (clears may follow it)
+            for (auto it = p->pending.rbegin(); it != p->pending.rend() && !last; ++it)
+                if (!it->clear) last = &*it;
+            const sr_mesh* m = last ? last->d.mesh : nullptr;
+            p->last_stats.triangles_in = m ? m->n_indices / std::max(1u, last->d.prim) : 0;
             p->last_stats.kernel_launches = p->last_launches;
             if (p->last_profiled) {
                 p->last_stats.profiled = 1;
@@ -830,7 +853,8 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
         SR_CK(cudaStreamSynchronize(p->stream));
         if (status == SR_EOVERFLOW || from >= p->pending.size()) break;
         for (uint32_t i = from; i < p->pending.size(); ++i) {
-            int rc = enqueue_draw(p, p->pending[i], i, true);
+            const PendingDraw& e = p->pending[i];
+            const int rc = e.clear ? enqueue_clear(p, e.clear_color) : enqueue_draw(p, e, i, true);
             if (rc != SR_OK) { status = rc; break; }
         }
         replayed = true;
@@ -851,6 +875,8 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
         texture_unref(pd.d.texture);
     }
     p->pending.clear();
+    if (status == SR_OK) status = p->deferred_status;
+    p->deferred_status = SR_OK;
     DeviceFlags z;
     std::memset(&z, 0, sizeof(z));
     z.poison_draw = 0xffffffffu;

@@ -39,6 +39,8 @@ struct PendingDraw {
     sr_uniforms vU, gU;         // the vertex and geometry stages' (earlier ones under sr_draw.reuse)
     uint64_t mesh_version;      // of the mesh the vertex outputs derive from
     uint32_t stencil_test, stencil_op, stencil_wrap;
+    uint32_t clear = 0;         // 1: a framebuffer clear between draws, not a draw
+    uint8_t clear_color[16] = {};
 };
 
 }  // namespace sr
@@ -83,7 +85,8 @@ struct sr_pipeline {
     sr::DevBuf<unsigned long long> st_glob;
     // capacities (elements) requested for the generated geometry
     uint64_t gen_tri_cap = 0, gen_vert_cap = 0, entry_cap = 0;
-    std::vector<sr::PendingDraw> pending;
+    std::vector<sr::PendingDraw> pending;     // draws (and clears between them) since the last sync
+    int deferred_status = SR_OK;              // a status of draws synced early, for the next sr_sync
     // the previous sr_render (what sr_draw.reuse refers to), and whether the
     // stage-output buffers (vertex store, generated geometry, line/point
     // vertices) still hold its outputs

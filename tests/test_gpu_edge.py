@@ -166,3 +166,36 @@ def test_nan_line_end_point(built_lib, oracle_mod, aa):
     sc.planes[0][2 * 7] = np.float32("nan")
     stats, ostats = check(sc, oracle_mod)
     assert stats["fragments"] > 0
+
+
+def test_clear_between_draws_survives_replay(built_lib, oracle_mod):
+    """Draw A, clear, draw B, sync: A outgrows its clip-output buffers on the
+    fresh pipeline, so sync replays from A -- and must clear again before B,
+    as the sequence did (Framebuffer::clear between render_mesh calls).
+    The frame equals B alone on the cleared framebuffer, stencil included."""
+    import softrender as sr
+    from util import compare_frame
+    kw = dict(color_format=A.SR_COLOR_RGBA8, stencil=True, stencil_test=A.SR_STENCIL_ALWAYS,
+              stencil_op=A.SR_STENCIL_INCREMENT, stencil_wrap=1)
+    a = scenes.grid_sphere_scene(64, 48, n_lat=16, n_lon=32, tex_size=16, **kw)
+    b = scenes.icosphere_scene(64, 48, subdiv=2, **kw)
+    b.clear_color = (0.2, 0.4, 0.6, 1.0)
+    pl, mesh_a, tex_a = sr.prepare_scene(a)
+    mesh_b = sr.Mesh(b.planes, b.indices)
+    try:
+        L = sr.lib()
+        da = sr.draw_for_scene(a, mesh_a, tex_a)
+        assert L.sr_render(pl.handle, C.byref(da)) == A.SR_OK
+        pl.clear(list(b.clear_bytes()))
+        pl.set_uniforms(b.uniforms)
+        db = sr.draw_for_scene(b, mesh_b)
+        assert L.sr_render(pl.handle, C.byref(db)) == A.SR_OK
+        assert pl.sync() == A.SR_OK
+        got = pl.read()
+    finally:
+        pl.destroy()
+        mesh_a.free()
+        mesh_b.free()
+        tex_a.free()
+    fb, _, _ = oracle_mod.render(b)
+    compare_frame(got, fb)
