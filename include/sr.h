@@ -223,9 +223,9 @@ SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color);
 SR_API int sr_framebuffer_read(sr_pipeline* p, void* color, float* depth, uint8_t* stencil);
 /* Enqueues the same copies on the pipeline's stream after the draws enqueued
  * so far and returns at once (no counterpart in the reference, whose reads are
- * synchronous).  The host buffers (pinned for a truly asynchronous copy) hold
- * the frame after the next sr_sync, which redoes the copies if it had to
- * replay draws. */
+ * synchronous).  Once the next sr_sync returns, the host buffers (pinned for a
+ * truly asynchronous copy) hold the planes as they were at this point of the
+ * sequence: a replay of the draws repeats the copy in its place. */
 SR_API int sr_framebuffer_read_async(sr_pipeline* p, void* color, float* depth, uint8_t* stencil);
 /* PixelWrite / UnsafeFramebuffer setters: host planes -> device (NULL skips).
  * Draws still pending are settled first, as sr_sync does; their status is
@@ -273,8 +273,8 @@ SR_API int sr_texture_free(sr_texture* t);
 SR_API int sr_texture_upload_rgba32f(const float* rgba, uint32_t width, uint32_t height, sr_texture** out);
 /* Render to texture: copies a framebuffer's colour plane (RGBA8 or RGBA f32)
  * into a texture of the same size and texel type, ordered on the pipeline's
- * stream after its draws (sr_sync the pipeline before draws on other
- * pipelines sample it). */
+ * stream after its draws and repeated in its place if sr_sync replays them
+ * (sr_sync the pipeline before draws on other pipelines sample it). */
 SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t);
 /* Texture-buffer colour attachment (src/framebuffer/texturebuffer.rs:13-48,
  * 111-117, TextureBufferRef: the framebuffer's colour, stored apart from depth

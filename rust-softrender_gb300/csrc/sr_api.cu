@@ -272,7 +272,7 @@ extern "C" SR_API int sr_framebuffer_clear(sr_pipeline* p, const void* color) {
     const int rc = enqueue_clear(p, color);
     if (rc == SR_OK && !p->pending.empty()) {
         PendingDraw pc{};
-        pc.clear = 1;
+        pc.kind = PENDING_CLEAR;
         const uint32_t f = p->fb.color_format;
         std::memcpy(pc.clear_color, color, f == SR_COLOR_RGBA32F ? 16 : f == SR_COLOR_RGBA8 ? 4 : 0);
         p->pending.push_back(pc);
@@ -451,14 +451,26 @@ extern "C" SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, ui
     return SR_OK;
 }
 
+static int enqueue_texture_copy(sr_pipeline* p, const sr_texture* t) {
+    SR_CK(cudaMemcpyAsync(t->data, p->color, (size_t)t->w * t->h * (t->f32 ? 16 : 4), cudaMemcpyDeviceToDevice,
+                          p->stream));
+    return SR_OK;
+}
+
 extern "C" SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t) {
     if (!p || !t || t->view || !p->color) return SR_EINVAL;
     const uint32_t f = p->fb.color_format;
     if ((f != SR_COLOR_RGBA8 && f != SR_COLOR_RGBA32F) || t->f32 != (f == SR_COLOR_RGBA32F ? 1u : 0u)) return SR_EINVAL;
     if (t->w != p->fb.width || t->h != p->fb.height) return SR_EINVAL;
-    SR_CK(cudaMemcpyAsync(t->data, p->color, (size_t)t->w * t->h * (t->f32 ? 16 : 4), cudaMemcpyDeviceToDevice,
-                          p->stream));
-    return SR_OK;
+    const int rc = enqueue_texture_copy(p, t);
+    if (rc == SR_OK && !p->pending.empty()) {   // repeated in sequence if sync replays the draws
+        PendingDraw pt{};
+        pt.kind = PENDING_TEXTURE_COPY;
+        pt.d.texture = t;
+        texture_ref(t);
+        p->pending.push_back(pt);
+    }
+    return rc;
 }
 
 void sr::texture_unref(const sr_texture* ct) {
@@ -794,14 +806,20 @@ int enqueue_read(sr_pipeline* p, void* color, float* depth, uint8_t* stencil) {
 extern "C" SR_API int sr_framebuffer_read_async(sr_pipeline* p, void* color, float* depth, uint8_t* stencil) {
     if (!p) return SR_EINVAL;
     const int rc = enqueue_read(p, color, depth, stencil);
-    if (rc == SR_OK && !p->pending.empty()) p->pending_reads.push_back({color, depth, stencil});
+    if (rc == SR_OK && !p->pending.empty()) {   // repeated in sequence if sync replays the draws
+        PendingDraw pr{};
+        pr.kind = PENDING_READ;
+        pr.read_color = color;
+        pr.read_depth = depth;
+        pr.read_stencil = stencil;
+        p->pending.push_back(pr);
+    }
     return rc;
 }
 
 extern "C" SR_API int sr_sync(sr_pipeline* p) {
     if (!p) return SR_EINVAL;
     int status = SR_OK;
-    bool replayed = false;
     bool settled = false;   // the flags read clean after the last enqueue or replay
     for (int attempt = 0; attempt < 8; ++attempt) {
         SR_CK(cudaMemcpyAsync(p->hflags, p->flags, sizeof(DeviceFlags), cudaMemcpyDeviceToHost, p->stream));
@@ -821,7 +839,7 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
             p->last_stats.overflow = f.overflow_bits;
             const PendingDraw* last = nullptr;   // the last draw (clears may follow it)
             for (auto it = p->pending.rbegin(); it != p->pending.rend() && !last; ++it)
-                if (!it->clear) last = &*it;
+                if (it->kind == PENDING_DRAW) last = &*it;
             const sr_mesh* m = last ? last->d.mesh : nullptr;
             p->last_stats.triangles_in = m ? m->n_indices / std::max(1u, last->d.prim) : 0;
             p->last_stats.kernel_launches = p->last_launches;
@@ -854,22 +872,20 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
         if (status == SR_EOVERFLOW || from >= p->pending.size()) break;
         for (uint32_t i = from; i < p->pending.size(); ++i) {
             const PendingDraw& e = p->pending[i];
-            const int rc = e.clear ? enqueue_clear(p, e.clear_color) : enqueue_draw(p, e, i, true);
+            int rc = SR_OK;
+            switch (e.kind) {
+            case PENDING_CLEAR: rc = enqueue_clear(p, e.clear_color); break;
+            case PENDING_READ: rc = enqueue_read(p, e.read_color, e.read_depth, e.read_stencil); break;
+            case PENDING_TEXTURE_COPY: rc = enqueue_texture_copy(p, e.d.texture); break;
+            default: rc = enqueue_draw(p, e, i, true); break;
+            }
             if (rc != SR_OK) { status = rc; break; }
         }
-        replayed = true;
         if (status != SR_OK) break;
     }
     // out of attempts with the last replay unchecked, or poisoned without a draw
     // to replay: the frame is incomplete
     if (!settled && status == SR_OK) status = SR_EOVERFLOW;
-    // asynchronous reads copied a framebuffer that replayed draws changed
-    if (replayed)
-        for (const auto& r : p->pending_reads) {
-            const int rc = enqueue_read(p, r.color, r.depth, r.stencil);
-            if (rc != SR_OK && status == SR_OK) status = rc;
-        }
-    p->pending_reads.clear();
     for (const auto& pd : p->pending) {
         mesh_unref(pd.d.mesh);
         texture_unref(pd.d.texture);

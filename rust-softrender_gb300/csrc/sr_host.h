@@ -33,14 +33,22 @@ struct DevBuf {
     void release() { if (p) cudaFree(p); p = nullptr; cap = 0; }
 };
 
+// What a pending entry is: a draw, or an operation on the framebuffer ordered
+// between draws, which a replay (sr_sync after an overflow) repeats in
+// sequence.
+enum PendingKind : uint32_t { PENDING_DRAW = 0, PENDING_CLEAR = 1, PENDING_READ = 2, PENDING_TEXTURE_COPY = 3 };
+
 struct PendingDraw {
     sr_draw d;
     sr_uniforms U;              // the fragment stage's uniforms
     sr_uniforms vU, gU;         // the vertex and geometry stages' (earlier ones under sr_draw.reuse)
     uint64_t mesh_version;      // of the mesh the vertex outputs derive from
     uint32_t stencil_test, stencil_op, stencil_wrap;
-    uint32_t clear = 0;         // 1: a framebuffer clear between draws, not a draw
-    uint8_t clear_color[16] = {};
+    uint32_t kind = PENDING_DRAW;
+    uint8_t clear_color[16] = {};       // PENDING_CLEAR
+    void* read_color = nullptr;         // PENDING_READ: host destinations
+    float* read_depth = nullptr;
+    uint8_t* read_stencil = nullptr;    // (PENDING_TEXTURE_COPY: the texture is d.texture)
 };
 
 }  // namespace sr
@@ -93,8 +101,6 @@ struct sr_pipeline {
     sr::PendingDraw prev;
     bool have_prev = false;
     bool outputs_intact = false;
-    struct PendingRead { void* color; float* depth; uint8_t* stencil; };
-    std::vector<PendingRead> pending_reads;   // sr_framebuffer_read_async since the last sync
     sr_stats last_stats;
     bool stats_valid = false;
     bool force_unsafe = false;   // SR_FORCE_UNSAFE=1: every primitive takes the exact unsafe path

@@ -172,7 +172,9 @@ def test_clear_between_draws_survives_replay(built_lib, oracle_mod):
     """Draw A, clear, draw B, sync: A outgrows its clip-output buffers on the
     fresh pipeline, so sync replays from A -- and must clear again before B,
     as the sequence did (Framebuffer::clear between render_mesh calls).
-    The frame equals B alone on the cleared framebuffer, stencil included."""
+    The frame equals B alone on the cleared framebuffer, stencil included,
+    and an asynchronous read enqueued right after A holds A alone (the
+    replay repeats the copy in its place)."""
     import softrender as sr
     from util import compare_frame
     kw = dict(color_format=A.SR_COLOR_RGBA8, stencil=True, stencil_test=A.SR_STENCIL_ALWAYS,
@@ -186,6 +188,10 @@ def test_clear_between_draws_survives_replay(built_lib, oracle_mod):
         L = sr.lib()
         da = sr.draw_for_scene(a, mesh_a, tex_a)
         assert L.sr_render(pl.handle, C.byref(da)) == A.SR_OK
+        hc = np.zeros((a.height, a.width), np.uint32)
+        hd = np.zeros((a.height, a.width), np.float32)
+        hs = np.zeros((a.height, a.width), np.uint8)
+        assert L.sr_framebuffer_read_async(pl.handle, hc.ctypes.data, hd.ctypes.data, hs.ctypes.data) == A.SR_OK
         pl.clear(list(b.clear_bytes()))
         pl.set_uniforms(b.uniforms)
         db = sr.draw_for_scene(b, mesh_b)
@@ -199,3 +205,5 @@ def test_clear_between_draws_survives_replay(built_lib, oracle_mod):
         tex_a.free()
     fb, _, _ = oracle_mod.render(b)
     compare_frame(got, fb)
+    fa, _, _ = oracle_mod.render(a)
+    compare_frame((hc, hd, hs), fa)
