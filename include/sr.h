@@ -205,7 +205,9 @@ SR_API int sr_pipeline_set_uniforms(sr_pipeline* p, const void* uniforms, size_t
  * (src/pipeline/mod.rs:86-88, src/stencil.rs:182-199) */
 SR_API int sr_pipeline_set_stencil(sr_pipeline* p, int test, int op, int wrap);
 /* PipelineObject::threadpool_mut (src/pipeline/mod.rs:78): the CUDA stream
- * (cudaStream_t as void*) that render calls are ordered on; NULL = legacy default. */
+ * (cudaStream_t as void*) that render calls are ordered on; NULL = legacy default.
+ * Draws still pending on the previous stream are settled first, as sr_sync
+ * does; their status is returned by the next sr_sync. */
 SR_API int sr_pipeline_set_stream(sr_pipeline* p, void* stream);
 SR_API int sr_pipeline_destroy(sr_pipeline* p);
 /* Records CUDA events between the stages of every draw (no counterpart in the

@@ -231,8 +231,16 @@ extern "C" SR_API int sr_pipeline_set_stencil(sr_pipeline* p, int test, int op, 
     return SR_OK;
 }
 
+extern "C" SR_API int sr_sync(sr_pipeline* p);
+
 extern "C" SR_API int sr_pipeline_set_stream(sr_pipeline* p, void* stream) {
     if (!p) return SR_EINVAL;
+    // sr_sync waits on the current stream: settle draws enqueued on the old
+    // one first (their status is kept for the next sr_sync)
+    if (!p->pending.empty()) {
+        const int st = sr_sync(p);
+        if (st != SR_OK && p->deferred_status == SR_OK) p->deferred_status = st;
+    }
     p->stream = stream ? (cudaStream_t)stream : p->own_stream;
     return SR_OK;
 }
