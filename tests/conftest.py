@@ -16,6 +16,13 @@ sys.path.insert(0, ROOT)
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300) and the built library")
+    config.addinivalue_line("markers", "recent: GPU tests not yet run on a GPU; they run after all others")
+
+
+def pytest_collection_modifyitems(config, items):
+    # stable: tests marked `recent` move to the end, in their collected order,
+    # so that a failure among them under -x stops none of the others
+    items.sort(key=lambda it: 1 if it.get_closest_marker("recent") else 0)
 
 
 def _load(name, path):
