@@ -448,7 +448,13 @@ SR_API int sr_server_destroy(sr_server* s);
  * ordering between them) race and corrupt each other's output.  Order them
  * on one stream or with events.  The first call on each device looks up the
  * array's device address (cudaGetSymbolAddress, with that device current);
- * make that first call before any stream capture begins. */
+ * make that first call before any stream capture begins.  Under CUDA's lazy
+ * module loading (the default since CUDA 12.2) the driver loads this
+ * library's device code, and with it reserves the array, only when it is
+ * first needed on a device, which can be inside that first call: that
+ * reservation is the driver's, not this call's, but it takes the time of a
+ * device allocation, so make the first call on each device before a
+ * latency-critical loop (a draw of an empty mesh is enough). */
 #define SR_STATIC_MAX_PIXELS    (1u << 20)
 #define SR_STATIC_MAX_TRIANGLES (1u << 16)
 #define SR_STATIC_MAX_VERTICES  (1u << 16)

@@ -51,17 +51,37 @@ const ShaderName kShaders[] = {
     {"over", SR_STAGE_BLEND, BLEND_OVER},
 };
 
-// Clears a colour plane (cn 32-bit words, pattern cv repeating every 4 words)
-// and a depth plane (dn words of dv) with 16-byte stores in one launch.
-__global__ void clear_planes_kernel(uint32_t* __restrict__ c, size_t cn, uint4 cv, uint32_t* __restrict__ d, size_t dn,
-                                    uint32_t dv) {
+// Clears a colour plane (cn 32-bit words, pattern cv repeating every 4 words),
+// a depth plane (dn words of dv) and a stencil plane (sn bytes of 0) with
+// 16-byte stores in one launch.  Like every framebuffer write of a draw it
+// does nothing once the pipeline is poisoned: sr_sync then replays the draws
+// from the first poisoned one with the clears between them in their places,
+// and that replay must start from the framebuffer as the poisoned draw found it.
+__global__ void clear_planes_kernel(const DeviceFlags* __restrict__ flags, uint32_t* __restrict__ c, size_t cn, uint4 cv,
+                                    uint32_t* __restrict__ d, size_t dn, uint32_t dv, uint8_t* __restrict__ s, size_t sn) {
+    if (flags->poison) return;
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
-    const size_t c4 = cn / 4, d4 = dn / 4;
+    const size_t c4 = cn / 4, d4 = dn / 4, s16 = sn / 16;
     const uint4 dv4 = make_uint4(dv, dv, dv, dv);
     for (size_t j = i; j < c4; j += stride) reinterpret_cast<uint4*>(c)[j] = cv;
     for (size_t j = i; j < d4; j += stride) reinterpret_cast<uint4*>(d)[j] = dv4;
+    for (size_t j = i; j < s16; j += stride) reinterpret_cast<uint4*>(s)[j] = make_uint4(0, 0, 0, 0);
     if (i < cn - 4 * c4) c[4 * c4 + i] = (&cv.x)[i & 3];
     if (i < dn - 4 * d4) d[4 * d4 + i] = dv;
+    if (i < sn - 16 * s16) s[16 * s16 + i] = 0;
+}
+
+// Copies n 32-bit words of a colour plane into a texture unless the pipeline
+// is poisoned: a draw replayed by sr_sync may sample the texture, and must
+// find it as it was when the draw was first enqueued.
+__global__ void copy_plane_kernel(const DeviceFlags* __restrict__ flags, uint32_t* __restrict__ dst,
+                                  const uint32_t* __restrict__ src, size_t n) {
+    if (flags->poison) return;
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (size_t)gridDim.x * blockDim.x;
+    const size_t n4 = n / 4;
+    for (size_t j = i; j < n4; j += stride)
+        reinterpret_cast<uint4*>(dst)[j] = reinterpret_cast<const uint4*>(src)[j];
+    if (i < n - 4 * n4) dst[4 * n4 + i] = src[4 * n4 + i];
 }
 
 int fs_min_varyings(int fs) {
@@ -263,12 +283,13 @@ static int enqueue_clear(sr_pipeline* p, const void* color) {
     uint32_t dv;
     std::memcpy(&dv, &far_, 4);
     const size_t dn = p->depth ? n : 0;
-    const size_t work = std::max(cn, dn) / 4 + 4;
+    const size_t sn = p->stencil ? n : 0;
+    const size_t work = std::max(std::max(cn, dn) / 4, sn / 16) + 16;
     const unsigned grid = (unsigned)std::min<size_t>((work + 255) / 256, 152 * 16);
-    if (cn || dn)
-        clear_planes_kernel<<<grid, 256, 0, p->stream>>>(reinterpret_cast<uint32_t*>(p->color), cn, cv,
-                                                         reinterpret_cast<uint32_t*>(p->depth), dn, dv);
-    if (p->stencil) SR_CK(cudaMemsetAsync(p->stencil, 0, n, p->stream));
+    if (cn || dn || sn)
+        clear_planes_kernel<<<grid, 256, 0, p->stream>>>(p->flags, reinterpret_cast<uint32_t*>(p->color), cn, cv,
+                                                         reinterpret_cast<uint32_t*>(p->depth), dn, dv,
+                                                         p->stencil, sn);
     SR_CK(cudaGetLastError());
     return SR_OK;
 }
@@ -460,8 +481,10 @@ extern "C" SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, ui
 }
 
 static int enqueue_texture_copy(sr_pipeline* p, const sr_texture* t) {
-    SR_CK(cudaMemcpyAsync(t->data, p->color, (size_t)t->w * t->h * (t->f32 ? 16 : 4), cudaMemcpyDeviceToDevice,
-                          p->stream));
+    const size_t n = (size_t)t->w * t->h * (t->f32 ? 4 : 1);
+    const unsigned grid = (unsigned)std::min<size_t>((n / 4 + 4 + 255) / 256, 152 * 16);
+    copy_plane_kernel<<<grid, 256, 0, p->stream>>>(p->flags, t->data, static_cast<const uint32_t*>(p->color), n);
+    SR_CK(cudaGetLastError());
     return SR_OK;
 }
 

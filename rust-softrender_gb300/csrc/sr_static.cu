@@ -14,8 +14,11 @@
 //
 // The scratch is one file-scope __device__ array, sized for the limits
 // SR_STATIC_MAX_PIXELS, SR_STATIC_MAX_TRIANGLES and SR_STATIC_MAX_VERTICES of
-// include/sr.h (about 17.5 MiB).  Every GPU that loads this library holds it
-// until the process exits.  The kernels are the ones sr_render runs for the
+// include/sr.h (about 17.5 MiB).  Every GPU that loads this library's device
+// code holds it until the process exits; with CUDA's lazy module loading that
+// happens when the code is first needed on a device, which can be during the
+// first call there (include/sr.h says to make that call ahead of any
+// latency-critical loop).  The kernels are the ones sr_render runs for the
 // same draw (vertex, setup, the opaque raster passes and the resolve), so the
 // framebuffer comes out bit-identical; only where their scratch lives differs.
 //

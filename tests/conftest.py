@@ -20,9 +20,14 @@ def pytest_configure(config):
 
 
 def pytest_collection_modifyitems(config, items):
-    # stable: tests marked `recent` move to the end, in their collected order,
-    # so that a failure among them under -x stops none of the others
-    items.sort(key=lambda it: 1 if it.get_closest_marker("recent") else 0)
+    # stable: tests marked `recent` move towards the end, in their collected
+    # order, so that a failure among them under -x stops none of the others;
+    # the allocation-free entry point's file (test_zz_no_alloc.py) stays last
+    def rank(it):
+        if os.path.basename(str(it.fspath)) == "test_zz_no_alloc.py":
+            return 2
+        return 1 if it.get_closest_marker("recent") else 0
+    items.sort(key=rank)
 
 
 def _load(name, path):

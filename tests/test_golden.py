@@ -21,9 +21,6 @@ def _gen():
 
 GEN = _gen()
 NAMES = sorted(GEN.golden_scenes().keys())
-# fixtures whose scenes have not yet been rendered on a GPU (see `recent`)
-RECENT = {"vertex_normals_96x64", "icosphere_aces_rgba32f_96x72", "icosphere_clip_aces_rgba8_80x64"}
-GPU_NAMES = [pytest.param(n, marks=pytest.mark.recent) if n in RECENT else n for n in NAMES]
 
 
 def _load(name):
@@ -48,7 +45,7 @@ def test_oracle_reproduces_golden(oracle_mod, name):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("name", GPU_NAMES)
+@pytest.mark.parametrize("name", NAMES)
 def test_gpu_matches_golden(built_lib, name):
     import softrender as sr
     sc = GEN.golden_scenes()[name]

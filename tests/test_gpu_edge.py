@@ -124,7 +124,6 @@ def test_index_out_of_range(built_lib, oracle_mod):
     assert np.array_equal(depth.view(np.uint32), fb.depth.view(np.uint32))
 
 
-@pytest.mark.recent
 def test_mesh_and_texture_freed_before_sync(built_lib, oracle_mod):
     """Meshes and textures are shared like the reference's Arc<Mesh>
     (src/pipeline/mod.rs:146): freeing the caller's handles right after
@@ -155,7 +154,6 @@ def test_mesh_and_texture_freed_before_sync(built_lib, oracle_mod):
     compare_frame(got, fb)
 
 
-@pytest.mark.recent
 @pytest.mark.parametrize("aa", [False, True])
 def test_nan_line_end_point(built_lib, oracle_mod, aa):
     """A line with a NaN vertex under stencil counting, Bresenham and Xiaolin
@@ -170,7 +168,6 @@ def test_nan_line_end_point(built_lib, oracle_mod, aa):
     assert stats["fragments"] > 0
 
 
-@pytest.mark.recent
 def test_clear_between_draws_survives_replay(built_lib, oracle_mod):
     """Draw A, clear, draw B, sync: A outgrows its clip-output buffers on the
     fresh pipeline, so sync replays from A -- and must clear again before B,

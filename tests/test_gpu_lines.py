@@ -93,7 +93,6 @@ def test_render_to_texture(built_lib, oracle_mod):
         tex.free()
 
 
-@pytest.mark.recent
 @pytest.mark.parametrize("tile", [(1, 1), (2, 2), (1, 3), (2, 5)])
 def test_wu_lines_tiny_tiles(built_lib, oracle_mod, tile):
     """Xiaolin Wu lines plot one pixel beyond their semantic tile; with tiles

@@ -223,7 +223,6 @@ def test_ordered_bins_longer_than_16k(built_lib, oracle_mod):
     assert stats["bin_entries"] > 16 * 16384
 
 
-@pytest.mark.recent
 @pytest.mark.parametrize("fmt", [A.SR_COLOR_RGBA32F, A.SR_COLOR_RGBA8])
 @pytest.mark.parametrize("gs_mode", [A.SR_GS_NONE, A.SR_GS_CLIP])
 def test_aces_lights(built_lib, oracle_mod, fmt, gs_mode):

@@ -100,7 +100,6 @@ def test_server_budget_admission(built_lib):
             m.free()
 
 
-@pytest.mark.recent
 def test_server_refuses_ineligible_request_alone(built_lib):
     """A request sr_batch_render would refuse (a zero semantic tile width, an
     unknown cull or texture edge mode) is refused when it is submitted, so it

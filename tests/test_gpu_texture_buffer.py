@@ -131,7 +131,6 @@ def test_texture_views_rejected(built_lib):
         mesh.free()
 
 
-@pytest.mark.recent
 def test_unknown_sampler_modes_rejected(built_lib):
     """sr_filter has two values and sr_edge three; any other value is refused
     by sr_render, sr_batch_render and sr_render_static alike."""
