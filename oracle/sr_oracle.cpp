@@ -60,6 +60,16 @@ void run_threads(int n, F f) {
     for (auto& t : ts) t.join();
 }
 
+/* n workers, worker k receiving k (the deterministic mode's fixed split). */
+template <class F>
+void run_threads_indexed(int n, F f) {
+    if (n <= 1) { f(0); return; }
+    std::vector<std::thread> ts;
+    ts.reserve(n);
+    for (int i = 0; i < n; ++i) ts.emplace_back(f, i);
+    for (auto& t : ts) t.join();
+}
+
 /* Mapper::map / map_move (src/parallel.rs:57-111): chunks of
  * CACHE_LINE_SIZE * size_of::<U>() elements claimed by an atomic counter. */
 template <class F>
@@ -699,7 +709,15 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
     c.H = fb->height;
     c.has_stencil = fb->stencil != nullptr;
     c.sref = c.has_stencil ? (uint8_t)d->stencil_ref : 0;
-    int nt = n_threads < 1 ? 1 : n_threads;
+    /* n_threads < 0: |n_threads| workers in the deterministic mode, whose
+     * result equals the 1-thread order (the geometry stage's outputs are
+     * concatenated in input order, and the fragment stage runs the tiles in
+     * phases: tile (r, c) in phase c + 2 r (c + K r for Xiaolin Wu lines on
+     * tiles narrower than 3 pixels, which plot one pixel past their tile),
+     * so tiles sharing a pixel fall in distinct phases taken in row-major
+     * order, and the tiles of one phase, which share none, run concurrently). */
+    const bool phased = n_threads < 0;
+    int nt = phased ? -n_threads : (n_threads < 1 ? 1 : n_threads);
     const size_t vfetch = 64 * (size_t)(vs_planes(c.vs) * 4);
 
     using clk = std::chrono::steady_clock;
@@ -720,7 +738,33 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
      * the order the workers finish (lock order). */
     std::vector<CV> gen_tris, gen_lines, gen_points;
     bool indexed = d->gs_mode == 0;
-    if (!indexed) {
+    auto geometry_of = [&](uint64_t i, std::vector<CV>& tris, std::vector<CV>& lines, std::vector<CV>& points) {
+        CV v[3];
+        for (uint32_t j = 0; j < pn; ++j) v[j] = verts[d->indices[i + j]];
+        if (c.gs == GS_CLIP) {
+            if (pn == 3) clip_triangle(v[0], v[1], v[2], c.nk, tris);
+            else if (pn == 2) clip_line(v[0], v[1], c.nk, lines);
+            else clip_point(v[0], points);
+        } else {
+            std::vector<CV>& same = pn == 3 ? tris : pn == 2 ? lines : points;
+            gs_normals(c.gs, v, (int)pn, c.U, c.nk, lines, same);
+        }
+    };
+    if (!indexed && phased) {
+        /* contiguous primitive ranges per worker, concatenated in range order */
+        const uint64_t nprim = d->n_indices / pn;
+        const uint64_t chunk = (nprim + (uint64_t)nt - 1) / (uint64_t)nt;
+        std::vector<std::vector<CV>> tp(nt), lp(nt), pp(nt);
+        run_threads_indexed(nt, [&](int k) {
+            const uint64_t b = (uint64_t)k * chunk, e = std::min<uint64_t>(b + chunk, nprim);
+            for (uint64_t q = b; q < e; ++q) geometry_of(q * pn, tp[k], lp[k], pp[k]);
+        });
+        for (int k = 0; k < nt; ++k) {
+            gen_tris.insert(gen_tris.end(), tp[k].begin(), tp[k].end());
+            gen_lines.insert(gen_lines.end(), lp[k].begin(), lp[k].end());
+            gen_points.insert(gen_points.end(), pp[k].begin(), pp[k].end());
+        }
+    } else if (!indexed) {
         std::atomic<uint64_t> next{0};
         std::mutex mu;
         std::vector<std::vector<CV>> tri_parts, line_parts, point_parts;
@@ -729,16 +773,7 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
             for (;;) {
                 uint64_t i = next.fetch_add(pn, std::memory_order_relaxed);
                 if (i >= d->n_indices) break;
-                CV v[3];
-                for (uint32_t j = 0; j < pn; ++j) v[j] = verts[d->indices[i + j]];
-                if (c.gs == GS_CLIP) {
-                    if (pn == 3) clip_triangle(v[0], v[1], v[2], c.nk, tris);
-                    else if (pn == 2) clip_line(v[0], v[1], c.nk, lines);
-                    else clip_point(v[0], points);
-                } else {
-                    std::vector<CV>& same = pn == 3 ? tris : pn == 2 ? lines : points;
-                    gs_normals(c.gs, v, (int)pn, c.U, c.nk, lines, same);
-                }
+                geometry_of(i, tris, lines, points);
             }
             std::lock_guard<std::mutex> g(mu);
             tri_parts.push_back(std::move(tris));
@@ -748,6 +783,8 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
         for (auto& p : tri_parts) gen_tris.insert(gen_tris.end(), p.begin(), p.end());
         for (auto& p : line_parts) gen_lines.insert(gen_lines.end(), p.begin(), p.end());
         for (auto& p : point_parts) gen_points.insert(gen_points.end(), p.begin(), p.end());
+    }
+    if (!indexed) {
         /* finish (geometry.rs:60-129): normalise every generated vertex */
         auto norm_all = [&](std::vector<CV>& vv) {
             std::vector<CV> out(vv.size());
@@ -788,29 +825,54 @@ int or_render_impl(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_beg
     uint32_t te = std::min<uint32_t>(tile_end, (uint32_t)tiles.size());
     std::vector<uint32_t> sel;
     for (uint64_t t = tb; t < te; t += std::max(1u, tile_step)) sel.push_back((uint32_t)t);
-    std::atomic<size_t> tile_counter{0};
-    run_threads(nt, [&]() {
-        for (;;) {
-            const size_t k = tile_counter.fetch_add(1, std::memory_order_relaxed);
-            if (k >= sel.size()) break;
-            const Tile& tile = tiles[sel[k]];
-            if (pn == 3 && indexed)
-                for (uint64_t i = 0; i < d->n_indices; i += 3)
-                    rasterize_triangle(c, tile, verts[d->indices[i]], verts[d->indices[i + 1]], verts[d->indices[i + 2]]);
-            for (size_t i = 0; i + 2 < gen_tris.size(); i += 3)
-                rasterize_triangle(c, tile, gen_tris[i], gen_tris[i + 1], gen_tris[i + 2]);
-            if (pn == 2 && indexed)
-                for (uint64_t i = 0; i < d->n_indices; i += 2)
-                    rasterize_line(c, tile, verts[d->indices[i]], verts[d->indices[i + 1]]);
-            for (size_t i = 0; i + 1 < gen_lines.size(); i += 2)
-                rasterize_line(c, tile, gen_lines[i], gen_lines[i + 1]);
-            if (pn == 1 && indexed)
-                for (uint64_t i = 0; i < d->n_indices; ++i)
-                    rasterize_point(c, tile, verts[d->indices[i]]);
-            for (size_t i = 0; i < gen_points.size(); ++i)
-                rasterize_point(c, tile, gen_points[i]);
+    auto raster_tile = [&](const Tile& tile) {
+        if (pn == 3 && indexed)
+            for (uint64_t i = 0; i < d->n_indices; i += 3)
+                rasterize_triangle(c, tile, verts[d->indices[i]], verts[d->indices[i + 1]], verts[d->indices[i + 2]]);
+        for (size_t i = 0; i + 2 < gen_tris.size(); i += 3)
+            rasterize_triangle(c, tile, gen_tris[i], gen_tris[i + 1], gen_tris[i + 2]);
+        if (pn == 2 && indexed)
+            for (uint64_t i = 0; i < d->n_indices; i += 2)
+                rasterize_line(c, tile, verts[d->indices[i]], verts[d->indices[i + 1]]);
+        for (size_t i = 0; i + 1 < gen_lines.size(); i += 2)
+            rasterize_line(c, tile, gen_lines[i], gen_lines[i + 1]);
+        if (pn == 1 && indexed)
+            for (uint64_t i = 0; i < d->n_indices; ++i)
+                rasterize_point(c, tile, verts[d->indices[i]]);
+        for (size_t i = 0; i < gen_points.size(); ++i)
+            rasterize_point(c, tile, gen_points[i]);
+    };
+    if (phased) {
+        uint32_t ncols = 0;
+        while (ncols < tiles.size() && tiles[ncols].y0 == tiles[0].y0) ++ncols;
+        const bool wu_narrow = d->aa_lines && (pn == 2 || !gen_lines.empty()) && d->tile_w < 3;
+        const uint32_t K = wu_narrow ? (d->tile_w == 2 ? 3u : 4u) : 2u;
+        std::vector<std::vector<uint32_t>> phases;
+        for (uint32_t t : sel) {
+            const uint32_t ph = (t % ncols) + K * (t / ncols);
+            if (ph >= phases.size()) phases.resize(ph + 1);
+            phases[ph].push_back(t);
         }
-    });
+        for (const auto& ph : phases) {
+            std::atomic<size_t> next{0};
+            run_threads(std::min<int>(nt, (int)ph.size()), [&]() {
+                for (;;) {
+                    const size_t k = next.fetch_add(1, std::memory_order_relaxed);
+                    if (k >= ph.size()) break;
+                    raster_tile(tiles[ph[k]]);
+                }
+            });
+        }
+    } else {
+        std::atomic<size_t> tile_counter{0};
+        run_threads(nt, [&]() {
+            for (;;) {
+                const size_t k = tile_counter.fetch_add(1, std::memory_order_relaxed);
+                if (k >= sel.size()) break;
+                raster_tile(tiles[sel[k]]);
+            }
+        });
+    }
 
     const clk::time_point t_raster = clk::now();
 

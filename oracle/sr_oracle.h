@@ -67,7 +67,10 @@ typedef struct or_stats {
 /* Renders one draw into fb.  n_threads == 1 is the normative (deterministic)
  * order; n_threads > 1 mirrors Pool::new(num_cpus) with its atomic-counter
  * work split (outputs then race on seam pixels exactly as the reference's do
- * and are not compared).  Only tiles [tile_begin, tile_end) of the row-major
+ * and are not compared); n_threads < 0 runs -n_threads workers in an order
+ * whose result equals the 1-thread order (geometry outputs concatenated in
+ * input order, tiles in phases that never run two tiles sharing a pixel at
+ * once).  Only tiles [tile_begin, tile_end) of the row-major
  * tile list are rasterised (tile_end = UINT32_MAX for all). */
 int or_render(const or_draw* d, or_fb* fb, int n_threads, uint32_t tile_begin, uint32_t tile_end,
               or_stats* stats);

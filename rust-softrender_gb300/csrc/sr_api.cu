@@ -178,6 +178,8 @@ int sr::pipeline_create_cap(const sr_fb_desc* fb, size_t cap_px, sr_pipeline** o
     p->stream = p->own_stream;
     const char* fu = std::getenv("SR_FORCE_UNSAFE");
     p->force_unsafe = fu && fu[0] == '1';
+    const char* ok = std::getenv("SR_OPAQUE_KEYS");
+    p->opaque_keys = ok && ok[0] == '1';
     DeviceFlags z;
     std::memset(&z, 0, sizeof(z));
     z.poison_draw = 0xffffffffu;
@@ -215,7 +217,7 @@ extern "C" SR_API int sr_pipeline_destroy(sr_pipeline* p) {
     if (p->hflags) cudaFreeHost(p->hflags);
     p->clip4.release(); p->scr4.release(); p->vary.release();
     p->clip_counts.release(); p->clip_offsets.release(); p->clip_tmp.release(); p->refs.release();
-    p->setup.release(); p->binrect.release();
+    p->setup.release(); p->unsafe_rect.release(); p->binrect.release();
     p->bin_counts.release(); p->bin_off.release(); p->bin_cursor.release(); p->bin_tmp.release(); p->entries.release(); p->unsafe_list.release();
     p->st_diff.release(); p->st_lines.release(); p->st_glob.release();
     p->area.release(); p->big_list.release(); p->gkeys.release(); p->bitmap.release();
@@ -668,7 +670,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
             return rc;
     }
     if ((rc = p->setup.ensure(4 * n_raster_cap)) || (rc = p->binrect.ensure(n_raster_cap)) ||
-        (rc = p->unsafe_list.ensure(n_raster_cap)))
+        (rc = p->unsafe_list.ensure(n_raster_cap)) || (rc = p->unsafe_rect.ensure(n_raster_cap)))
         return rc;
     BinBuffers B{};
     if (ordered && !P.mode_b) {
@@ -683,18 +685,28 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
         B = BinBuffers{p->pcount.p, p->poff.p, p->bin_tmp.p, {p->pkeys0.p, p->pkeys1.p}, {p->pvals0.p, p->pvals1.p},
                        p->hist.p, p->hist_off.p, p->ranges.p, p->entry_cap};
     }
+    // opaque draws: binned (sr_tiled.cu) unless SR_OPAQUE_KEYS selects the
+    // global key buffer path (sr_opaque.cu)
+    const bool tiled = !ordered && !p->opaque_keys;
     if (!ordered) {
         const size_t npx = (size_t)W * H;
         const size_t nblk = (size_t)((W + 31) / 32) * ((H + 31) / 32);
         const bool fresh = p->gkeys.cap < npx || p->bitmap.cap < (nblk + 31) / 32;
-        if ((rc = p->area.ensure(n_raster_cap + 1)) || (rc = p->big_list.ensure(n_raster_cap + 1)) ||
-            (rc = p->gkeys.ensure(npx)) ||
-            (rc = p->bitmap.ensure((nblk + 31) / 32)))
+        if (tiled) {
+            if ((rc = p->bin_counts.ensure(2 * (size_t)n_bins)) || (rc = p->bin_off.ensure((size_t)n_bins + 1)) ||
+                (rc = p->entries.ensure(p->entry_cap)) || (rc = p->gkeys.ensure(npx)) ||
+                (rc = p->bitmap.ensure((nblk + 31) / 32)))
+                return rc;
+        } else if ((rc = p->area.ensure(n_raster_cap + 1)) || (rc = p->big_list.ensure(n_raster_cap + 1)) ||
+                   (rc = p->gkeys.ensure(npx)) || (rc = p->bitmap.ensure((nblk + 31) / 32))) {
             return rc;
-        if (fresh) {   // zero once; the resolve pass leaves them zero
+        }
+        if (fresh) {   // zero once; the raster passes leave them zero
             SR_CK(cudaMemsetAsync(p->gkeys.p, 0, p->gkeys.cap * 8, st));
             SR_CK(cudaMemsetAsync(p->bitmap.p, 0, p->bitmap.cap * 4, st));
         }
+        // the bin counts and slot cursors start at zero in every draw
+        if (tiled) SR_CK(cudaMemsetAsync(p->bin_counts.p, 0, 2 * (size_t)n_bins * 4, st));
     }
     StencilCountArgs S{nullptr, nullptr, nullptr};
     if (P.stencil_active && !P.mode_b) {
@@ -730,8 +742,9 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
         vidx = p->refs.p;
     }
     if (ev) cudaEventRecord(ev[2], st);
-    launch_setup_bin(P, vidx, vs, p->setup.p, reinterpret_cast<uint32_t*>(p->binrect.p), nullptr, nullptr,
-                     nullptr, nullptr, nullptr, p->unsafe_list.p, ordered ? nullptr : p->area.p, S, p->flags, st);
+    launch_setup_bin(P, vidx, vs, p->setup.p, reinterpret_cast<uint32_t*>(p->binrect.p),
+                     tiled ? p->bin_counts.p : nullptr, nullptr, nullptr, nullptr, nullptr, p->unsafe_list.p,
+                     p->unsafe_rect.p, (ordered || tiled) ? nullptr : p->area.p, S, p->flags, st);
     launches += 1;
     const uint32_t* bin_list = nullptr;
     if (ordered && !P.mode_b) {
@@ -746,9 +759,14 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
         launch_ordered(P, pd.U, p->setup.p, P.mode_b ? nullptr : p->ranges.p, bin_list, vidx, p->vary.p, tex, p->color,
                        p->depth, p->stencil, gate, p->flags, st);
         launches += 1;
+    } else if (tiled) {
+        TiledArgs T{p->setup.p, p->binrect.p, p->bin_counts.p, p->bin_counts.p + n_bins, p->bin_off.p, p->entries.p,
+                    p->entry_cap, p->gkeys.p, p->bitmap.p, p->unsafe_list.p, p->unsafe_rect.p, vidx, p->vary.p,
+                    tex, p->color, p->depth, p->stencil, gate, p->flags};
+        launches += (uint32_t)launch_tiled(P, pd.U, T, st);
     } else {
         OpaqueArgs A{p->setup.p, p->area.p, p->big_list.p, p->gkeys.p, p->bitmap.p, p->unsafe_list.p,
-                     vidx, p->vary.p, tex, p->color, p->depth, p->stencil, gate, p->flags};
+                     p->unsafe_rect.p, vidx, p->vary.p, tex, p->color, p->depth, p->stencil, gate, p->flags};
         launches += (uint32_t)launch_opaque(P, pd.U, A, st);
     }
     if (ev) cudaEventRecord(ev[4], st);

@@ -80,7 +80,7 @@ struct sr_pipeline {
     sr::DevBuf<float> vary;
     sr::DevBuf<unsigned long long> clip_counts, clip_offsets, clip_tmp;
     sr::DevBuf<uint32_t> refs;
-    sr::DevBuf<float4> setup;
+    sr::DevBuf<float4> setup, unsafe_rect;
     sr::DevBuf<uint2> binrect;
     sr::DevBuf<uint32_t> bin_counts, bin_off, bin_cursor, bin_tmp, entries, unsafe_list;
     sr::DevBuf<unsigned long long> area, gkeys;
@@ -104,6 +104,7 @@ struct sr_pipeline {
     sr_stats last_stats;
     bool stats_valid = false;
     bool force_unsafe = false;   // SR_FORCE_UNSAFE=1: every primitive takes the exact unsafe path
+    bool opaque_keys = false;    // SR_OPAQUE_KEYS=1: opaque draws through the global key buffer (sr_opaque.cu)
     bool profiling = false;
     cudaEvent_t ev[6] = {};
     uint32_t last_launches = 0;

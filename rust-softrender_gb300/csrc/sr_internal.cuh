@@ -327,7 +327,7 @@ void launch_clip(const DrawParams& P, const sr_mesh* m, VertexStore vs, unsigned
                  DeviceFlags* flags, cudaStream_t st);
 void launch_setup_bin(const DrawParams& P, const uint32_t* vidx, VertexStore vs, float4* setup,
                       uint32_t* binrect, uint32_t* bin_counts, uint32_t* bin_off, uint32_t* bin_cursor,
-                      uint32_t* entries, uint32_t* scan_tmp, uint32_t* unsafe_list,
+                      uint32_t* entries, uint32_t* scan_tmp, uint32_t* unsafe_list, float4* unsafe_rect,
                       unsigned long long* area, const StencilCountArgs& S, DeviceFlags* flags, cudaStream_t st);
 
 void launch_stencil_apply(const DrawParams& P, const StencilCountArgs& S, uint8_t* stencil,
@@ -340,6 +340,7 @@ struct OpaqueArgs {
     unsigned long long* gkeys;       // W x H winner keys, zero between draws
     uint32_t* bitmap;                // touched 32x32 blocks, zero between draws
     const uint32_t* unsafe_list;
+    const float4* unsafe_rect;       // per unsafe-list entry: its coverage region (NaN: unbounded), or null
     const uint32_t* vidx;
     const float* vary;
     const uint32_t* tex;
@@ -351,6 +352,30 @@ struct OpaqueArgs {
 };
 // Opaque draws (sr_opaque.cu); returns the number of kernels launched.
 int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A, cudaStream_t st);
+// Opaque draws over 32x32 screen bins (sr_tiled.cu), after setup has counted
+// each bin's primitives; returns the number of kernels launched.
+struct TiledArgs {
+    const float4* setup;
+    const uint2* binrect;            // per raster primitive: its bbox's bin rectangle (setup output)
+    const uint32_t* bin_counts;      // primitives per bin (setup output)
+    uint32_t* cursor;                // n_bins slot counters, zero
+    uint32_t* bin_off;               // n_bins + 1 list offsets
+    uint32_t* entries;               // the bins' primitive lists
+    uint64_t entry_cap;
+    unsigned long long* gkeys;       // W x H extension keys, zero between draws
+    uint32_t* bitmap;                // bins holding extension keys, zero between draws
+    const uint32_t* unsafe_list;
+    const float4* unsafe_rect;       // per unsafe-list entry: its coverage region (NaN: unbounded)
+    const uint32_t* vidx;
+    const float* vary;
+    const uint32_t* tex;
+    void* color;
+    float* depth;
+    const uint8_t* stencil;
+    uint32_t gate;
+    DeviceFlags* flags;
+};
+int launch_tiled(const DrawParams& P, const sr_uniforms& U, const TiledArgs& A, cudaStream_t st);
 // Bin lists of the ordered path (sr_bins.cu): pairs counted per primitive,
 // written in primitive order and stably radix-sorted by bin.
 struct BinBuffers {

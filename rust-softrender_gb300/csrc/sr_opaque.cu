@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(RG_THREADS) raster_big_kernel(
 // key with the rank of the tile being processed.
 
 __global__ void __launch_bounds__(256) ext_direct_kernel(DrawParams P, const uint32_t* __restrict__ unsafe_list,
+                                                         const float4* __restrict__ unsafe_rect,
                                                          const float4* __restrict__ setup,
                                                          unsigned long long* __restrict__ gkeys,
                                                          uint32_t* __restrict__ bitmap, const uint8_t* __restrict__ stencil,
@@ -189,9 +190,18 @@ __global__ void __launch_bounds__(256) ext_direct_kernel(DrawParams P, const uin
     const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
     const uint32_t lane = threadIdx.x & 31;
+    const uint32_t blocks_x = (P.W + 31) >> 5;
     unsigned long long frags = 0;
-    for (uint32_t k = warp; k < nu; k += nwarps)
-        ext_prim(P, unsafe_list[k], N, setup, gkeys, bitmap, stencil, gate_with_stencil, lane, frags);
+    for (uint32_t k = warp; k < nu; k += nwarps) {
+        // a primitive with a bounded coverage region takes the ring of pixels
+        // around its bbox; the rest every semantic tile's clamped segment
+        const float4 rg = unsafe_rect ? unsafe_rect[k] : make_float4(NAN, NAN, NAN, NAN);
+        if (!isnan(rg.x))
+            ext_prim_ring(P, unsafe_list[k], N, rg, setup, gkeys, stencil, gate_with_stencil, lane, frags,
+                          [=](uint32_t px, uint32_t py) { mark_touched(bitmap, blocks_x, px, py); });
+        else
+            ext_prim(P, unsafe_list[k], N, setup, gkeys, bitmap, stencil, gate_with_stencil, lane, frags);
+    }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
     if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&flags->fragments, frags);
 }
@@ -211,6 +221,13 @@ __global__ void __launch_bounds__(256) resolve_kernel(DrawParams P, sr_uniforms 
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
     resolve_block<FS, FMT>(P, U, b, N, setup, vidx, vary, tex, color, depth, stencil, gate_with_stencil, gkeys,
                            bitmap);
+}
+
+void ext_direct_launch(const DrawParams& P, const uint32_t* unsafe_list, const float4* unsafe_rect,
+                       const float4* setup, unsigned long long* gkeys, uint32_t* bitmap, const uint8_t* stencil,
+                       uint32_t gate, DeviceFlags* flags, cudaStream_t st) {
+    ext_direct_kernel<<<resident_grid(ext_direct_kernel, 256, 4), 256, 0, st>>>(P, unsafe_list, unsafe_rect, setup,
+                                                                               gkeys, bitmap, stencil, gate, flags);
 }
 
 template <int FS>
@@ -246,7 +263,7 @@ int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A
 #undef SR_RS
     raster_big_kernel<<<resident_grid(raster_big_kernel, RG_THREADS, 2), RG_THREADS, 0, st>>>(P, A.setup, A.area, A.gkeys, A.bitmap, A.stencil, A.gate,
                                                        A.big_list, A.flags);
-    ext_direct_kernel<<<resident_grid(ext_direct_kernel, 256, 4), 256, 0, st>>>(P, A.unsafe_list, A.setup, A.gkeys, A.bitmap, A.stencil, A.gate, A.flags);
+    ext_direct_launch(P, A.unsafe_list, A.unsafe_rect, A.setup, A.gkeys, A.bitmap, A.stencil, A.gate, A.flags, st);
     switch (P.fs) {
     case FS_BLINN_PHONG_DIR: launch_resolve_fs<FS_BLINN_PHONG_DIR>(P, U, A, st); break;
     case FS_TEXTURED_BLINN_PHONG: launch_resolve_fs<FS_TEXTURED_BLINN_PHONG>(P, U, A, st); break;

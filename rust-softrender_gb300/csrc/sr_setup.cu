@@ -70,6 +70,7 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
                                                     const float4* __restrict__ scr4, float4* __restrict__ setup,
                                                     uint2* __restrict__ binrect, uint32_t* __restrict__ bin_counts,
                                                     uint32_t* __restrict__ unsafe_list,
+                                                    float4* __restrict__ unsafe_rect,
                                                     unsigned long long* __restrict__ area, StencilCountArgs S,
                                                     DeviceFlags* flags) {
     if (flags->poison) return;
@@ -118,7 +119,13 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
                 if (P.stencil_active && !P.mode_b) gmask = stencil_count_tri(P, S, ix0, iy0, ix1, iy1);
                 bool no_frag = det == 0.0f || isnan(det) || (s0.z >= 0.0f && s1.z >= 0.0f && s2.z >= 0.0f);
                 if (!no_frag || P.mode_b) {
-                    bool safe = !P.mode_b && !P.force_unsafe && inflated_region(x1, y1, x2, y2, x3, y3, det, P.W, P.H, ix0, iy0, ix1, iy1);
+                    // the coverage region of an unsafe primitive bounds its
+                    // fragments outside the bbox (the SR_FORCE_UNSAFE test hook
+                    // leaves it unbounded, so every tile's segment is evaluated)
+                    float4 region = make_float4(NAN, NAN, NAN, NAN);
+                    bool safe = !P.mode_b && !P.force_unsafe &&
+                                inflated_region(x1, y1, x2, y2, x3, y3, det, P.W, P.H, ix0, iy0, ix1, iy1, &region);
+                    if (P.force_unsafe) region = make_float4(NAN, NAN, NAN, NAN);
                     int qx0 = max(ix0, 0), qy0 = max(iy0, 0), qx1 = min(ix1, W - 1), qy1 = min(iy1, H - 1);
                     bool b_in = qx0 <= qx1 && qy0 <= qy1;
                     if (b_in || !safe) {
@@ -136,6 +143,7 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
                             if (!safe) {
                                 unsigned long long k = atomicAdd(&flags->n_unsafe_list, 1ull);
                                 unsafe_list[k] = t;
+                                if (unsafe_rect) unsafe_rect[k] = region;
                             }
                         } else if (!P.mode_b) {
                             if (b_in) {
@@ -148,6 +156,7 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
                             if (!safe) {
                                 unsigned long long k = atomicAdd(&flags->n_unsafe_list, 1ull);
                                 unsafe_list[k] = t;
+                                if (unsafe_rect) unsafe_rect[k] = region;
                             }
                         }
                     }
@@ -189,19 +198,20 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
 
 void launch_setup_bin(const DrawParams& P, const uint32_t* vidx, VertexStore vs, float4* setup, uint32_t* binrect,
                       uint32_t* bin_counts, uint32_t* bin_off, uint32_t* bin_cursor, uint32_t* entries,
-                      uint32_t* scan_tmp, uint32_t* unsafe_list, unsigned long long* area, const StencilCountArgs& S,
-                      DeviceFlags* flags, cudaStream_t st) {
+                      uint32_t* scan_tmp, uint32_t* unsafe_list, float4* unsafe_rect, unsigned long long* area,
+                      const StencilCountArgs& S, DeviceFlags* flags, cudaStream_t st) {
     uint32_t n_host = P.n_raster_host;
     uint32_t n_launch = n_host ? n_host : P.gen_tri_cap;
     dim3 block(256), grid((n_launch + 255) / 256 ? (n_launch + 255) / 256 : 1);
     if (area) {   // opaque path: no bins
         setup_kernel<<<grid, block, 0, st>>>(P, n_host, vidx, vs.scr4, setup, reinterpret_cast<uint2*>(binrect),
-                                             bin_counts, unsafe_list, area, S, flags);
+                                             bin_counts, unsafe_list, unsafe_rect, area, S, flags);
         return;
     }
-    // ordered path: setup only; bins are built by launch_bins (sr_bins.cu)
+    // binned opaque path: setup counts each bin's primitives; ordered path
+    // (bin_counts null): setup only, bins are built by launch_bins (sr_bins.cu)
     setup_kernel<<<grid, block, 0, st>>>(P, n_host, vidx, vs.scr4, setup, reinterpret_cast<uint2*>(binrect),
-                                         nullptr, unsafe_list, nullptr, S, flags);
+                                         bin_counts, unsafe_list, unsafe_rect, nullptr, S, flags);
     (void)bin_off; (void)bin_cursor; (void)entries; (void)scan_tmp;
 }
 

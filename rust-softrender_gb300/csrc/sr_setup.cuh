@@ -99,9 +99,13 @@ __device__ __forceinline__ void tri_slots(uint32_t t, const uint32_t* __restrict
 
 // Conservative bound of the pixel centres whose computed coverage
 // !(u<0 || v<0 || w<0) can hold (the inflated triangle of sr_setup.cu): true when no pixel centre
-// outside the integer bbox [ix0, ix1] x [iy0, iy1] can be covered.
-__device__ __forceinline__ bool inflated_region(float x1, float y1, float x2, float y2, float x3, float y3, float det,
-                                uint32_t W, uint32_t H, int ix0, int iy0, int ix1, int iy1) {
+// outside the integer bbox [ix0, ix1] x [iy0, iy1] can be covered.  `region`, when given,
+// receives the inflated triangle's rectangle (x0, y0, x1, y1): every pixel centre of the
+// frame whose computed coverage holds lies inside it; all NaN when no bound is computed.
+__host__ __device__ __forceinline__ bool inflated_region(float x1, float y1, float x2, float y2, float x3, float y3,
+                                                         float det, uint32_t W, uint32_t H, int ix0, int iy0, int ix1,
+                                                         int iy1, float4* region = nullptr) {
+    if (region) *region = make_float4(NAN, NAN, NAN, NAN);
     const float BIG = 1.0e6f;
     if (!(fabsf(x1) < BIG && fabsf(x2) < BIG && fabsf(x3) < BIG && fabsf(y1) < BIG && fabsf(y2) < BIG &&
           fabsf(y3) < BIG))
@@ -131,6 +135,7 @@ __device__ __forceinline__ bool inflated_region(float x1, float y1, float x2, fl
     float slack = 1.0e-3f + 4.0e-6f * (fabsf(x1) + fabsf(x2) + fabsf(x3) + fabsf(y1) + fabsf(y2) + fabsf(y3));
     float fx0 = fminf(fminf(v1x, v2x), v3x) - slack, fx1 = fmaxf(fmaxf(v1x, v2x), v3x) + slack;
     float fy0 = fminf(fminf(v1y, v2y), v3y) - slack, fy1 = fmaxf(fmaxf(v1y, v2y), v3y) + slack;
+    if (region) *region = make_float4(fx0, fy0, fx1, fy1);
     // a side only constrains where the frame has pixel centres beyond it
     // (ix0 etc. are clamped to [-1, W] / [-1, H])
     bool ok_l = ix0 <= 0 || fx0 > (float)ix0 - 0.5f;

@@ -200,9 +200,9 @@ extern "C" SR_API int sr_render_static(const sr_draw* d, const void* uniforms, s
     VertexStore vs{nullptr, scr4, vary, (uint32_t)ST_MAXV};
     StencilCountArgs S{nullptr, nullptr, nullptr};
     launch_vertex(P, U, &m, vs, false, st);
-    launch_setup_bin(P, indices, vs, setup, binrect, nullptr, nullptr, nullptr, nullptr, nullptr, unsafe_list, area,
+    launch_setup_bin(P, indices, vs, setup, binrect, nullptr, nullptr, nullptr, nullptr, nullptr, unsafe_list, nullptr, area,
                      S, flags, st);
-    OpaqueArgs A{setup, area, big_list, gkeys, bitmap, unsafe_list, indices, vary, texture,
+    OpaqueArgs A{setup, area, big_list, gkeys, bitmap, unsafe_list, nullptr, indices, vary, texture,
                  fb->color_format != SR_COLOR_NONE ? color : nullptr, fb->depth ? depth : nullptr, nullptr, 0u,
                  flags};
     launch_opaque(P, U, A, st);

@@ -44,6 +44,21 @@ def test_oracle_reproduces_golden(oracle_mod, name):
     assert int(got["fragments"]) == int(want["fragments"])
 
 
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_phased_threads_equal_one_thread(oracle_mod, name):
+    """The oracle's deterministic multi-threaded mode (order-preserving
+    geometry, tiles in phases) reproduces the 1-thread frame: the full-frame
+    digests of the benchmark scenes are made with it."""
+    sc = GEN.golden_scenes()[name]
+    want = _load(name)
+    fb, stats, status = oracle_mod.render(sc, n_threads=-3)
+    for k in ("color", "depth", "stencil"):
+        if k in want:
+            assert_bitexact(k, getattr(fb, k), want[k])
+    assert int(stats["fragments"]) == int(want["fragments"])
+    assert status == int(want["status"])
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", NAMES)
 def test_gpu_matches_golden(built_lib, name):
@@ -58,3 +73,38 @@ def test_gpu_matches_golden(built_lib, name):
     if "stencil" in want:
         assert_bitexact("stencil", stencil, want["stencil"])
     assert stats["fragments"] == int(want["fragments"])
+
+
+@pytest.mark.parametrize("tile", [(1, 1), (2, 3), (3, 2), (7, 5)])
+@pytest.mark.parametrize("kind", ["wu_lines", "stencil_blend"])
+def test_oracle_phased_threads_small_tiles(oracle_mod, tile, kind):
+    """The phased mode on semantic tiles of 1-7 pixels, where seams are
+    everywhere: Xiaolin Wu lines (which plot one pixel past their tile) and
+    blended triangles with stencil counting, against the 1-thread order."""
+    from softrender import scenes
+    import softrender._abi as A
+    if kind == "wu_lines":
+        sc = scenes.lines_scene(n=150, size=40, seed=21, aa_lines=True, blend="over", tile=tile)
+    else:
+        sc = scenes.sliver_scene(n=300, size=40, seed=22, color_format=A.SR_COLOR_RGBA8, stencil=True,
+                                 stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT, blend="over", tile=tile)
+    want, wstats, wst = oracle_mod.render(sc, n_threads=1)
+    got, gstats, gst = oracle_mod.render(sc, n_threads=-4)
+    for k in ("color", "depth", "stencil"):
+        assert_bitexact(k, getattr(got, k), getattr(want, k))
+    assert gstats["fragments"] == wstats["fragments"] and gst == wst
+
+
+def test_fullframe_digest_inputs_match_scene_generators():
+    """The stored full-frame digests (tests/golden/fullframe_digests.npz) were
+    made from the scenes the generators build today: a generator change must
+    come with regenerated digests."""
+    spec = importlib.util.spec_from_file_location("make_fullframe_digests",
+                                                  os.path.join(HERE, "make_fullframe_digests.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    stored = dict(np.load(mod.OUT))
+    for name, make in mod.fullframe_scenes().items():
+        sc = make()
+        assert np.array_equal(mod.input_digest(sc), stored[name + "__input"]), name
+        assert stored[name + "__rows"].shape[0] == sc.height
