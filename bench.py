@@ -460,42 +460,60 @@ def _timed(fn):
     return time.perf_counter() - t0
 
 
-def run_served(rate=2000.0, duration=10.0, sat_duration=1.0):
+SWEEP_RATES = (2000.0, 5000.0, 10000.0, 20000.0, 40000.0)
+
+
+def run_served(rate=2000.0, duration=10.0, sat_duration=1.0, sweep=SWEEP_RATES, served_inflight=8):
     """Poisson request stream against the serving loop and against the plain
     per-request loop (same server code, one request at a time through
     sr_render + sr_sync): p50/p99 latency and throughput at `rate`, the plain
-    pipeline's single-request latency, and each mode's saturated throughput
-    (offered load far above capacity)."""
+    pipeline's single-request latency, each mode's saturated throughput
+    (offered load far above capacity), and a sweep of offered rates giving,
+    per mode, the highest rate whose p99 stays within twice the plain
+    pipeline's single-request p99.  The sweep's streams are the `rate` stream
+    with its arrival times scaled (a Poisson process at rate R, time-scaled
+    by R / r, is one at rate r): at least 4,000 requests or half a second of
+    arrivals per rate."""
+    import collections
     import softrender as sr
     from softrender import scenes
     meshes, reqs = scenes.served_workload(rate=rate, duration=duration)
     dev_meshes = [sr.Mesh(p, i) for p, i in meshes]
     built = [sr.Server.request(sr.draw_for_scene(sc, dev_meshes[mi]), sc.uniforms, sc.width, sc.height,
                                sc.color_format, sc.clear_bytes()) for _, mi, sc in reqs]
-    arrivals = [a for a, _, _ in reqs]
+    arrivals = np.asarray([a for a, _, _ in reqs])
 
-    def stream(srv, burst=False, limit=None):
+    def stream(srv, arr=arrivals, burst=False, limit=None):
+        """Submits requests at their arrival times (busy-waiting the last
+        fraction of a millisecond) and releases finished ones in between, on
+        this one thread; latency is stamped by the server from submission to
+        completion."""
         n = len(built) if limit is None else min(limit, len(built))
-        tickets = [None] * n
-        def reader():
-            for k in range(n):
-                while tickets[k] is None:
-                    time.sleep(0.0001)
-                srv.wait(tickets[k], 600000)
-                srv.release(tickets[k])
-        th = threading.Thread(target=reader)
-        th.start()
+        out = collections.deque()
         t0 = time.perf_counter()
         for k in range(n):
-            dt = arrivals[k] - (time.perf_counter() - t0)
-            if dt > 0 and not burst:
-                time.sleep(dt)
+            if not burst:
+                while True:
+                    left = arr[k] - (time.perf_counter() - t0)
+                    if left <= 0:
+                        break
+                    if out and srv.release(out[0]) == 0:
+                        out.popleft()
+                    elif left > 0.0006:
+                        time.sleep(0.0002)
             st, t = srv.submit(built[k])
             if st != 0:
                 raise RuntimeError("submit failed: %d" % st)
-            tickets[k] = t
-        th.join()
-        return srv.stats()
+            out.append(t)
+            while out and srv.release(out[0]) == 0:
+                out.popleft()
+        offered = n / max(1e-9, time.perf_counter() - t0)
+        while out:
+            srv.wait(out[0], 600000)
+            srv.release(out.popleft())
+        st = srv.stats()
+        st["offered_rps"] = offered
+        return st
 
     def warm(srv):
         for k in range(min(2000, len(built))):
@@ -511,22 +529,33 @@ def run_served(rate=2000.0, duration=10.0, sat_duration=1.0):
     out = {"workload": "Poisson arrivals at %g req/s for %g s (seed 5); pool of 12 resident sphere meshes, "
                        "1,000-500,000 tris (log-uniform); frames log-uniform 128..1920 x 128..1080; RGBA8 + f32 "
                        "depth; Blinn-Phong; HBM admission budget 64 GB" % (rate, duration),
-           "requests": len(built)}
-    res = {}
+           "requests": len(built), "served_max_inflight": served_inflight}
+    res, sweeps = {}, {}
     for name, plain in (("served", False), ("plain", True)):
-        srv = sr.Server(hbm_budget=64 << 30, max_inflight=3, max_batch=256, plain=plain)
+        srv = sr.Server(hbm_budget=64 << 30, max_inflight=served_inflight, max_batch=256, plain=plain)
         warm(srv)
         s = stream(srv)
         srv.reset_stats()
         # saturation: the stream's requests submitted back to back (the
         # offered load exceeds either mode's capacity), 20x `rate` x 1 s worth
         sat = stream(srv, burst=True, limit=int(rate * 20 * sat_duration))
+        srv.reset_stats()
         res[name] = {"p50_ms": round(s["p50_ms"], 3), "p99_ms": round(s["p99_ms"], 3),
                      "mean_ms": round(s["mean_ms"], 3), "throughput_rps": round(s["throughput_rps"], 1),
                      "mean_batch": round(s["mean_batch"], 2), "peak_bytes": int(s["peak_bytes"]),
                      "saturated_throughput_rps": round(sat["throughput_rps"], 1),
                      "saturated_mean_batch": round(sat["mean_batch"], 2),
                      "saturated_p99_ms": round(sat["p99_ms"], 3)}
+        sw = []
+        for r in sweep:
+            scale = rate / r
+            n = int(min(len(built), max(4000, r * 0.5)))
+            x = stream(srv, arr=arrivals * scale, limit=n)
+            srv.reset_stats()
+            sw.append({"rate_rps": r, "requests": n, "offered_rps": round(x["offered_rps"], 1),
+                       "p50_ms": round(x["p50_ms"], 3), "p99_ms": round(x["p99_ms"], 3),
+                       "throughput_rps": round(x["throughput_rps"], 1), "mean_batch": round(x["mean_batch"], 2)})
+        sweeps[name] = sw
         if plain:
             lat = []
             for k in range(min(1000, len(built))):
@@ -544,6 +573,18 @@ def run_served(rate=2000.0, duration=10.0, sat_duration=1.0):
     out.update(res)
     out["saturated_throughput_ratio"] = round(res["served"]["saturated_throughput_rps"] /
                                               max(1e-9, res["plain"]["saturated_throughput_rps"]), 2)
+    bound = 2.0 * res["plain"]["single_request_ms"]["p99"]
+    best = {}
+    for name in ("served", "plain"):
+        ok = [x["rate_rps"] for x in sweeps[name] if x["p99_ms"] <= bound]
+        best[name] = max(ok) if ok else None
+    out["rate_sweep"] = {"bound_p99_ms": round(bound, 3),
+                         "bound": "2 x the plain pipeline's single-request p99",
+                         "served": sweeps["served"], "plain": sweeps["plain"],
+                         "served_max_rate_within_bound": best["served"],
+                         "plain_max_rate_within_bound": best["plain"],
+                         "rate_ratio_within_bound": (round(best["served"] / best["plain"], 2)
+                                                     if best["served"] and best["plain"] else None)}
     out["timing"] = "latency = host clock from submission to the completion callback / sync"
     return out
 

@@ -220,7 +220,7 @@ extern "C" SR_API int sr_pipeline_destroy(sr_pipeline* p) {
     p->setup.release(); p->unsafe_rect.release(); p->binrect.release();
     p->bin_counts.release(); p->bin_off.release(); p->bin_cursor.release(); p->bin_tmp.release(); p->entries.release(); p->unsafe_list.release();
     p->st_diff.release(); p->st_lines.release(); p->st_glob.release();
-    p->area.release(); p->big_list.release(); p->gkeys.release(); p->bitmap.release();
+    p->area.release(); p->big_list.release(); p->gids.release(); p->gkeys.release(); p->bitmap.release();
     p->lpv.release(); p->lpvalid.release();
     p->pcount.release(); p->poff.release(); p->pkeys0.release(); p->pkeys1.release(); p->pvals0.release();
     p->pvals1.release(); p->hist.release(); p->hist_off.release(); p->ranges.release();
@@ -695,7 +695,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
         if (tiled) {
             if ((rc = p->bin_counts.ensure(2 * (size_t)n_bins)) || (rc = p->bin_off.ensure((size_t)n_bins + 1)) ||
                 (rc = p->entries.ensure(p->entry_cap)) || (rc = p->gkeys.ensure(npx)) ||
-                (rc = p->bitmap.ensure((nblk + 31) / 32)))
+                (rc = p->bitmap.ensure((nblk + 31) / 32)) || (rc = p->gids.ensure((size_t)n_bins << 10)))
                 return rc;
         } else if ((rc = p->area.ensure(n_raster_cap + 1)) || (rc = p->big_list.ensure(n_raster_cap + 1)) ||
                    (rc = p->gkeys.ensure(npx)) || (rc = p->bitmap.ensure((nblk + 31) / 32))) {
@@ -761,8 +761,8 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
         launches += 1;
     } else if (tiled) {
         TiledArgs T{p->setup.p, p->binrect.p, p->bin_counts.p, p->bin_counts.p + n_bins, p->bin_off.p, p->entries.p,
-                    p->entry_cap, p->gkeys.p, p->bitmap.p, p->unsafe_list.p, p->unsafe_rect.p, vidx, p->vary.p,
-                    tex, p->color, p->depth, p->stencil, gate, p->flags};
+                    p->entry_cap, p->gkeys.p, p->bitmap.p, p->gids.p, p->unsafe_list.p, p->unsafe_rect.p, vidx,
+                    p->vary.p, tex, p->color, p->depth, p->stencil, gate, p->flags};
         launches += (uint32_t)launch_tiled(P, pd.U, T, st);
     } else {
         OpaqueArgs A{p->setup.p, p->area.p, p->big_list.p, p->gkeys.p, p->bitmap.p, p->unsafe_list.p,

@@ -2,8 +2,10 @@
 //
 //   vertex_kernel  VertexShader::run / run_to_fragment (stages/vertex.rs:87-160):
 //                  out[v] = vs(vertex v); screen = ClipVertex::normalize
-//                  (geometry/clipvertex.rs:89-127).  One thread per 4 vertices,
-//                  each attribute plane read with one 128-bit load.
+//                  (geometry/clipvertex.rs:89-127).  One thread per vertex:
+//                  a warp reads 32 consecutive floats of each attribute plane
+//                  (one 128-byte transaction per plane), and writes its
+//                  vertices' screen positions and varyings contiguously.
 //   clip_*_kernel  GeometryShader::clip_primitives, triangle arm
 //                  (stages/geometry.rs:264-299) + finish (geometry.rs:60-129):
 //                  a counting pass, an exclusive scan (order-preserving

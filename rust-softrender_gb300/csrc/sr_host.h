@@ -84,7 +84,7 @@ struct sr_pipeline {
     sr::DevBuf<uint2> binrect;
     sr::DevBuf<uint32_t> bin_counts, bin_off, bin_cursor, bin_tmp, entries, unsafe_list;
     sr::DevBuf<unsigned long long> area, gkeys;
-    sr::DevBuf<uint32_t> big_list;
+    sr::DevBuf<uint32_t> big_list, gids;
     sr::DevBuf<uint32_t> bitmap;
     sr::DevBuf<int> st_diff, st_lines;
     sr::DevBuf<uint32_t> pcount, poff, pkeys0, pkeys1, pvals0, pvals1, hist, hist_off, ranges;   // ordered bins

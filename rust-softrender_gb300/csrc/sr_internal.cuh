@@ -364,6 +364,7 @@ struct TiledArgs {
     uint64_t entry_cap;
     unsigned long long* gkeys;       // W x H extension keys, zero between draws
     uint32_t* bitmap;                // bins holding extension keys, zero between draws
+    uint32_t* gids;                  // 1024 winner slots per bin (bin-major)
     const uint32_t* unsafe_list;
     const float4* unsafe_rect;       // per unsafe-list entry: its coverage region (NaN: unbounded)
     const uint32_t* vidx;

@@ -132,8 +132,12 @@ __device__ __forceinline__ uint32_t seam_bits(uint32_t x0, uint32_t y0, uint32_t
 constexpr uint32_t RG_BIG = 2048;   // bbox pixels above which a primitive goes to the block-cooperative pass
 
 // Extension fragments of one unsafe primitive t (see ext_direct_kernel): the
-// warp's lanes stride over the semantic tiles.  `mark(px, py)` records the
-// pixel's 32x32 block as touched.
+// warp's lanes stride over the semantic tiles, each finding its tile's
+// clamped segment (triangle.rs:66-78) and testing it with the sound sign
+// test; the segments the test does not clear are then evaluated one after
+// another with the lanes spread over the segment's pixels (a segment is one
+// pixel wide or high, up to a tile long).  `mark(px, py)` records the pixel's
+// 32x32 block as touched.
 template <class Mark>
 __device__ __forceinline__ void ext_prim_m(const DrawParams& P, uint32_t t, uint32_t N,
                                            const float4* __restrict__ setup, unsigned long long* __restrict__ gkeys,
@@ -144,18 +148,32 @@ __device__ __forceinline__ void ext_prim_m(const DrawParams& P, uint32_t t, uint
     const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
     const int ix0 = __float_as_int(r3.x), iy0 = __float_as_int(r3.y);
     const int ix1 = __float_as_int(r3.z), iy1 = __float_as_int(r3.w);
-    for (uint32_t ti = lane; ti < ntiles; ti += 32) {
-        const uint32_t C = ti % P.ncols, R = ti / P.ncols;
-        const uint32_t lx = C * P.tile_w, hx = min((C + 1) * P.tile_w, P.W - 1);
-        const uint32_t ly = R * P.tile_h, hy = min((R + 1) * P.tile_h, P.H - 1);
-        if (ix1 >= (int)lx && ix0 <= (int)hx && iy1 >= (int)ly && iy0 <= (int)hy) continue;
-        const uint32_t cx0 = ix0 < (int)lx ? lx : (ix0 > (int)hx ? hx : (uint32_t)ix0);
-        const uint32_t cx1 = ix1 < (int)lx ? lx : (ix1 > (int)hx ? hx : (uint32_t)ix1);
-        const uint32_t cy0 = iy0 < (int)ly ? ly : (iy0 > (int)hy ? hy : (uint32_t)iy0);
-        const uint32_t cy1 = iy1 < (int)ly ? ly : (iy1 > (int)hy ? hy : (uint32_t)iy1);
-        if (segment_cleared(r0, r1, cx0, cy0, cx1, cy1)) continue;
-        for (uint32_t py = cy0; py <= cy1; ++py) {
-            for (uint32_t px = cx0; px <= cx1; ++px) {
+    for (uint32_t tb = 0; tb < ntiles; tb += 32) {
+        const uint32_t ti = tb + lane;
+        uint32_t cx0 = 0, cx1 = 0, cy0 = 0, cy1 = 0;
+        bool open = false;
+        if (ti < ntiles) {
+            const uint32_t C = ti % P.ncols, R = ti / P.ncols;
+            const uint32_t lx = C * P.tile_w, hx = min((C + 1) * P.tile_w, P.W - 1);
+            const uint32_t ly = R * P.tile_h, hy = min((R + 1) * P.tile_h, P.H - 1);
+            if (!(ix1 >= (int)lx && ix0 <= (int)hx && iy1 >= (int)ly && iy0 <= (int)hy)) {
+                cx0 = ix0 < (int)lx ? lx : (ix0 > (int)hx ? hx : (uint32_t)ix0);
+                cx1 = ix1 < (int)lx ? lx : (ix1 > (int)hx ? hx : (uint32_t)ix1);
+                cy0 = iy0 < (int)ly ? ly : (iy0 > (int)hy ? hy : (uint32_t)iy0);
+                cy1 = iy1 < (int)ly ? ly : (iy1 > (int)hy ? hy : (uint32_t)iy1);
+                open = !segment_cleared(r0, r1, cx0, cy0, cx1, cy1);
+            }
+        }
+        uint32_t todo = __ballot_sync(0xffffffffu, open);
+        while (todo) {
+            const uint32_t src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const uint32_t sx0 = __shfl_sync(0xffffffffu, cx0, src), sx1 = __shfl_sync(0xffffffffu, cx1, src);
+            const uint32_t sy0 = __shfl_sync(0xffffffffu, cy0, src), sy1 = __shfl_sync(0xffffffffu, cy1, src);
+            const uint32_t sti = tb + src, C = sti % P.ncols, R = sti / P.ncols;
+            const uint32_t sw = sx1 - sx0 + 1, npx = sw * (sy1 - sy0 + 1);
+            for (uint32_t i = lane; i < npx; i += 32) {
+                const uint32_t px = sx0 + i % sw, py = sy0 + i / sw;
                 const float x = (float)px + 0.5f, y = (float)py + 0.5f;
                 const float dx = x - r1.x, dy = y - r1.y;
                 const float u = (r0.x * dx + r0.y * dy) / r1.z;
@@ -294,6 +312,49 @@ __device__ __forceinline__ bool resolve_pixel(const DrawParams& P, const sr_unif
     const float v = (r0.z * dx + r0.w * dy) / r1.z;
     const float w = 1.0f - u - v;
     const float z = (r1.w * u + r2.x * v) + r2.y * w;
+    constexpr int NK = FsTraits<FS>::NK;
+    float kv[12];
+    if (NK > 0) {
+        const uint32_t a = __ldg(vidx + 3 * (size_t)t), bq = __ldg(vidx + 3 * (size_t)t + 1),
+                       c = __ldg(vidx + 3 * (size_t)t + 2);
+        interp_varyings<NK>(vary, a, bq, c, u, v, w, kv);
+    }
+    if (FMT == SR_COLOR_RGBA32F) {
+        const sr_v4 col = shade_fs<FS>(U, kv, tex, P);
+        reinterpret_cast<float4*>(color)[gi] = make_float4(col.x, col.y, col.z, col.w);
+    } else if (FMT == SR_COLOR_RGBA8) {
+        reinterpret_cast<uint32_t*>(color)[gi] = shade_fs_rgba8<FS>(U, kv, tex, P);
+    }
+    if (P.has_depth) depth[gi] = z;
+    return true;
+}
+
+// Resolve of one pixel from its winner's low key word (pass * N + primitive
+// + 1, non-zero): the winner's barycentrics and z recomputed -- the same
+// values its fragment had -- then z against the depth the draw started from
+// (d0; ignored without a depth attachment), the stencil gate, varyings,
+// shading, colour and depth written.  Returns false when the winner loses.
+template <int FS, int FMT>
+__device__ __forceinline__ bool resolve_winner(const DrawParams& P, const sr_uniforms& U, uint32_t px, uint32_t py,
+                                               uint32_t id, float d0, uint32_t N, const float4* __restrict__ setup,
+                                               const uint32_t* __restrict__ vidx, const float* __restrict__ vary,
+                                               const uint32_t* __restrict__ tex, void* __restrict__ color,
+                                               float* __restrict__ depth, const uint8_t* __restrict__ stencil,
+                                               uint32_t gate_with_stencil) {
+    const size_t gi = (size_t)py * P.W + px;
+    uint32_t t = id - 1u;
+#pragma unroll
+    for (int pass = 0; pass < 3; ++pass) t = t >= N ? t - N : t;
+    const float4* r = setup + 4 * (size_t)t;
+    const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2);
+    const float x = (float)px + 0.5f, y = (float)py + 0.5f;
+    const float dx = x - r1.x, dy = y - r1.y;
+    const float u = (r0.x * dx + r0.y * dy) / r1.z;
+    const float v = (r0.z * dx + r0.w * dy) / r1.z;
+    const float w = 1.0f - u - v;
+    const float z = (r1.w * u + r2.x * v) + r2.y * w;
+    if (P.has_depth && (isnan(d0) || zkey(z) < zkey(d0))) return false;
+    if (gate_with_stencil && !stencil_test(P.stencil_test, stencil[gi], P.sref)) return false;
     constexpr int NK = FsTraits<FS>::NK;
     float kv[12];
     if (NK > 0) {

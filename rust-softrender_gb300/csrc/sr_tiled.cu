@@ -13,14 +13,17 @@
 //   4. unsafe primitives' fragments outside their bbox (the clamped
 //      tile-edge events of triangle.rs:66-78) go, rarely, through the global
 //      key buffer and the touched-bin bitmap (ext_direct_kernel);
-//   5. the bin kernel seeds its 1024 keys (from the global buffer where the
-//      bitmap says so), walks its primitive list with the bbox pixels of a
-//      warp's primitives flattened over the lanes (shared-memory atomicMax
-//      of the key), and then resolves its pixels in place: start depth,
-//      winner's barycentrics, varyings, shading, one colour and depth write.
-// Nothing per pixel goes through global memory except the framebuffer itself
-// (and the rare extension keys), and no global atomics are taken per
-// fragment.
+//   5. the bin raster kernel seeds its 1024 keys (from the global buffer where
+//      the bitmap says so), walks its primitive list -- a cheap sign pre-test
+//      on every bbox pixel, the reference's exact arithmetic on the pixels it
+//      keeps, a shared-memory atomicMax of the key -- and writes each pixel's
+//      winner (the key's low word) to the bin's 1024 slots;
+//   6. the bin resolve kernel shades every pixel with a winner: start depth,
+//      the winner's barycentrics, varyings, shading, one colour and depth
+//      write.
+// Per pixel, global memory sees the framebuffer and one 32-bit winner slot
+// written and read once (and the rare extension keys); no global atomics are
+// taken per fragment.
 #include "sr_internal.cuh"
 #include "sr_scan.cuh"
 #include "sr_shade.cuh"
@@ -34,24 +37,41 @@ constexpr uint32_t TL_WARPS = TL_THREADS / 32;
 constexpr uint32_t TL_BIN_LOG2 = 5;   // bins of 32 x 32 pixels (the touched-block bitmap's granularity)
 static_assert(TL_BIN_LOG2 == TOUCH_LOG2, "the extension keys' bitmap marks bins");
 
-// Exclusive scan of n <= 2^24 bin counts in one CTA: each thread sums a
-// contiguous run, the CTA scans the run sums, each thread writes its run's
-// offsets.  out[n] = total.
+// Exclusive scan of the n bin counts in one CTA, 8192 at a time: coalesced
+// loads into shared memory, each thread scans 8 consecutive counts (padded
+// slots, no bank conflicts), a CTA-wide scan of the thread sums, coalesced
+// stores.  out[n] = total.
+constexpr uint32_t BS_TILE = 8192;
+__device__ __forceinline__ uint32_t bs_slot(uint32_t i) { return i + (i >> 5); }
 __global__ void __launch_bounds__(1024) bin_scan_kernel(const uint32_t* __restrict__ in, uint32_t n,
                                                         uint32_t* __restrict__ out, const DeviceFlags* flags) {
+    __shared__ uint32_t tile[BS_TILE + BS_TILE / 32];
     if (flags->poison) return;
-    const uint32_t per = (n + 1023) / 1024;
-    const uint32_t j0 = threadIdx.x * per, j1 = min(j0 + per, n);
-    uint32_t s = 0;
-    for (uint32_t j = j0; j < j1; ++j) s += in[j];
-    uint32_t tot;
-    uint32_t ex = block_exclusive_scan<uint32_t, 1024>(s, &tot);
-    for (uint32_t j = j0; j < j1; ++j) {
-        const uint32_t v = in[j];
-        out[j] = ex;
-        ex += v;
+    uint32_t carry = 0;
+    for (uint32_t base = 0; base < n; base += BS_TILE) {
+        const uint32_t m = min(BS_TILE, n - base);
+        for (uint32_t i = threadIdx.x; i < BS_TILE; i += 1024) tile[bs_slot(i)] = i < m ? in[base + i] : 0u;
+        __syncthreads();
+        uint32_t v[BS_TILE / 1024];
+        uint32_t s = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < BS_TILE / 1024; ++k) {
+            v[k] = tile[bs_slot(threadIdx.x * (BS_TILE / 1024) + k)];
+            s += v[k];
+        }
+        uint32_t tot;
+        uint32_t ex = block_exclusive_scan<uint32_t, 1024>(s, &tot) + carry;
+#pragma unroll
+        for (uint32_t k = 0; k < BS_TILE / 1024; ++k) {
+            tile[bs_slot(threadIdx.x * (BS_TILE / 1024) + k)] = ex;
+            ex += v[k];
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < m; i += 1024) out[base + i] = tile[bs_slot(i)];
+        carry += tot;
+        __syncthreads();
     }
-    if (threadIdx.x == 0) out[n] = tot;
+    if (threadIdx.x == 0) out[n] = carry;
 }
 
 // Writes every primitive into the list of each bin its clamped bbox meets.
@@ -102,29 +122,65 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t n_host, uint3
     }
 }
 
-// One CTA per 32x32 bin.  G = primitives a warp takes from the bin's list at a
-// time; their bbox pixels (clipped to the bin) are flattened over the lanes in
-// items of two horizontally adjacent pixels, as in raster_small_kernel.
-template <int FS, int FMT, uint32_t G>
-__global__ void __launch_bounds__(TL_THREADS) bin_raster_kernel(
-    DrawParams P, sr_uniforms U, const float4* __restrict__ setup, const uint32_t* __restrict__ bin_off,
-    const uint32_t* __restrict__ entries, const uint32_t* __restrict__ vidx, const float* __restrict__ vary,
-    const uint32_t* __restrict__ tex, void* __restrict__ color, float* __restrict__ depth,
-    const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil, unsigned long long* __restrict__ gkeys,
-    uint32_t* __restrict__ bitmap, DeviceFlags* flags) {
+constexpr uint32_t TL_CHUNK = 128;   // primitives staged per chunk
+constexpr uint32_t TL_QCAP = 160;    // pixels a warp's stack holds: 31 waiting + 4 x 32 pushed
+
+// Per staged primitive, the sign pre-test's operands: the numerators' edge
+// coefficients times s = det_sign(det), the anchor, |det| and the three
+// rejection thresholds (see bin_raster_kernel).
+struct PreRec {
+    float4 e;    // s A, s B, s C, s D   (A = y2-y3, B = x3-x2, C = y3-y1, D = x1-x3)
+    float4 a;    // x3, y3, s det, Tu
+    float2 t;    // Tv, Tw
+};
+
+// One CTA per 32x32 bin reduces the winner key of each of its pixels in
+// shared memory and writes the key's low word (pass * N + primitive + 1, 0
+// for no fragment) to the bin's 1024 slots of `gids`; bin_resolve_kernel
+// shades them.  The bin's primitive list is taken in chunks of TL_CHUNK: each
+// primitive's bbox clipped to the bin gives its items (runs of four
+// horizontally adjacent pixels, ceil(w / 4) per row), a CTA-wide scan numbers
+// them, and the items are split into equal contiguous ranges, one per warp.
+// Every binned primitive's bbox meets its bin, so every primitive of a chunk
+// has items and their first items are strictly increasing: a warp finds the
+// owner of its first item by binary search and then, per window of 32 items,
+// the primitives starting inside the window from one load per lane.
+//
+// Pre-test.  With s = det_sign(det) (non-zero for 0 < |det| < 1e18), the run's
+// first pixel gets eu = (sA) dx + (sB) dy and ev = (sC) dx + (sD) dy with the
+// reference's operations, i.e. exactly s nu and s nv of the reference; the
+// next pixels add sA and sC (the exact edge functions step by exactly that).
+// Each addition errs by at most 2^-24 of its result, and the reference's own
+// numerators differ from the exact edge functions by at most 3.0001 2^-24 S,
+// S = |A| Xr + |B| Yr over the clipped bbox (Xr, Yr bounding |x - x3|,
+// |y - y3|), so eu stays within 9.01 2^-24 Su of s nu:
+//   eu < -(1e-18 + 2^-20 Su)   proves s nu < -1e-18, i.e. u < 0;  v alike;
+//   ew = (|det| - eu) - ev < -2^-20 (|det| + Su + Sv) - 2^-140 |det|
+// proves w = (1-u)-v < 0 (frag_key's third-edge argument, whose slack is
+// 3.01 2^-24 |det| + 13.1 2^-24 (Su + Sv) with these approximations).  The
+// pixels the pre-test keeps -- those covered and a thin margin along the
+// edges -- go onto a per-warp stack in shared memory, and whenever 32 wait the
+// whole warp evaluates them exactly (frag_key: the reference's divisions, z,
+// the key) with every lane busy.
+__global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
+    DrawParams P, const float4* __restrict__ setup, const uint32_t* __restrict__ bin_off,
+    const uint32_t* __restrict__ entries, const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
+    unsigned long long* __restrict__ gkeys, const uint32_t* __restrict__ bitmap, uint32_t* __restrict__ gids,
+    DeviceFlags* flags) {
     __shared__ unsigned long long keys[1u << (2 * TL_BIN_LOG2)];
-    __shared__ float4 srec[TL_WARPS][G][3];
-    __shared__ uint32_t sxy[TL_WARPS][G];             // x0 | y0 << 16 (bin-relative) | seam bits 15, 31
-    __shared__ uint32_t sw[TL_WARPS][G];              // pairs per row | clipped width << 16
-    __shared__ uint32_t sst[TL_WARPS][G];             // first item
-    __shared__ uint32_t st[TL_WARPS][G];              // primitive index
-    __shared__ unsigned long long smag[TL_WARPS][G];  // ceil(2^32 / pairs per row)
-    __shared__ uint32_t s_next;
+    __shared__ float4 srec[TL_CHUNK][3];
+    __shared__ PreRec spre[TL_CHUNK];
+    __shared__ uint32_t sst[TL_CHUNK + 1];            // first item of each primitive; [n] = items
+    __shared__ uint32_t sxy[TL_CHUNK];                // x0 | y0 << 16 (bin-relative) | seam bits 15, 31
+    __shared__ uint32_t sw[TL_CHUNK];                 // runs per row | clipped width << 16
+    __shared__ uint32_t smag[TL_CHUNK];               // ceil(2^32 / runs per row), 0 for one run
+    __shared__ uint32_t st[TL_CHUNK];                 // primitive index
+    __shared__ uint32_t squeue[TL_WARPS][TL_QCAP];    // pre-tested pixels: chunk slot << 10 | y << 5 | x
     if (flags->poison) return;
     const uint32_t b = blockIdx.x;
     const uint32_t e0 = bin_off[b], cnt = bin_off[b + 1] - e0;
     const bool ext = (bitmap[b >> 5] >> (b & 31)) & 1u;
-    if (cnt == 0 && !ext) return;   // no fragment can land here: the pixels keep their values
+    if (cnt == 0 && !ext) return;   // no fragment can land here (bin_resolve_kernel skips it too)
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
     const uint32_t X0 = (b % P.bins_x) << TL_BIN_LOG2, Y0 = (b / P.bins_x) << TL_BIN_LOG2;
     const uint32_t X1 = min(X0 + (1u << TL_BIN_LOG2) - 1, P.W - 1), Y1 = min(Y0 + (1u << TL_BIN_LOG2) - 1, P.H - 1);
@@ -140,99 +196,173 @@ __global__ void __launch_bounds__(TL_THREADS) bin_raster_kernel(
         }
         keys[i] = k;
     }
-    if (threadIdx.x == 0) s_next = 0;
-    __syncthreads();
 
     const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     unsigned long long frags = 0;
     const uint32_t mx = div_magic(P.tile_w), my = div_magic(P.tile_h);
-    for (;;) {
-        uint32_t k0 = 0;
-        if (lane == 0) k0 = atomicAdd(&s_next, G);
-        k0 = __shfl_sync(0xffffffffu, k0, 0);
-        if (k0 >= cnt) break;
-        uint32_t a = 0, x0 = 0, y0 = 0, x1 = 0, y1 = 0, t = 0;
-        if (lane < G && k0 + lane < cnt) {
-            t = __ldg(entries + e0 + k0 + lane);
-            const float4 r3 = __ldg(setup + 4 * (size_t)t + 3);
-            x0 = (uint32_t)max(__float_as_int(r3.x), (int)X0);
-            y0 = (uint32_t)max(__float_as_int(r3.y), (int)Y0);
-            x1 = (uint32_t)min(__float_as_int(r3.z), (int)X1);
-            y1 = (uint32_t)min(__float_as_int(r3.w), (int)Y1);
-            if (x0 <= x1 && y0 <= y1) a = (y1 - y0 + 1) * ((x1 - x0 + 2) >> 1);
-        }
-        const uint32_t inc = warp_inclusive_scan(a);
-        const uint32_t total = __shfl_sync(0xffffffffu, inc, 31);
-        const uint32_t ex = inc - a;
-        const uint32_t nonempty = __ballot_sync(0xffffffffu, a != 0);
-        if (a) {
-            const uint32_t c = __popc(nonempty & ((1u << lane) - 1u));
+    const uint32_t lt = (1u << lane) - 1u;   // lanes below this one
+    for (uint32_t c0 = 0; c0 < cnt; c0 += TL_CHUNK) {
+        const uint32_t n = min(cnt - c0, TL_CHUNK);
+        uint32_t a = 0;
+        if (threadIdx.x < n) {
+            const uint32_t t = __ldg(entries + e0 + c0 + threadIdx.x);
             const float4* r = setup + 4 * (size_t)t;
-            srec[wl][c][0] = __ldg(r);
-            srec[wl][c][1] = __ldg(r + 1);
-            srec[wl][c][2] = __ldg(r + 2);
-            const uint32_t w = x1 - x0 + 1, wp = (w + 1) >> 1;
+            const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
+            const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), (int)X0);
+            const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), (int)Y0);
+            const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)X1);
+            const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)Y1);
+            const uint32_t w = x1 - x0 + 1, wq = (w + 3) >> 2;
+            a = (y1 - y0 + 1) * wq;
+            srec[threadIdx.x][0] = r0;
+            srec[threadIdx.x][1] = r1;
+            srec[threadIdx.x][2] = r2;
+            const float s = r2.w;
+            PreRec pr;
+            pr.e = make_float4(s * r0.x, s * r0.y, s * r0.z, s * r0.w);
+            const float INF = __int_as_float(0x7f800000);
+            if (s != 0.0f) {
+                // bounds of |x - x3| and |y - y3| over the clipped bbox's pixel centres
+                const float xr = fmaxf(fabsf(((float)x0 + 0.5f) - r1.x), fabsf(((float)x1 + 0.5f) - r1.x)) * 1.001f;
+                const float yr = fmaxf(fabsf(((float)y0 + 0.5f) - r1.y), fabsf(((float)y1 + 0.5f) - r1.y)) * 1.001f;
+                const float su = fabsf(r0.x) * xr + fabsf(r0.y) * yr, sv = fabsf(r0.z) * xr + fabsf(r0.w) * yr;
+                const float ad = fabsf(r1.z);
+                pr.a = make_float4(r1.x, r1.y, ad, 1.0e-18f + 0x1p-20f * su);
+                pr.t = make_float2(1.0e-18f + 0x1p-20f * sv, 0x1p-20f * ((ad + su) + sv) + 0x1p-140f * ad);
+            } else {   // no sign information: keep every pixel for the exact test
+                pr.a = make_float4(r1.x, r1.y, 0.0f, INF);
+                pr.t = make_float2(INF, INF);
+            }
+            spre[threadIdx.x] = pr;
             const uint32_t sb = seam_bits(x0, y0, x1, y1, P.W, P.H, P.tile_w, P.tile_h);
-            sxy[wl][c] = (x0 - X0) | ((y0 - Y0) << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
-            sw[wl][c] = wp | (w << 16);
-            sst[wl][c] = ex;
-            st[wl][c] = t;
-            smag[wl][c] = ((1ull << 32) + wp - 1) / wp;
+            sxy[threadIdx.x] = (x0 - X0) | ((y0 - Y0) << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
+            sw[threadIdx.x] = wq | (w << 16);
+            st[threadIdx.x] = t;
+            smag[threadIdx.x] = wq == 1 ? 0u : 0xffffffffu / wq + 1u;   // ceil(2^32 / wq) for wq >= 2
         }
-        __syncwarp();
-        const uint32_t le = (2u << lane) - 1u;
-        uint32_t before = 0;
-        for (uint32_t base = 0; base < total; base += 32) {
+        uint32_t total;
+        const uint32_t ex = block_exclusive_scan<uint32_t, TL_THREADS>(a, &total);
+        if (threadIdx.x < n) sst[threadIdx.x] = ex;
+        if (threadIdx.x == 0) sst[n] = total;
+        __syncthreads();
+        // this warp's items [q0, q1): equal shares in whole windows of 32
+        const uint32_t per = ((total + TL_WARPS * 32 - 1) / (TL_WARPS * 32)) * 32;
+        const uint32_t q0 = min(wl * per, total), q1 = min(q0 + per, total);
+        uint32_t cur = 0;   // owner of item q0: the last primitive whose first item is <= q0
+        {
+            uint32_t lo = 0, hi = n;   // sst[lo] <= q0 < sst[hi]
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (sst[mid] <= q0) lo = mid; else hi = mid;
+            }
+            cur = lo;
+        }
+        uint32_t qn = 0;   // pixels waiting on the warp's stack (warp-uniform)
+        for (uint32_t base = q0; base < q1; base += 32) {
+            // primitives cur+1 .. cur+32 that start inside [base, base + 32)
+            const uint32_t j = cur + 1 + lane;
+            const uint32_t sj = j < n ? sst[j] : 0xffffffffu;
+            const uint32_t starts = __reduce_or_sync(0xffffffffu, sj - base < 32u ? (1u << (sj - base)) : 0u);
+            const uint32_t o = cur + __popc(starts & (lt | (1u << lane)));
+            cur += __popc(starts);
             const uint32_t q = base + lane;
-            const uint32_t rel = ex - base;
-            const uint32_t starts = __reduce_or_sync(0xffffffffu, (a && rel < 32u) ? (1u << rel) : 0u);
-            const uint32_t o = before + __popc(starts & le) - 1u;
-            before += __popc(starts);
-            if (q < total) {
-                const uint32_t local = q - sst[wl][o];
-                const uint32_t wpw = sw[wl][o], wp = wpw & 0xffffu;
-                const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][o]) >> 32);
-                const uint32_t col = 2 * (local - row * wp);
-                const uint32_t xy = sxy[wl][o];
-                const float4 r0 = srec[wl][o][0], r1 = srec[wl][o][1], r2 = srec[wl][o][2];
-                const uint32_t lx = (xy & 0x7fffu) + col, ly = ((xy >> 16) & 0x7fffu) + row, tt = st[wl][o];
-                const uint32_t seams = ((xy >> 15) & 1u) | ((xy >> 30) & 2u);
-                const uint32_t slot = (ly << TL_BIN_LOG2) + lx;
-                unsigned long long k = frag_key(P.W, P.H, P.tile_w, P.tile_h, mx, my, seams, P.has_depth != 0, r0, r1,
-                                                r2, tt, X0 + lx, Y0 + ly, N, stencil, gate_with_stencil,
-                                                P.stencil_test, P.sref, frags);
-                if (k) atomicMax(keys + slot, k);
-                if (col + 1 < (wpw >> 16)) {
-                    k = frag_key(P.W, P.H, P.tile_w, P.tile_h, mx, my, seams, P.has_depth != 0, r0, r1, r2, tt,
-                                 X0 + lx + 1, Y0 + ly, N, stencil, gate_with_stencil, P.stencil_test, P.sref, frags);
-                    if (k) atomicMax(keys + slot + 1, k);
+            uint32_t cm = 0, lx = 0, ly = 0;   // candidate pixels of this lane's run (bit k: pixel lx + k)
+            if (q < q1) {
+                const uint32_t local = q - sst[o];
+                const uint32_t wqw = sw[o], wq = wqw & 0xffffu, mg = smag[o];
+                const uint32_t row = mg ? __umulhi(local, mg) : local;
+                const uint32_t col = 4 * (local - row * wq);
+                const uint32_t xy = sxy[o];
+                lx = (xy & 0x7fffu) + col;
+                ly = ((xy >> 16) & 0x7fffu) + row;
+                const uint32_t left = min((wqw >> 16) - col, 4u);
+                const PreRec pr = spre[o];
+                const float dx = ((float)(X0 + lx) + 0.5f) - pr.a.x;
+                const float dy = ((float)(Y0 + ly) + 0.5f) - pr.a.y;
+                float eu = pr.e.x * dx + pr.e.y * dy;
+                float ev = pr.e.z * dx + pr.e.w * dy;
+#pragma unroll
+                for (uint32_t k = 0; k < 4; ++k) {
+                    if (k) { eu = eu + pr.e.x; ev = ev + pr.e.z; }
+                    const float ew = (pr.a.z - eu) - ev;
+                    const bool keep = !(eu < -pr.a.w) && !(ev < -pr.t.x) && !(ew < -pr.t.y);
+                    if (k < left && keep) cm |= 1u << k;
                 }
             }
+            // push the candidates (slots in lane order per pixel position k)
+            uint32_t pos = qn;
+#pragma unroll
+            for (uint32_t k = 0; k < 4; ++k) {
+                const uint32_t bal = __ballot_sync(0xffffffffu, (cm >> k) & 1u);
+                if ((cm >> k) & 1u) squeue[wl][pos + __popc(bal & lt)] = (o << 10) | (ly << 5) | (lx + k);
+                pos += __popc(bal);
+            }
+            qn = pos;
+            __syncwarp();
+            // exact evaluation, 32 pixels at a time from the top of the stack
+            // (what is left after the warp's last window, too)
+            while (qn >= 32 || (qn && base + 32 >= q1)) {
+                const uint32_t m = min(qn, 32u);
+                if (lane < m) {
+                    const uint32_t e = squeue[wl][qn - m + lane];
+                    const uint32_t oo = e >> 10, ex_ = e & 31u, ey = (e >> 5) & 31u;
+                    const uint32_t xy = sxy[oo];
+                    const uint32_t seams = ((xy >> 15) & 1u) | ((xy >> 30) & 2u);
+                    const unsigned long long k =
+                        frag_key(P.W, P.H, P.tile_w, P.tile_h, mx, my, seams, P.has_depth != 0, srec[oo][0],
+                                 srec[oo][1], srec[oo][2], st[oo], X0 + ex_, Y0 + ey, N, stencil, gate_with_stencil,
+                                 P.stencil_test, P.sref, frags);
+                    if (k) atomicMax(keys + (ey << TL_BIN_LOG2) + ex_, k);
+                }
+                qn -= m;
+                __syncwarp();
+            }
         }
-        __syncwarp();
+        __syncthreads();   // the chunk's staging is reused by the next chunk
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
     if (lane == 0 && frags) atomicAdd(&flags->fragments, frags);
-    __syncthreads();
-    if (ext && threadIdx.x == 0) atomicAnd(bitmap + (b >> 5), ~(1u << (b & 31)));
+    if (cnt == 0) __syncthreads();   // the extension keys' seeding, when no chunk ran
+    uint32_t* out = gids + ((size_t)b << (2 * TL_BIN_LOG2));
+    for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS)
+        out[i] = (uint32_t)(keys[i] & 0xffffffffull);
+}
 
-    // resolve: the bin's pixels with a winner
+// One CTA per 32x32 bin: each pixel with a winner (bin_raster_kernel's slots)
+// is resolved -- start depth, the winner's barycentrics, varyings, shading,
+// one colour and depth write; the bin's extension-key bit is cleared.
+template <int FS, int FMT>
+__global__ void __launch_bounds__(TL_THREADS, 5) bin_resolve_kernel(
+    DrawParams P, sr_uniforms U, const float4* __restrict__ setup, const uint32_t* __restrict__ bin_off,
+    const uint32_t* __restrict__ gids, const uint32_t* __restrict__ vidx, const float* __restrict__ vary,
+    const uint32_t* __restrict__ tex, void* __restrict__ color, float* __restrict__ depth,
+    const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil, uint32_t* __restrict__ bitmap,
+    DeviceFlags* flags) {
+    if (flags->poison) return;
+    const uint32_t b = blockIdx.x;
+    const uint32_t cnt = bin_off[b + 1] - bin_off[b];
+    const bool ext = (bitmap[b >> 5] >> (b & 31)) & 1u;
+    if (cnt == 0 && !ext) return;
+    __syncthreads();   // every thread has read the bit before it is cleared
+    if (ext && threadIdx.x == 0) atomicAnd(bitmap + (b >> 5), ~(1u << (b & 31)));
+    const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
+    const uint32_t X0 = (b % P.bins_x) << TL_BIN_LOG2, Y0 = (b / P.bins_x) << TL_BIN_LOG2;
+    const uint32_t* in = gids + ((size_t)b << (2 * TL_BIN_LOG2));
     for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS) {
-        const unsigned long long k = keys[i];
-        if (!k) continue;
+        const uint32_t id = in[i];
+        if (!id) continue;   // also every slot outside the frame
         const uint32_t px = X0 + (i & 31), py = Y0 + (i >> TL_BIN_LOG2);
-        if (px > X1 || py > Y1) continue;
         const float d0 = P.has_depth ? depth[(size_t)py * P.W + px] : 0.0f;
-        resolve_pixel<FS, FMT>(P, U, px, py, k, d0, N, setup, vidx, vary, tex, color, depth, stencil,
-                               gate_with_stencil);
+        resolve_winner<FS, FMT>(P, U, px, py, id, d0, N, setup, vidx, vary, tex, color, depth, stencil,
+                                gate_with_stencil);
     }
 }
 
 template <int FS>
-static void launch_bin_raster_fs(const DrawParams& P, const sr_uniforms& U, const TiledArgs& A, uint32_t n_bins,
-                                 cudaStream_t st) {
-#define SR_BR(FMT) bin_raster_kernel<FS, FMT, 16><<<n_bins, TL_THREADS, 0, st>>>(P, U, A.setup, A.bin_off, A.entries, \
-        A.vidx, A.vary, A.tex, A.color, A.depth, A.stencil, A.gate, A.gkeys, A.bitmap, A.flags)
+static void launch_bin_resolve_fs(const DrawParams& P, const sr_uniforms& U, const TiledArgs& A, uint32_t n_bins,
+                                  cudaStream_t st) {
+#define SR_BR(FMT) bin_resolve_kernel<FS, FMT><<<n_bins, TL_THREADS, 0, st>>>(P, U, A.setup, A.bin_off, A.gids, \
+        A.vidx, A.vary, A.tex, A.color, A.depth, A.stencil, A.gate, A.bitmap, A.flags)
     if (P.color_format == SR_COLOR_RGBA32F) SR_BR(SR_COLOR_RGBA32F);
     else if (P.color_format == SR_COLOR_RGBA8) SR_BR(SR_COLOR_RGBA8);
     else SR_BR(SR_COLOR_NONE);
@@ -243,8 +373,8 @@ void ext_direct_launch(const DrawParams& P, const uint32_t* unsafe_list, const f
                        const float4* setup, unsigned long long* gkeys, uint32_t* bitmap, const uint8_t* stencil,
                        uint32_t gate, DeviceFlags* flags, cudaStream_t st);
 
-// launches: bin scan, scatter, extension keys, bin raster (setup, with the
-// bin counts, is launched by the caller)
+// launches: bin scan, scatter, extension keys, bin raster, bin resolve
+// (setup, with the bin counts, is launched by the caller)
 int launch_tiled(const DrawParams& P, const sr_uniforms& U, const TiledArgs& A, cudaStream_t st) {
     const uint32_t n_bins = P.bins_x * P.bins_y;
     bin_scan_kernel<<<1, 1024, 0, st>>>(A.bin_counts, n_bins, A.bin_off, A.flags);
@@ -253,14 +383,16 @@ int launch_tiled(const DrawParams& P, const sr_uniforms& U, const TiledArgs& A, 
         P.n_raster_host, n_launch, P.bins_x, A.binrect, A.bin_off, n_bins, A.cursor, A.entries, A.entry_cap,
         P.draw_id, A.flags);
     ext_direct_launch(P, A.unsafe_list, A.unsafe_rect, A.setup, A.gkeys, A.bitmap, A.stencil, A.gate, A.flags, st);
+    bin_raster_kernel<<<n_bins, TL_THREADS, 0, st>>>(P, A.setup, A.bin_off, A.entries, A.stencil, A.gate, A.gkeys,
+                                                     A.bitmap, A.gids, A.flags);
     switch (P.fs) {
-    case FS_BLINN_PHONG_DIR: launch_bin_raster_fs<FS_BLINN_PHONG_DIR>(P, U, A, n_bins, st); break;
-    case FS_TEXTURED_BLINN_PHONG: launch_bin_raster_fs<FS_TEXTURED_BLINN_PHONG>(P, U, A, n_bins, st); break;
-    case FS_VERTEX_COLOR: launch_bin_raster_fs<FS_VERTEX_COLOR>(P, U, A, n_bins, st); break;
-    case FS_ACES_LIGHTS: launch_bin_raster_fs<FS_ACES_LIGHTS>(P, U, A, n_bins, st); break;
-    default: launch_bin_raster_fs<FS_CONSTANT_COLOR>(P, U, A, n_bins, st); break;
+    case FS_BLINN_PHONG_DIR: launch_bin_resolve_fs<FS_BLINN_PHONG_DIR>(P, U, A, n_bins, st); break;
+    case FS_TEXTURED_BLINN_PHONG: launch_bin_resolve_fs<FS_TEXTURED_BLINN_PHONG>(P, U, A, n_bins, st); break;
+    case FS_VERTEX_COLOR: launch_bin_resolve_fs<FS_VERTEX_COLOR>(P, U, A, n_bins, st); break;
+    case FS_ACES_LIGHTS: launch_bin_resolve_fs<FS_ACES_LIGHTS>(P, U, A, n_bins, st); break;
+    default: launch_bin_resolve_fs<FS_CONSTANT_COLOR>(P, U, A, n_bins, st); break;
     }
-    return 4;
+    return 5;
 }
 
 }  // namespace sr

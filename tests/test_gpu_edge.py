@@ -48,6 +48,16 @@ GOOD = [(-0.8, -0.7, 0.3, 1.0), (0.7, -0.6, 0.4, 1.0), (0.0, 0.8, 0.5, 1.0),
         (-0.5, 0.5, 0.2, 1.0), (0.9, 0.9, 0.6, 1.0), (-0.9, 0.1, 0.7, 1.0)]
 
 
+@pytest.mark.parametrize("cull", [A.SR_CULL_CLOCKWISE, A.SR_CULL_COUNTER_CLOCKWISE])
+def test_nan_shoelace_area_culling(built_lib, oracle_mod, cull):
+    """A NaN shoelace sum (triangle.rs:53-61) winds counter-clockwise on the
+    GPU as in the oracle: the stencil shows whether the triangle was culled."""
+    nan = float("nan")
+    sc = _clip_scene(24, 20, [(-0.6, nan, 0.5, 1.0), (0.6, -0.5, 0.5, 1.0), (0.0, 0.7, 0.5, 1.0)] + GOOD[:3],
+                     stencil=True, stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT, cull=cull)
+    check(sc, oracle_mod)
+
+
 @pytest.mark.parametrize("gs_mode", [A.SR_GS_NONE, A.SR_GS_CLIP])
 def test_nan_vertex(built_lib, oracle_mod, gs_mode):
     nan = float("nan")

@@ -43,10 +43,12 @@ def test_png_round_trip(tmp_path):
 
 
 def _reference_asset(rel):
-    """A file of the reference checkout (SOFTRENDER_REFERENCE, else the
-    checkout this repository was built beside); None where it is absent."""
+    """A file of the reference checkout named by SOFTRENDER_REFERENCE; None
+    when that variable is unset or the file is absent."""
     import os
-    base = os.environ.get("SOFTRENDER_REFERENCE", "/root/reference")
+    base = os.environ.get("SOFTRENDER_REFERENCE")
+    if not base:
+        return None
     p = os.path.join(base, rel)
     return p if os.path.exists(p) else None
 
@@ -62,7 +64,7 @@ def test_obj_reference_suzanne(oracle_mod):
     from softrender import scenes
     path = _reference_asset("examples/assets/suzanne.obj")
     if path is None:
-        pytest.skip("the reference checkout is not present")
+        pytest.skip("SOFTRENDER_REFERENCE does not name a reference checkout")
     text = open(path).read()
     pos, nrm, uv, idx = sio.load_obj(path)
     assert idx.shape == (3 * 968,) and idx.max() < pos.shape[0]

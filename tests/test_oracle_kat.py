@@ -372,3 +372,27 @@ def test_nan_line_end_point(oracle_mod, aa):
     assert np.array_equal(fb.depth.view(np.uint32), fb2.depth.view(np.uint32))
     assert np.array_equal(fb.stencil, fb2.stencil)
     assert st["fragments"] == st2["fragments"] > 0
+
+
+@pytest.mark.parametrize("cull", [A.SR_CULL_CLOCKWISE, A.SR_CULL_COUNTER_CLOCKWISE])
+def test_nan_shoelace_area_winds_counter_clockwise(oracle_mod, cull):
+    """triangle.rs:53-61 culls by `a.is_sign_negative()` of the shoelace sum.
+    A vertex with a NaN coordinate makes that sum NaN, whose sign bit IEEE
+    754 leaves to the platform (x86's default NaN has it set, AArch64's and
+    CUDA's do not, and an input NaN's sign propagates).  Here a NaN sum is
+    read as not negative -- counter-clockwise -- on every platform: with
+    back faces counter-clockwise the triangle is culled and leaves the
+    stencil untouched; with clockwise culling it is kept, and its (finite,
+    NaN-ignoring) bbox counts stencil events in every tile pass though no
+    pixel is covered with a finite depth."""
+    W = H = 12
+    sc = _one_triangle_scene([(2.0, 2.0), (9.0, 3.0), (4.0, 9.0)], W, H, stencil=True,
+                             stencil_test=A.SR_STENCIL_ALWAYS, stencil_op=A.SR_STENCIL_INCREMENT, cull=cull)
+    sc.planes[1] = sc.planes[1].copy()
+    sc.planes[1][0] = np.float32(np.nan)          # vertex 1: y = NaN
+    fb, st, status = oracle_mod.render(sc)
+    assert status == 0 and st["fragments"] == 0
+    if cull == A.SR_CULL_COUNTER_CLOCKWISE:
+        assert (fb.stencil == 0).all()
+    else:
+        assert fb.stencil.max() >= 1
