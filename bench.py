@@ -137,6 +137,13 @@ def subsample_scene(scene, every):
     return sc
 
 
+def scenes_tiles(scene):
+    """The scene's semantic tiles (fragment.rs:188-216), from the oracle."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    return oracle.tiles(scene.width, scene.height, *scene.tile)
+
+
 def cpu_frame_estimate(scene, every, tiles, tile_begin=0, threads=None):
     """Times the oracle (the reference path restated, all host threads) on a
     bounded sample and extrapolates to one full frame, from the stage times
@@ -711,17 +718,19 @@ def run_reference(args, rank, world):
     from softrender import scenes
     scene = scenes.grid_sphere_scene()
     n_tris = scene.n_tris
+    # warm-up steps: small samples (the CPU path has no state to warm beyond
+    # caches); timed steps: whole frames -- every triangle through the vertex
+    # stage and the clip GS, every tile rasterised -- measured, not
+    # extrapolated (about 12-15 s each on 16 host cores).  Runs of more than
+    # 24 steps time 1 in n of the tiles per step instead (n chosen so the run
+    # stays near 24 frames' worth) and extrapolate the raster stage linearly.
     for i in range(args.warmup):
         cpu_frame_estimate(scene, every=64, tiles=4, tile_begin=4 * i)
     frames, sample, threads = [], "", os.cpu_count()
-    # one step samples 1 in 2 triangles over 64 tiles (about 7 s on 8 cores);
-    # beyond 20 steps each step samples up to 3x less (1 in 6 triangles over
-    # 21 tiles still estimates the frame within a few percent), so that long
-    # runs stay within a few minutes
-    shrink = min(3, max(1, -(-args.steps // 20)))
-    tiles = 64 // shrink
+    n_tiles = len(scenes_tiles(scene))
+    shrink = max(1, -(-args.steps // 24))
     for i in range(args.steps):
-        f, sample, threads = cpu_frame_estimate(scene, every=2 * shrink, tiles=tiles, tile_begin=i)
+        f, sample, threads = cpu_frame_estimate(scene, every=1, tiles=n_tiles // shrink, tile_begin=i)
         frames.append(f)
     frame_s = float(np.mean(frames))
     value = n_tris / frame_s / 1e6

@@ -533,6 +533,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
     std::memset(&P, 0, sizeof(P));
     P.W = W; P.H = H;
     P.tile_w = d->tile_w; P.tile_h = d->tile_h;
+    P.magic_w = div_magic(d->tile_w); P.magic_h = div_magic(d->tile_h);
     P.ncols = W >= 2 ? (W - 1 + d->tile_w - 1) / d->tile_w : 0;
     P.nrows = H >= 2 ? (H - 1 + d->tile_h - 1) / d->tile_h : 0;
     P.n_verts = m->n_verts;

@@ -322,7 +322,7 @@ __global__ void __launch_bounds__(256, 6) batch_raster_small_kernel(BTables T, c
             const uint32_t W = I.P.W, H = I.P.H;
             const uint32_t w = x1 - x0 + 1, wp = (w + 1) >> 1;
             mark_rect(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1);
-            const uint32_t sb = seam_bits(x0, y0, x1, y1, W, H, I.P.tile_w, I.P.tile_h);
+            const uint32_t sb = seam_bits(x0, y0, x1, y1, I.P);
             sxy[wl][lane_c] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
             sw[wl][lane_c] = wp | (w << 16);
             Slot S;
@@ -420,7 +420,7 @@ __global__ void __launch_bounds__(256) batch_raster_big_kernel(BTables T, const 
                 if (!(I.bitmap[bb >> 5] & bit)) atomicOr(I.bitmap + (bb >> 5), bit);
             }
         }
-        const uint32_t sb = seam_bits(x0, y0, x1, y1, W, H, I.P.tile_w, I.P.tile_h);
+        const uint32_t sb = seam_bits(x0, y0, x1, y1, I.P);
         // bbox pixels of the chunk, row-major; each thread steps its (row,
         // column) by blockDim pixels instead of dividing per pixel
         const uint32_t at = (uint32_t)area[g];
@@ -903,6 +903,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         DrawParams& P = I.P;
         P.W = W; P.H = H;
         P.tile_w = d->tile_w; P.tile_h = d->tile_h;
+        P.magic_w = div_magic(d->tile_w); P.magic_h = div_magic(d->tile_h);
         P.ncols = W >= 2 ? (W - 1 + d->tile_w - 1) / d->tile_w : 0;
         P.nrows = H >= 2 ? (H - 1 + d->tile_h - 1) / d->tile_h : 0;
         P.n_verts = m->n_verts;

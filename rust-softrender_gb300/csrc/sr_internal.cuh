@@ -103,6 +103,7 @@ struct DrawParams {
     uint32_t draw_id;             // sequence number of the draw since the last sync
     uint32_t force_unsafe;        // test hook: treat every primitive as unsafe
     uint32_t aa_lines;            // Xiaolin Wu lines (FragmentShader::antialiased_lines)
+    uint32_t magic_w, magic_h;    // div_magic(tile_w), div_magic(tile_h): set with the tile size on the host
 };
 
 // Setup record of a raster triangle (64 bytes):
@@ -120,6 +121,15 @@ struct StencilCountArgs {
     int* lines;                  // CX, CXa, CXb (W+1 each), CY, CYl, CYr (H+1 each)
     unsigned long long* globals; // N, L, R, A, B, LA, LB, RA, RB
 };
+
+// m = ceil(2^32 / t), so that floor(p / t) == umulhi32(p, m) for p < 2^15 and
+// 2 <= t < 2^16 (m = (2^32 + e) / t with e < t: the excess p e / (t 2^32)
+// stays below 1 / t).  For t == 1 it wraps to 0, which seam_count reads as
+// "every coordinate is a multiple of t".  Computed once per draw on the host
+// (DrawParams::magic_w, magic_h): the 64-bit division is slow on the device.
+__host__ __device__ __forceinline__ uint32_t div_magic(uint32_t t) {
+    return (uint32_t)((0x100000000ull + t - 1) / t);
+}
 
 // ------------------------------------------------------------ device helpers
 __device__ __forceinline__ uint32_t zkey(float z) {

@@ -50,7 +50,7 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
     const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     unsigned long long frags = 0;
-    const uint32_t mx = div_magic(P.tile_w), my = div_magic(P.tile_h);
+    const uint32_t mx = P.magic_w, my = P.magic_h;
     const uint32_t blocks_x = (P.W + 31) >> 5;
     for (;;) {
         // dynamic work queue: a warp takes the next G primitives
@@ -87,7 +87,7 @@ __global__ void __launch_bounds__(RG_THREADS) raster_small_kernel(
             srec[wl][c][2] = __ldg(r + 2);
             const uint32_t w = x1 - x0 + 1, wp = (w + 1) >> 1;
             mark_rect(bitmap, blocks_x, x0, y0, x1, y1);
-            const uint32_t sb = seam_bits(x0, y0, x1, y1, P.W, P.H, P.tile_w, P.tile_h);
+            const uint32_t sb = seam_bits(x0, y0, x1, y1, P);
             sxy[wl][c] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
             sw[wl][c] = wp | (w << 16);
             sst[wl][c] = ex;
@@ -134,7 +134,7 @@ __global__ void __launch_bounds__(RG_THREADS) raster_big_kernel(
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
     const uint32_t nb = (uint32_t)flags->n_big;
     unsigned long long frags = 0;
-    const uint32_t mx = div_magic(P.tile_w), my = div_magic(P.tile_h);
+    const uint32_t mx = P.magic_w, my = P.magic_h;
     const uint32_t blocks_x = (P.W + 31) >> 5;
     for (uint32_t k = blockIdx.x; k < nb; k += gridDim.x) {
         const uint32_t t = big_list[k];
@@ -145,8 +145,7 @@ __global__ void __launch_bounds__(RG_THREADS) raster_big_kernel(
         const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)P.W - 1);
         const uint32_t w = x1 - x0 + 1;
         const unsigned long long at = area[t];
-        const uint32_t sb = seam_bits(x0, y0, x1, (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1), P.W, P.H,
-                                      P.tile_w, P.tile_h);
+        const uint32_t sb = seam_bits(x0, y0, x1, (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1), P);
         {
             const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)P.H - 1);
             const uint32_t bx0 = x0 >> TOUCH_LOG2, by0 = y0 >> TOUCH_LOG2;

@@ -26,13 +26,6 @@ __host__ __device__ __forceinline__ uint32_t umulhi32(uint32_t a, uint32_t b) {
     return (uint32_t)(((uint64_t)a * b) >> 32);
 #endif
 }
-// m = ceil(2^32 / t), so that floor(p / t) == umulhi32(p, m) for p < 2^15 and
-// 2 <= t < 2^16 (m = (2^32 + e) / t with e < t: the excess p e / (t 2^32)
-// stays below 1 / t).  For t == 1 it wraps to 0, which seam_count reads as
-// "every coordinate is a multiple of t".
-__host__ __device__ __forceinline__ uint32_t div_magic(uint32_t t) {
-    return (uint32_t)((0x100000000ull + t - 1) / t);
-}
 // number of semantic tiles along one axis containing coordinate p (1 or 2)
 __host__ __device__ __forceinline__ int seam_count(uint32_t p, uint32_t t, uint32_t m, uint32_t last) {
     return (p > 0 && p < last && (m == 0 || umulhi32(p, m) * t == p)) ? 2 : 1;
@@ -114,17 +107,19 @@ __device__ __forceinline__ void rg_fragment(const DrawParams& P, float4 r0, floa
 }
 
 // Whether the clamped bbox [x0, x1] x [y0, y1] contains a seam column (bit 0:
-// 0 < p < W-1 with p a multiple of the tile width) or a seam row (bit 1).
-__device__ __forceinline__ uint32_t seam_bits(uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1, uint32_t W,
-                                              uint32_t H, uint32_t tile_w, uint32_t tile_h) {
+// 0 < p < W-1 with p a multiple of the tile width) or a seam row (bit 1): the
+// largest multiple of t up to hi, floor(hi / t) t (hi < 2^15, by the tile
+// size's division magic), is at least lo.
+__device__ __forceinline__ uint32_t seam_bits(uint32_t x0, uint32_t y0, uint32_t x1, uint32_t y1,
+                                              const DrawParams& P) {
     uint32_t s = 0;
     {
-        const uint32_t lo = max(x0, 1u), hi = min(x1, W - 2);
-        if (lo <= hi && ((lo + tile_w - 1) / tile_w) * tile_w <= hi) s |= 1u;
+        const uint32_t lo = max(x0, 1u), hi = min(x1, P.W - 2);
+        if (lo <= hi && (P.magic_w == 0 || umulhi32(hi, P.magic_w) * P.tile_w >= lo)) s |= 1u;
     }
     {
-        const uint32_t lo = max(y0, 1u), hi = min(y1, H - 2);
-        if (lo <= hi && ((lo + tile_h - 1) / tile_h) * tile_h <= hi) s |= 2u;
+        const uint32_t lo = max(y0, 1u), hi = min(y1, P.H - 2);
+        if (lo <= hi && (P.magic_h == 0 || umulhi32(hi, P.magic_h) * P.tile_h >= lo)) s |= 2u;
     }
     return s;
 }

@@ -155,6 +155,7 @@ extern "C" SR_API int sr_render_static(const sr_draw* d, const void* uniforms, s
     std::memset(&P, 0, sizeof(P));
     P.W = W; P.H = H;
     P.tile_w = d->tile_w; P.tile_h = d->tile_h;
+    P.magic_w = div_magic(d->tile_w); P.magic_h = div_magic(d->tile_h);
     P.ncols = (W - 1 + d->tile_w - 1) / d->tile_w;
     P.nrows = (H - 1 + d->tile_h - 1) / d->tile_h;
     P.n_verts = n_verts;

@@ -122,16 +122,14 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t n_host, uint3
     }
 }
 
-constexpr uint32_t TL_CHUNK = 128;   // primitives staged per chunk
+constexpr uint32_t TL_CHUNK = TL_THREADS;   // primitives staged per chunk (one per thread)
 constexpr uint32_t TL_QCAP = 160;    // pixels a warp's stack holds: 31 waiting + 4 x 32 pushed
 
-// Per staged primitive, the sign pre-test's operands: the numerators' edge
-// coefficients times s = det_sign(det), the anchor, |det| and the three
-// rejection thresholds (see bin_raster_kernel).
+// Per staged primitive, the sign pre-test's three rejection thresholds (see
+// bin_raster_kernel); the edge coefficients, anchor and det come from the
+// setup record, the sign s from its last word.
 struct PreRec {
-    float4 e;    // s A, s B, s C, s D   (A = y2-y3, B = x3-x2, C = y3-y1, D = x1-x3)
-    float4 a;    // x3, y3, s det, Tu
-    float2 t;    // Tv, Tw
+    float tu, tv, tw;
 };
 
 // One CTA per 32x32 bin reduces the winner key of each of its pixels in
@@ -170,6 +168,7 @@ __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
     __shared__ unsigned long long keys[1u << (2 * TL_BIN_LOG2)];
     __shared__ float4 srec[TL_CHUNK][3];
     __shared__ PreRec spre[TL_CHUNK];
+    __shared__ unsigned long long sfrags;
     __shared__ uint32_t sst[TL_CHUNK + 1];            // first item of each primitive; [n] = items
     __shared__ uint32_t sxy[TL_CHUNK];                // x0 | y0 << 16 (bin-relative) | seam bits 15, 31
     __shared__ uint32_t sw[TL_CHUNK];                 // runs per row | clipped width << 16
@@ -199,7 +198,7 @@ __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
 
     const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
     unsigned long long frags = 0;
-    const uint32_t mx = div_magic(P.tile_w), my = div_magic(P.tile_h);
+    const uint32_t mx = P.magic_w, my = P.magic_h;
     const uint32_t lt = (1u << lane) - 1u;   // lanes below this one
     for (uint32_t c0 = 0; c0 < cnt; c0 += TL_CHUNK) {
         const uint32_t n = min(cnt - c0, TL_CHUNK);
@@ -217,24 +216,22 @@ __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
             srec[threadIdx.x][0] = r0;
             srec[threadIdx.x][1] = r1;
             srec[threadIdx.x][2] = r2;
-            const float s = r2.w;
             PreRec pr;
-            pr.e = make_float4(s * r0.x, s * r0.y, s * r0.z, s * r0.w);
-            const float INF = __int_as_float(0x7f800000);
-            if (s != 0.0f) {
+            if (r2.w != 0.0f) {
                 // bounds of |x - x3| and |y - y3| over the clipped bbox's pixel centres
                 const float xr = fmaxf(fabsf(((float)x0 + 0.5f) - r1.x), fabsf(((float)x1 + 0.5f) - r1.x)) * 1.001f;
                 const float yr = fmaxf(fabsf(((float)y0 + 0.5f) - r1.y), fabsf(((float)y1 + 0.5f) - r1.y)) * 1.001f;
                 const float su = fabsf(r0.x) * xr + fabsf(r0.y) * yr, sv = fabsf(r0.z) * xr + fabsf(r0.w) * yr;
                 const float ad = fabsf(r1.z);
-                pr.a = make_float4(r1.x, r1.y, ad, 1.0e-18f + 0x1p-20f * su);
-                pr.t = make_float2(1.0e-18f + 0x1p-20f * sv, 0x1p-20f * ((ad + su) + sv) + 0x1p-140f * ad);
+                pr.tu = 1.0e-18f + 0x1p-20f * su;
+                pr.tv = 1.0e-18f + 0x1p-20f * sv;
+                pr.tw = 0x1p-20f * ((ad + su) + sv) + 0x1p-140f * ad;
             } else {   // no sign information: keep every pixel for the exact test
-                pr.a = make_float4(r1.x, r1.y, 0.0f, INF);
-                pr.t = make_float2(INF, INF);
+                const float INF = __int_as_float(0x7f800000);
+                pr.tu = INF; pr.tv = INF; pr.tw = INF;
             }
             spre[threadIdx.x] = pr;
-            const uint32_t sb = seam_bits(x0, y0, x1, y1, P.W, P.H, P.tile_w, P.tile_h);
+            const uint32_t sb = seam_bits(x0, y0, x1, y1, P);
             sxy[threadIdx.x] = (x0 - X0) | ((y0 - Y0) << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
             sw[threadIdx.x] = wq | (w << 16);
             st[threadIdx.x] = t;
@@ -277,15 +274,18 @@ __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
                 ly = ((xy >> 16) & 0x7fffu) + row;
                 const uint32_t left = min((wqw >> 16) - col, 4u);
                 const PreRec pr = spre[o];
-                const float dx = ((float)(X0 + lx) + 0.5f) - pr.a.x;
-                const float dy = ((float)(Y0 + ly) + 0.5f) - pr.a.y;
-                float eu = pr.e.x * dx + pr.e.y * dy;
-                float ev = pr.e.z * dx + pr.e.w * dy;
+                const float4 r0 = srec[o][0], r1 = srec[o][1];
+                const float sg = srec[o][2].w;   // det_sign(det)
+                const float sa = sg * r0.x, sb = sg * r0.y, sc = sg * r0.z, sd = sg * r0.w, ad = sg * r1.z;
+                const float dx = ((float)(X0 + lx) + 0.5f) - r1.x;
+                const float dy = ((float)(Y0 + ly) + 0.5f) - r1.y;
+                float eu = sa * dx + sb * dy;
+                float ev = sc * dx + sd * dy;
 #pragma unroll
                 for (uint32_t k = 0; k < 4; ++k) {
-                    if (k) { eu = eu + pr.e.x; ev = ev + pr.e.z; }
-                    const float ew = (pr.a.z - eu) - ev;
-                    const bool keep = !(eu < -pr.a.w) && !(ev < -pr.t.x) && !(ew < -pr.t.y);
+                    if (k) { eu = eu + sa; ev = ev + sc; }
+                    const float ew = (ad - eu) - ev;
+                    const bool keep = !(eu < -pr.tu) && !(ev < -pr.tv) && !(ew < -pr.tw);
                     if (k < left && keep) cm |= 1u << k;
                 }
             }
@@ -318,11 +318,15 @@ __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
                 __syncwarp();
             }
         }
-        __syncthreads();   // the chunk's staging is reused by the next chunk
+        if (c0 + TL_CHUNK < cnt) __syncthreads();   // the chunk's staging is reused by the next chunk
     }
+    // one atomic per CTA for the fragment count
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
-    if (lane == 0 && frags) atomicAdd(&flags->fragments, frags);
-    if (cnt == 0) __syncthreads();   // the extension keys' seeding, when no chunk ran
+    if (threadIdx.x == 0) sfrags = 0;
+    __syncthreads();   // every warp's keys are final (and the extension keys' seeding, when no chunk ran)
+    if (lane == 0 && frags) atomicAdd(&sfrags, frags);
+    __syncthreads();
+    if (threadIdx.x == 0 && sfrags) atomicAdd(&flags->fragments, sfrags);
     uint32_t* out = gids + ((size_t)b << (2 * TL_BIN_LOG2));
     for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS)
         out[i] = (uint32_t)(keys[i] & 0xffffffffull);
