@@ -283,8 +283,10 @@ SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t);
  * and stencil, read as a texture without a copy): a texture that reads the
  * pipeline's colour plane in place, RGBA8 or RGBA f32.  It sees the
  * pipeline's draws once they are complete (sr_sync the pipeline, or draw on
- * the same stream), stays valid until the pipeline is destroyed, and is
- * released with sr_texture_free (which leaves the plane alone).  A draw may
+ * the same stream).  The view holds a reference on the colour plane, as draws
+ * hold references on meshes: destroying the pipeline leaves the plane (with
+ * its last contents) to the views and the pending draws that sample them, and
+ * the last sr_texture_free of a view frees it.  A draw may
  * not sample the plane it writes, a batch or a server request may not sample
  * a view at all, and sr_texture_update of a view is refused (SR_EINVAL). */
 SR_API int sr_texture_view_framebuffer(sr_pipeline* p, sr_texture** out);

@@ -164,7 +164,12 @@ int sr::pipeline_create_cap(const sr_fb_desc* fb, size_t cap_px, sr_pipeline** o
     const size_t n = std::max(cap_px, (size_t)fb->width * fb->height);
     p->cap_px = n;
     cudaError_t e = cudaSuccess;
-    if (bytes_per_color(fb->color_format)) e = cudaMalloc(&p->color, n * bytes_per_color(fb->color_format));
+    if (bytes_per_color(fb->color_format)) {
+        p->color_plane = new (std::nothrow) sr_color_plane();
+        if (!p->color_plane) { sr_pipeline_destroy(p); return SR_ENOMEM; }
+        e = cudaMalloc(&p->color_plane->data, n * bytes_per_color(fb->color_format));
+        p->color = p->color_plane->data;
+    }
     if (e == cudaSuccess && fb->depth) e = cudaMalloc(&p->depth, n * 4);
     if (e == cudaSuccess && fb->stencil) e = cudaMalloc(&p->stencil, n);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->own_stream, cudaStreamNonBlocking);
@@ -210,7 +215,7 @@ extern "C" SR_API int sr_pipeline_destroy(sr_pipeline* p) {
         texture_unref(pd.d.texture);
     }
     p->pending.clear();
-    if (p->color) cudaFree(p->color);
+    color_plane_unref(p->color_plane);   // texture views may still hold the plane
     if (p->depth) cudaFree(p->depth);
     if (p->stencil) cudaFree(p->stencil);
     if (p->flags) cudaFree(p->flags);
@@ -470,6 +475,8 @@ extern "C" SR_API int sr_texture_view_framebuffer(sr_pipeline* p, sr_texture** o
     t->h = p->fb.height;
     t->f32 = p->fb.color_format == SR_COLOR_RGBA32F ? 1u : 0u;
     t->view = true;
+    t->plane = p->color_plane;
+    t->plane->refs.fetch_add(1, std::memory_order_relaxed);
     *out = t;
     return SR_OK;
 }
@@ -509,7 +516,8 @@ extern "C" SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t)
 void sr::texture_unref(const sr_texture* ct) {
     sr_texture* t = const_cast<sr_texture*>(ct);
     if (!t || t->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
-    if (t->data && !t->view) cudaFree(t->data);
+    if (t->view) color_plane_unref(t->plane);
+    else if (t->data) cudaFree(t->data);
     delete t;
 }
 
@@ -655,7 +663,10 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
         if (p->gen_vert_cap > (1ull << 30)) p->gen_vert_cap = 1ull << 30;
     }
     uint64_t n_raster_cap = indexed ? P.n_in : p->gen_tri_cap;
-    if (p->entry_cap < 2 * n_raster_cap + n_bins) p->entry_cap = 2 * n_raster_cap + n_bins;
+    // (bin, primitive) pairs: about two per small primitive, plus the bins of
+    // large ones -- 16 per bin covers a frame overlapped a dozen times by
+    // large triangles without the overflow replay (a few KB per bin)
+    if (p->entry_cap < 2 * n_raster_cap + 16ull * n_bins) p->entry_cap = 2 * n_raster_cap + 16ull * n_bins;
     if (p->entry_cap > 0xffffffffull) p->entry_cap = 0xffffffffull;
     P.gen_tri_cap = (uint32_t)p->gen_tri_cap;
     P.gen_vert_cap = (uint32_t)p->gen_vert_cap;
@@ -694,7 +705,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
         const size_t nblk = (size_t)((W + 31) / 32) * ((H + 31) / 32);
         const bool fresh = p->gkeys.cap < npx || p->bitmap.cap < (nblk + 31) / 32;
         if (tiled) {
-            if ((rc = p->bin_counts.ensure(2 * (size_t)n_bins)) || (rc = p->bin_off.ensure((size_t)n_bins + 1)) ||
+            if ((rc = p->bin_counts.ensure(2 * (size_t)n_bins)) || (rc = p->bin_off.ensure(2 * (size_t)n_bins + 2)) ||
                 (rc = p->entries.ensure(p->entry_cap)) || (rc = p->gkeys.ensure(npx)) ||
                 (rc = p->bitmap.ensure((nblk + 31) / 32)) || (rc = p->gids.ensure((size_t)n_bins << 10)))
                 return rc;
@@ -761,7 +772,8 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
                        p->depth, p->stencil, gate, p->flags, st);
         launches += 1;
     } else if (tiled) {
-        TiledArgs T{p->setup.p, p->binrect.p, p->bin_counts.p, p->bin_counts.p + n_bins, p->bin_off.p, p->entries.p,
+        TiledArgs T{p->setup.p, p->binrect.p, p->bin_counts.p, p->bin_counts.p + n_bins, p->bin_off.p,
+                    p->bin_off.p + n_bins + 1, p->entries.p,
                     p->entry_cap, p->gkeys.p, p->bitmap.p, p->gids.p, p->unsafe_list.p, p->unsafe_rect.p, vidx,
                     p->vary.p, tex, p->color, p->depth, p->stencil, gate, p->flags};
         launches += (uint32_t)launch_tiled(P, pd.U, T, st);

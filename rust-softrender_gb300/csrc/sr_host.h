@@ -66,7 +66,8 @@ struct PendingDraw {
 struct sr_pipeline {
     sr_fb_desc fb;
     size_t cap_px = 0;          // pixels the colour/depth/stencil planes were allocated for
-    void* color = nullptr;
+    void* color = nullptr;                  // color_plane->data
+    sr_color_plane* color_plane = nullptr;  // referenced by the pipeline and its texture views
     float* depth = nullptr;
     uint8_t* stencil = nullptr;
     sr_uniforms U;
@@ -122,6 +123,12 @@ inline void texture_ref(const sr_texture* t) {
 }
 void mesh_unref(const sr_mesh* m);
 void texture_unref(const sr_texture* t);
+// Releases one reference on a colour plane; the last frees its memory.
+inline void color_plane_unref(sr_color_plane* c) {
+    if (!c || c->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
+    if (c->data) cudaFree(c->data);
+    delete c;
+}
 // Target-independent eligibility of a draw for sr_batch_render (SR_OK or
 // SR_EINVAL), shared with the server's submission checks.
 int batch_draw_check(const sr_draw* d);

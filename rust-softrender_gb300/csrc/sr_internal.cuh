@@ -291,11 +291,19 @@ struct sr_mesh {
     std::atomic<uint32_t> refs{1};
 };
 
+// A pipeline's colour plane, shared with the texture views of it: the
+// pipeline and every view hold a reference, the last release frees it.
+struct sr_color_plane {
+    void* data = nullptr;
+    std::atomic<uint32_t> refs{1};
+};
+
 struct sr_texture {
     uint32_t* data = nullptr;       // RGBA8 texels, or RGBA f32 texels (4 floats each) when f32
     uint32_t w = 0, h = 0;
     uint32_t f32 = 0;               // 1: RGBA f32 texels
-    bool view = false;              // reads a pipeline's colour plane in place (data not owned)
+    bool view = false;              // reads a pipeline's colour plane in place (`plane`, referenced)
+    sr_color_plane* plane = nullptr;
     std::atomic<uint32_t> refs{1};
 };
 
@@ -370,6 +378,7 @@ struct TiledArgs {
     const uint32_t* bin_counts;      // primitives per bin (setup output)
     uint32_t* cursor;                // n_bins slot counters, zero
     uint32_t* bin_off;               // n_bins + 1 list offsets
+    uint32_t* chunk_off;             // n_bins + 1 offsets of the bins' raster work items
     uint32_t* entries;               // the bins' primitive lists
     uint64_t entry_cap;
     unsigned long long* gkeys;       // W x H extension keys, zero between draws

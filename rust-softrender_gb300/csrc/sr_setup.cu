@@ -171,9 +171,22 @@ __global__ void __launch_bounds__(256) setup_kernel(DrawParams P, uint32_t n_hos
         // counts come from the per-primitive scan (sr_bins.cu)
     } else if (single_bin < 0xfffffffeu) {
         if (lane == __ffs(peers) - 1) atomicAdd(bin_counts + single_bin, (uint32_t)__popc(peers));
-    } else if (n_entries) {
+    } else if (n_entries && n_entries <= 16) {
         for (uint32_t by = ry0; by <= ry1; ++by)
             for (uint32_t bx = rx0; bx <= rx1; ++bx) atomicAdd(bin_counts + by * P.bins_x + bx, 1u);
+    }
+    // bin rectangles of more than 16 bins: the warp's lanes share each one's bins
+    if (bin_counts) {
+        uint32_t big = __ballot_sync(0xffffffffu, n_entries > 16);
+        while (big) {
+            const uint32_t src = __ffs(big) - 1;
+            big &= big - 1;
+            const uint32_t bx0 = __shfl_sync(0xffffffffu, rx0, src), by0 = __shfl_sync(0xffffffffu, ry0, src);
+            const uint32_t bw = __shfl_sync(0xffffffffu, rx1, src) - bx0 + 1;
+            const uint32_t nb = (uint32_t)__shfl_sync(0xffffffffu, (uint32_t)n_entries, src);
+            for (uint32_t i = lane; i < nb; i += 32)
+                atomicAdd(bin_counts + (by0 + i / bw) * P.bins_x + bx0 + i % bw, 1u);
+        }
     }
     // stencil global counters, one atomic per warp and counter
     if (P.stencil_active && !P.mode_b) {

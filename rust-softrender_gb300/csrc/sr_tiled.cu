@@ -37,64 +37,88 @@ constexpr uint32_t TL_WARPS = TL_THREADS / 32;
 constexpr uint32_t TL_BIN_LOG2 = 5;   // bins of 32 x 32 pixels (the touched-block bitmap's granularity)
 static_assert(TL_BIN_LOG2 == TOUCH_LOG2, "the extension keys' bitmap marks bins");
 
-// Exclusive scan of the n bin counts in one CTA, 8192 at a time: coalesced
-// loads into shared memory, each thread scans 8 consecutive counts (padded
-// slots, no bank conflicts), a CTA-wide scan of the thread sums, coalesced
-// stores.  out[n] = total.
-constexpr uint32_t BS_TILE = 8192;
+constexpr uint32_t TL_CHUNK = TL_THREADS;   // primitives a raster work item stages (one per thread)
+
+// Exclusive scans, in one CTA, of the n bins' primitive counts (list offsets)
+// and of their work items: ceil(count / TL_CHUNK) chunks per bin, one for a
+// bin with only extension keys, none for an empty bin.  4096 bins at a time:
+// coalesced loads into shared memory, each thread scans 4 consecutive bins,
+// a CTA-wide scan of the thread sums, coalesced stores.  off[n] and
+// chunk_off[n] are the totals.  A draw whose lists outgrow the entry buffer
+// (the total summed in 64 bits) poisons the pipeline: sr_sync grows the
+// buffer and replays.
+constexpr uint32_t BS_TILE = 4096;
 __device__ __forceinline__ uint32_t bs_slot(uint32_t i) { return i + (i >> 5); }
-__global__ void __launch_bounds__(1024) bin_scan_kernel(const uint32_t* __restrict__ in, uint32_t n,
-                                                        uint32_t* __restrict__ out, const DeviceFlags* flags) {
-    __shared__ uint32_t tile[BS_TILE + BS_TILE / 32];
+__global__ void __launch_bounds__(1024) bin_scan_kernel(const uint32_t* __restrict__ counts,
+                                                        const uint32_t* __restrict__ bitmap, uint32_t n,
+                                                        uint32_t* __restrict__ off, uint32_t* __restrict__ chunk_off,
+                                                        uint64_t cap, uint32_t draw_id, DeviceFlags* flags) {
+    __shared__ uint32_t te[BS_TILE + BS_TILE / 32], tc[BS_TILE + BS_TILE / 32];
     if (flags->poison) return;
-    uint32_t carry = 0;
+    unsigned long long carry_e = 0;
+    uint32_t carry_c = 0;
     for (uint32_t base = 0; base < n; base += BS_TILE) {
         const uint32_t m = min(BS_TILE, n - base);
-        for (uint32_t i = threadIdx.x; i < BS_TILE; i += 1024) tile[bs_slot(i)] = i < m ? in[base + i] : 0u;
-        __syncthreads();
-        uint32_t v[BS_TILE / 1024];
-        uint32_t s = 0;
-#pragma unroll
-        for (uint32_t k = 0; k < BS_TILE / 1024; ++k) {
-            v[k] = tile[bs_slot(threadIdx.x * (BS_TILE / 1024) + k)];
-            s += v[k];
-        }
-        uint32_t tot;
-        uint32_t ex = block_exclusive_scan<uint32_t, 1024>(s, &tot) + carry;
-#pragma unroll
-        for (uint32_t k = 0; k < BS_TILE / 1024; ++k) {
-            tile[bs_slot(threadIdx.x * (BS_TILE / 1024) + k)] = ex;
-            ex += v[k];
+        for (uint32_t i = threadIdx.x; i < BS_TILE; i += 1024) {
+            const uint32_t b = base + i;
+            const uint32_t e = i < m ? counts[b] : 0u;
+            const bool ext = i < m && ((bitmap[b >> 5] >> (b & 31)) & 1u);
+            te[bs_slot(i)] = e;
+            tc[bs_slot(i)] = e ? (e + TL_CHUNK - 1) / TL_CHUNK : (ext ? 1u : 0u);
         }
         __syncthreads();
-        for (uint32_t i = threadIdx.x; i < m; i += 1024) out[base + i] = tile[bs_slot(i)];
-        carry += tot;
+        constexpr uint32_t PER = BS_TILE / 1024;
+        uint32_t ve[PER], vc[PER];
+        unsigned long long se = 0;
+        uint32_t sc = 0;
+#pragma unroll
+        for (uint32_t k = 0; k < PER; ++k) {
+            ve[k] = te[bs_slot(threadIdx.x * PER + k)];
+            vc[k] = tc[bs_slot(threadIdx.x * PER + k)];
+            se += ve[k];
+            sc += vc[k];
+        }
+        unsigned long long tot_e;
+        uint32_t tot_c;
+        unsigned long long xe = block_exclusive_scan<unsigned long long, 1024>(se, &tot_e) + carry_e;
+        uint32_t xc = block_exclusive_scan<uint32_t, 1024>(sc, &tot_c) + carry_c;
+#pragma unroll
+        for (uint32_t k = 0; k < PER; ++k) {
+            te[bs_slot(threadIdx.x * PER + k)] = (uint32_t)min(xe, 0xffffffffull);
+            tc[bs_slot(threadIdx.x * PER + k)] = xc;
+            xe += ve[k];
+            xc += vc[k];
+        }
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < m; i += 1024) {
+            off[base + i] = te[bs_slot(i)];
+            chunk_off[base + i] = tc[bs_slot(i)];
+        }
+        carry_e += tot_e;
+        carry_c += tot_c;
         __syncthreads();
     }
-    if (threadIdx.x == 0) out[n] = carry;
-}
-
-// Writes every primitive into the list of each bin its clamped bbox meets.
-// A draw whose lists outgrow the entry buffer poisons the pipeline (sr_sync
-// grows the buffer and replays).  `cursor` (n_bins, zero) counts the slots
-// taken per bin.  One-bin primitives of a warp that share a bin take their
-// slots with one atomic.
-__global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t n_host, uint32_t n_launch, uint32_t bins_x,
-                                                          const uint2* __restrict__ binrect,
-                                                          const uint32_t* __restrict__ bin_off, uint32_t n_bins,
-                                                          uint32_t* __restrict__ cursor, uint32_t* __restrict__ entries,
-                                                          uint64_t cap, uint32_t draw_id, DeviceFlags* flags) {
-    if (flags->poison) return;
-    const uint32_t total = bin_off[n_bins];
-    if (total > cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) {
-            if (total > flags->need_entries) flags->need_entries = total;
+    if (threadIdx.x == 0) {
+        off[n] = (uint32_t)min(carry_e, 0xffffffffull);
+        chunk_off[n] = carry_c;
+        if (carry_e > cap) {
+            if (carry_e > flags->need_entries) flags->need_entries = carry_e;
             atomicOr(&flags->overflow_bits, (unsigned)OVF_ENTRIES);
             atomicOr(&flags->poison, 1u);
             atomicMin(&flags->poison_draw, draw_id);
         }
-        return;
     }
+}
+
+// Writes every primitive into the list of each bin its clamped bbox meets.
+// `cursor` (n_bins, zero) counts the slots taken per bin.  One-bin primitives
+// of a warp that share a bin take their slots with one atomic.
+__global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t n_host, uint32_t n_launch, uint32_t bins_x,
+                                                          const uint2* __restrict__ binrect,
+                                                          const uint32_t* __restrict__ bin_off, uint32_t n_bins,
+                                                          uint32_t* __restrict__ cursor, uint32_t* __restrict__ entries,
+                                                          DeviceFlags* flags) {
+    if (flags->poison) return;   // also when the lists outgrow the entry buffer (bin_scan_kernel)
     const uint32_t n = n_host ? n_host : (uint32_t)flags->n_gen_tris;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t lane = threadIdx.x & 31;
@@ -111,18 +135,31 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t n_host, uint3
     uint32_t base = 0;
     if (single != 0xffffffffu && lane == leader) base = atomicAdd(cursor + single, (uint32_t)__popc(peers));
     base = __shfl_sync(0xffffffffu, base, leader);
+    const uint32_t nb = br.x != RECT_EMPTY ? (bx1 - bx0 + 1) * (by1 - by0 + 1) : 0u;
     if (single != 0xffffffffu) {
         entries[bin_off[single] + base + __popc(peers & ((1u << lane) - 1u))] = t;
-    } else if (br.x != RECT_EMPTY) {
+    } else if (nb && nb <= 16) {
         for (uint32_t by = by0; by <= by1; ++by)
             for (uint32_t bx = bx0; bx <= bx1; ++bx) {
                 const uint32_t b = by * bins_x + bx;
                 entries[bin_off[b] + atomicAdd(cursor + b, 1u)] = t;
             }
     }
+    // rectangles of more than 16 bins: the warp's lanes share each one's bins
+    uint32_t big = __ballot_sync(0xffffffffu, nb > 16);
+    while (big) {
+        const uint32_t src = __ffs(big) - 1;
+        big &= big - 1;
+        const uint32_t sx0 = __shfl_sync(0xffffffffu, bx0, src), sy0 = __shfl_sync(0xffffffffu, by0, src);
+        const uint32_t sw = __shfl_sync(0xffffffffu, bx1, src) - sx0 + 1;
+        const uint32_t sn = __shfl_sync(0xffffffffu, nb, src), st = __shfl_sync(0xffffffffu, t, src);
+        for (uint32_t i = lane; i < sn; i += 32) {
+            const uint32_t b = (sy0 + i / sw) * bins_x + sx0 + i % sw;
+            entries[bin_off[b] + atomicAdd(cursor + b, 1u)] = st;
+        }
+    }
 }
 
-constexpr uint32_t TL_CHUNK = TL_THREADS;   // primitives staged per chunk (one per thread)
 constexpr uint32_t TL_QCAP = 160;    // pixels a warp's stack holds: 31 waiting + 4 x 32 pushed
 
 // Per staged primitive, the sign pre-test's three rejection thresholds (see
@@ -132,17 +169,22 @@ struct PreRec {
     float tu, tv, tw;
 };
 
-// One CTA per 32x32 bin reduces the winner key of each of its pixels in
-// shared memory and writes the key's low word (pass * N + primitive + 1, 0
-// for no fragment) to the bin's 1024 slots of `gids`; bin_resolve_kernel
-// shades them.  The bin's primitive list is taken in chunks of TL_CHUNK: each
-// primitive's bbox clipped to the bin gives its items (runs of four
-// horizontally adjacent pixels, ceil(w / 4) per row), a CTA-wide scan numbers
-// them, and the items are split into equal contiguous ranges, one per warp.
-// Every binned primitive's bbox meets its bin, so every primitive of a chunk
-// has items and their first items are strictly increasing: a warp finds the
-// owner of its first item by binary search and then, per window of 32 items,
-// the primitives starting inside the window from one load per lane.
+// Work item = one chunk of up to TL_CHUNK primitives of one 32x32 bin's list
+// (bin_scan_kernel numbers them).  Persistent CTAs take items from a counter.
+// For each item the CTA reduces the winner key of each pixel of the bin in
+// shared memory; a bin with one item writes the keys' low words (pass * N +
+// primitive + 1, 0 for no fragment) to its 1024 slots of `gids`, a bin with
+// several items -- a long list, as a dense mesh on a small frame gives --
+// merges each non-zero key into the pixel's slot of the global key buffer
+// with a 64-bit atomicMax, which also holds any extension keys of the bin;
+// bin_resolve_kernel shades either.  Each chunk primitive's bbox clipped to
+// the bin gives its items (runs of four horizontally adjacent pixels,
+// ceil(w / 4) per row), a CTA-wide scan numbers them, and they are split into
+// equal contiguous ranges, one per warp.  Every binned primitive's bbox meets
+// its bin, so every primitive of a chunk has items and their first items are
+// strictly increasing: a warp finds the owner of its first item by binary
+// search and then, per window of 32 items, the primitives starting inside the
+// window from one load per lane.
 //
 // Pre-test.  With s = det_sign(det) (non-zero for 0 < |det| < 1e18), the run's
 // first pixel gets eu = (sA) dx + (sB) dy and ev = (sC) dx + (sD) dy with the
@@ -162,13 +204,14 @@ struct PreRec {
 // the key) with every lane busy.
 __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
     DrawParams P, const float4* __restrict__ setup, const uint32_t* __restrict__ bin_off,
-    const uint32_t* __restrict__ entries, const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
-    unsigned long long* __restrict__ gkeys, const uint32_t* __restrict__ bitmap, uint32_t* __restrict__ gids,
-    DeviceFlags* flags) {
+    const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ entries, const uint8_t* __restrict__ stencil,
+    uint32_t gate_with_stencil, unsigned long long* __restrict__ gkeys, const uint32_t* __restrict__ bitmap,
+    uint32_t* __restrict__ gids, DeviceFlags* flags) {
     __shared__ unsigned long long keys[1u << (2 * TL_BIN_LOG2)];
     __shared__ float4 srec[TL_CHUNK][3];
     __shared__ PreRec spre[TL_CHUNK];
     __shared__ unsigned long long sfrags;
+    __shared__ uint32_t sitem;
     __shared__ uint32_t sst[TL_CHUNK + 1];            // first item of each primitive; [n] = items
     __shared__ uint32_t sxy[TL_CHUNK];                // x0 | y0 << 16 (bin-relative) | seam bits 15, 31
     __shared__ uint32_t sw[TL_CHUNK];                 // runs per row | clipped width << 16
@@ -176,35 +219,52 @@ __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
     __shared__ uint32_t st[TL_CHUNK];                 // primitive index
     __shared__ uint32_t squeue[TL_WARPS][TL_QCAP];    // pre-tested pixels: chunk slot << 10 | y << 5 | x
     if (flags->poison) return;
-    const uint32_t b = blockIdx.x;
-    const uint32_t e0 = bin_off[b], cnt = bin_off[b + 1] - e0;
-    const bool ext = (bitmap[b >> 5] >> (b & 31)) & 1u;
-    if (cnt == 0 && !ext) return;   // no fragment can land here (bin_resolve_kernel skips it too)
+    const uint32_t n_bins = P.bins_x * P.bins_y;
+    const uint32_t n_items = chunk_off[n_bins];
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
-    const uint32_t X0 = (b % P.bins_x) << TL_BIN_LOG2, Y0 = (b / P.bins_x) << TL_BIN_LOG2;
-    const uint32_t X1 = min(X0 + (1u << TL_BIN_LOG2) - 1, P.W - 1), Y1 = min(Y0 + (1u << TL_BIN_LOG2) - 1, P.H - 1);
-    for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS) {
-        unsigned long long k = 0;
-        if (ext) {
-            const uint32_t px = X0 + (i & 31), py = Y0 + (i >> TL_BIN_LOG2);
-            if (px <= X1 && py <= Y1) {
-                const size_t gi = (size_t)py * P.W + px;
-                k = gkeys[gi];
-                if (k) gkeys[gi] = 0;
-            }
-        }
-        keys[i] = k;
-    }
-
     const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    unsigned long long frags = 0;
     const uint32_t mx = P.magic_w, my = P.magic_h;
     const uint32_t lt = (1u << lane) - 1u;   // lanes below this one
-    for (uint32_t c0 = 0; c0 < cnt; c0 += TL_CHUNK) {
-        const uint32_t n = min(cnt - c0, TL_CHUNK);
+    if (threadIdx.x == 0) sfrags = 0;
+    unsigned long long frags = 0;
+    for (;;) {
+        if (threadIdx.x == 0) sitem = (uint32_t)atomicAdd(&flags->work_raster, 1ull);
+        __syncthreads();   // the previous item is done with the shared arrays
+        const uint32_t item = sitem;
+        if (item >= n_items) break;
+        // the item's bin: the last bin whose first item is <= item
+        uint32_t b = 0;
+        {
+            uint32_t lo = 0, hi = n_bins;
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (__ldg(chunk_off + mid) <= item) lo = mid; else hi = mid;
+            }
+            b = lo;
+        }
+        const uint32_t c_first = __ldg(chunk_off + b), n_chunks = __ldg(chunk_off + b + 1) - c_first;
+        const bool whole = n_chunks == 1;   // the bin's only item: it owns the pixels' keys
+        const uint32_t e_bin = __ldg(bin_off + b), cnt_bin = __ldg(bin_off + b + 1) - e_bin;
+        const uint32_t c0 = (item - c_first) * TL_CHUNK;
+        const uint32_t n = cnt_bin > c0 ? min(cnt_bin - c0, TL_CHUNK) : 0u;
+        const bool ext = (bitmap[b >> 5] >> (b & 31)) & 1u;
+        const uint32_t X0 = (b % P.bins_x) << TL_BIN_LOG2, Y0 = (b / P.bins_x) << TL_BIN_LOG2;
+        const uint32_t X1 = min(X0 + (1u << TL_BIN_LOG2) - 1, P.W - 1), Y1 = min(Y0 + (1u << TL_BIN_LOG2) - 1, P.H - 1);
+        for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS) {
+            unsigned long long k = 0;
+            if (whole && ext) {   // seed with the bin's extension keys (they stay in gkeys otherwise)
+                const uint32_t px = X0 + (i & 31), py = Y0 + (i >> TL_BIN_LOG2);
+                if (px <= X1 && py <= Y1) {
+                    const size_t gi = (size_t)py * P.W + px;
+                    k = gkeys[gi];
+                    if (k) gkeys[gi] = 0;
+                }
+            }
+            keys[i] = k;
+        }
         uint32_t a = 0;
         if (threadIdx.x < n) {
-            const uint32_t t = __ldg(entries + e0 + c0 + threadIdx.x);
+            const uint32_t t = __ldg(entries + e_bin + c0 + threadIdx.x);
             const float4* r = setup + 4 * (size_t)t;
             const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
             const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), (int)X0);
@@ -318,44 +378,60 @@ __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
                 __syncwarp();
             }
         }
-        if (c0 + TL_CHUNK < cnt) __syncthreads();   // the chunk's staging is reused by the next chunk
+        __syncthreads();   // every warp's keys are final
+        if (whole) {
+            uint32_t* out = gids + ((size_t)b << (2 * TL_BIN_LOG2));
+            for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS)
+                out[i] = (uint32_t)(keys[i] & 0xffffffffull);
+        } else {
+            for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS) {
+                const unsigned long long k = keys[i];
+                if (k) atomicMax(gkeys + (size_t)(Y0 + (i >> TL_BIN_LOG2)) * P.W + X0 + (i & 31), k);
+            }
+        }
     }
     // one atomic per CTA for the fragment count
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
-    if (threadIdx.x == 0) sfrags = 0;
-    __syncthreads();   // every warp's keys are final (and the extension keys' seeding, when no chunk ran)
     if (lane == 0 && frags) atomicAdd(&sfrags, frags);
     __syncthreads();
     if (threadIdx.x == 0 && sfrags) atomicAdd(&flags->fragments, sfrags);
-    uint32_t* out = gids + ((size_t)b << (2 * TL_BIN_LOG2));
-    for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS)
-        out[i] = (uint32_t)(keys[i] & 0xffffffffull);
 }
 
-// One CTA per 32x32 bin: each pixel with a winner (bin_raster_kernel's slots)
-// is resolved -- start depth, the winner's barycentrics, varyings, shading,
-// one colour and depth write; the bin's extension-key bit is cleared.
+// One CTA per 32x32 bin: each pixel with a winner is resolved -- start depth,
+// the winner's barycentrics, varyings, shading, one colour and depth write.
+// A bin raster in one work item left its winners in `gids`; one raster in
+// several left its keys in the global key buffer (read here, then zeroed).
+// The bin's extension-key bit is cleared.
 template <int FS, int FMT>
 __global__ void __launch_bounds__(TL_THREADS, 5) bin_resolve_kernel(
-    DrawParams P, sr_uniforms U, const float4* __restrict__ setup, const uint32_t* __restrict__ bin_off,
-    const uint32_t* __restrict__ gids, const uint32_t* __restrict__ vidx, const float* __restrict__ vary,
-    const uint32_t* __restrict__ tex, void* __restrict__ color, float* __restrict__ depth,
-    const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil, uint32_t* __restrict__ bitmap,
-    DeviceFlags* flags) {
+    DrawParams P, sr_uniforms U, const float4* __restrict__ setup, const uint32_t* __restrict__ chunk_off,
+    const uint32_t* __restrict__ gids, unsigned long long* __restrict__ gkeys, const uint32_t* __restrict__ vidx,
+    const float* __restrict__ vary, const uint32_t* __restrict__ tex, void* __restrict__ color,
+    float* __restrict__ depth, const uint8_t* __restrict__ stencil, uint32_t gate_with_stencil,
+    uint32_t* __restrict__ bitmap, DeviceFlags* flags) {
     if (flags->poison) return;
     const uint32_t b = blockIdx.x;
-    const uint32_t cnt = bin_off[b + 1] - bin_off[b];
+    const uint32_t n_chunks = chunk_off[b + 1] - chunk_off[b];
+    if (n_chunks == 0) return;
     const bool ext = (bitmap[b >> 5] >> (b & 31)) & 1u;
-    if (cnt == 0 && !ext) return;
     __syncthreads();   // every thread has read the bit before it is cleared
     if (ext && threadIdx.x == 0) atomicAnd(bitmap + (b >> 5), ~(1u << (b & 31)));
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
     const uint32_t X0 = (b % P.bins_x) << TL_BIN_LOG2, Y0 = (b / P.bins_x) << TL_BIN_LOG2;
     const uint32_t* in = gids + ((size_t)b << (2 * TL_BIN_LOG2));
     for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS) {
-        const uint32_t id = in[i];
-        if (!id) continue;   // also every slot outside the frame
         const uint32_t px = X0 + (i & 31), py = Y0 + (i >> TL_BIN_LOG2);
+        uint32_t id;
+        if (n_chunks == 1) {
+            id = in[i];   // 0 also for every slot outside the frame
+        } else {
+            if (px >= P.W || py >= P.H) continue;
+            const size_t gi = (size_t)py * P.W + px;
+            const unsigned long long k = gkeys[gi];
+            if (k) gkeys[gi] = 0;
+            id = (uint32_t)(k & 0xffffffffull);
+        }
+        if (!id) continue;
         const float d0 = P.has_depth ? depth[(size_t)py * P.W + px] : 0.0f;
         resolve_winner<FS, FMT>(P, U, px, py, id, d0, N, setup, vidx, vary, tex, color, depth, stencil,
                                 gate_with_stencil);
@@ -365,8 +441,8 @@ __global__ void __launch_bounds__(TL_THREADS, 5) bin_resolve_kernel(
 template <int FS>
 static void launch_bin_resolve_fs(const DrawParams& P, const sr_uniforms& U, const TiledArgs& A, uint32_t n_bins,
                                   cudaStream_t st) {
-#define SR_BR(FMT) bin_resolve_kernel<FS, FMT><<<n_bins, TL_THREADS, 0, st>>>(P, U, A.setup, A.bin_off, A.gids, \
-        A.vidx, A.vary, A.tex, A.color, A.depth, A.stencil, A.gate, A.bitmap, A.flags)
+#define SR_BR(FMT) bin_resolve_kernel<FS, FMT><<<n_bins, TL_THREADS, 0, st>>>(P, U, A.setup, A.chunk_off, A.gids, \
+        A.gkeys, A.vidx, A.vary, A.tex, A.color, A.depth, A.stencil, A.gate, A.bitmap, A.flags)
     if (P.color_format == SR_COLOR_RGBA32F) SR_BR(SR_COLOR_RGBA32F);
     else if (P.color_format == SR_COLOR_RGBA8) SR_BR(SR_COLOR_RGBA8);
     else SR_BR(SR_COLOR_NONE);
@@ -377,18 +453,18 @@ void ext_direct_launch(const DrawParams& P, const uint32_t* unsafe_list, const f
                        const float4* setup, unsigned long long* gkeys, uint32_t* bitmap, const uint8_t* stencil,
                        uint32_t gate, DeviceFlags* flags, cudaStream_t st);
 
-// launches: bin scan, scatter, extension keys, bin raster, bin resolve
+// launches: extension keys, bin scan, scatter, bin raster, bin resolve
 // (setup, with the bin counts, is launched by the caller)
 int launch_tiled(const DrawParams& P, const sr_uniforms& U, const TiledArgs& A, cudaStream_t st) {
     const uint32_t n_bins = P.bins_x * P.bins_y;
-    bin_scan_kernel<<<1, 1024, 0, st>>>(A.bin_counts, n_bins, A.bin_off, A.flags);
+    ext_direct_launch(P, A.unsafe_list, A.unsafe_rect, A.setup, A.gkeys, A.bitmap, A.stencil, A.gate, A.flags, st);
+    bin_scan_kernel<<<1, 1024, 0, st>>>(A.bin_counts, A.bitmap, n_bins, A.bin_off, A.chunk_off, A.entry_cap,
+                                        P.draw_id, A.flags);
     const uint32_t n_launch = P.n_raster_host ? P.n_raster_host : P.gen_tri_cap;
     bin_scatter_kernel<<<(n_launch + 255) / 256 ? (n_launch + 255) / 256 : 1, 256, 0, st>>>(
-        P.n_raster_host, n_launch, P.bins_x, A.binrect, A.bin_off, n_bins, A.cursor, A.entries, A.entry_cap,
-        P.draw_id, A.flags);
-    ext_direct_launch(P, A.unsafe_list, A.unsafe_rect, A.setup, A.gkeys, A.bitmap, A.stencil, A.gate, A.flags, st);
-    bin_raster_kernel<<<n_bins, TL_THREADS, 0, st>>>(P, A.setup, A.bin_off, A.entries, A.stencil, A.gate, A.gkeys,
-                                                     A.bitmap, A.gids, A.flags);
+        P.n_raster_host, n_launch, P.bins_x, A.binrect, A.bin_off, n_bins, A.cursor, A.entries, A.flags);
+    bin_raster_kernel<<<resident_grid(bin_raster_kernel, TL_THREADS, 6), TL_THREADS, 0, st>>>(
+        P, A.setup, A.bin_off, A.chunk_off, A.entries, A.stencil, A.gate, A.gkeys, A.bitmap, A.gids, A.flags);
     switch (P.fs) {
     case FS_BLINN_PHONG_DIR: launch_bin_resolve_fs<FS_BLINN_PHONG_DIR>(P, U, A, n_bins, st); break;
     case FS_TEXTURED_BLINN_PHONG: launch_bin_resolve_fs<FS_TEXTURED_BLINN_PHONG>(P, U, A, n_bins, st); break;

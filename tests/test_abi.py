@@ -121,8 +121,8 @@ def _header_text():
 
 
 def _rust_block():
-    txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    return "\n".join(b for b in re.findall(r"```rust\n(.*?)```", txt, flags=re.S) if "extern \"C\"" in b)
+    """The declarations of the Rust -sys crate (ffi/softrender-cuda-sys)."""
+    return open(os.path.join(ROOT, "ffi", "softrender-cuda-sys", "src", "lib.rs")).read()
 
 
 def test_rust_binding_functions_match_header():

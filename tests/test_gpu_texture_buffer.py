@@ -162,3 +162,24 @@ def test_unknown_sampler_modes_rejected(built_lib):
         mesh.free()
         if tex is not None:
             tex.free()
+
+
+def test_view_outlives_its_pipeline(built_lib, oracle_mod):
+    """A view holds a reference on the colour plane: the pipeline that drew it
+    can be destroyed first, and the view still samples its last frame (the
+    plane is freed with the view's last reference)."""
+    import softrender as sr
+    first = scenes.icosphere_scene(64, 48, color_format=A.SR_COLOR_RGBA8)
+    second = _second(A.SR_COLOR_RGBA8, A.SR_SAMPLE_BILINEAR, A.SR_SAMPLE_CLAMP)
+    pl, mesh, _ = sr.prepare_scene(first)
+    sr.submit_scene(pl, mesh, None, first)
+    assert pl.sync() == 0
+    view = sr.Texture.view(pl)
+    pl.destroy()
+    mesh.free()
+    got = _render_with(second, view)
+    view.free()
+    fb1, _, _ = oracle_mod.render(first)
+    second.texture = fb1.color.view(np.uint32).reshape(48, 64).copy()
+    fb2, _, _ = oracle_mod.render(second)
+    compare_frame(got, fb2)
