@@ -423,6 +423,43 @@ def run_frames():
     return out
 
 
+def profile_stress(args):
+    """The ordered stress frame at a quarter of its area, for ncu captures of
+    the ordered kernels on a case that holds about 1 GB on the device: the
+    same densities (4 tiny triangles per pixel, 4,096 large alpha triangles
+    over the frame, so about as many blended fragments per pixel) at
+    1024x1024, stencil Increment wrapping; --warmup untimed and --steps timed
+    frames, their device time printed."""
+    import torch
+    import softrender as sr
+    from softrender import scenes
+    sc = scenes.stress_scene(n_tiny=4194304, n_large=4096, size=1024)
+    pl, mesh, tex = sr.prepare_scene(sc)
+    stream = torch.cuda.Stream()
+    pl.set_stream(stream.cuda_stream)
+
+    def frame():
+        pl.clear(list(sc.clear_bytes()))
+        sr.submit_scene(pl, mesh, tex, sc)
+    for _ in range(args.warmup):
+        frame()
+        if pl.sync() != 0:
+            raise RuntimeError("stress frame failed")
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        frame()
+    e1.record(stream)
+    if pl.sync() != 0:
+        raise RuntimeError("stress frame failed")
+    st = pl.stats()
+    print(json.dumps({"profile": "stress_4M_tiny_4096_alpha_1024x1024", "ms_per_frame":
+                      round(e0.elapsed_time(e1) / max(1, args.steps), 3), "triangles": int(sc.n_tris),
+                      "fragments": int(st["fragments"]), "kernel_launches": int(st["kernel_launches"])}))
+    pl.destroy()
+    mesh.free()
+
+
 def profile_batched(args):
     """The batched leg's draws alone, for launch lists and ncu captures: the
     first N instances of the batched workload rendered as one batch with the
@@ -640,6 +677,10 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-draws measurement")
     ap.add_argument("--no-frames", action="store_true", help="skip the small and stress frame measurements")
     ap.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
+    ap.add_argument("--served-inflight", type=int, default=8, help="batches the serving loop keeps on the GPU")
+    ap.add_argument("--profile-stress", action="store_true",
+                    help="profiling aid: the ordered stress frame at 1024x1024 (--warmup untimed, --steps timed "
+                         "frames), its timing only")
     ap.add_argument("--profile-batched", type=int, default=0, metavar="N",
                     help="profiling aid: render the first N batched instances (--warmup untimed and --steps timed "
                          "batches, fixed launch configuration, no tuner, no graphs) and print their timing only")
@@ -647,6 +688,9 @@ def main():
     rank, world, local = dist_env()
     if args.profile_batched:
         profile_batched(args)
+        return
+    if args.profile_stress:
+        profile_stress(args)
         return
 
     if args.impl == "reference":
@@ -698,7 +742,7 @@ def main():
         if not args.no_batched:
             line["batched"] = run_batched()
         if not args.no_served:
-            line["served"] = run_served()
+            line["served"] = run_served(served_inflight=args.served_inflight)
         if not args.no_cpu_baseline:
             frame_s, sample, threads = cpu_frame_estimate(scene, every=1, tiles=510)
             line["cpu_baseline"] = {"value": round(n_tris / frame_s / 1e6, 5), "unit": "Mtris/s",
