@@ -723,12 +723,14 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
     StencilCountArgs S{nullptr, nullptr, nullptr};
     if (P.stencil_active && !P.mode_b) {
         size_t nd = (size_t)(W + 1) * (H + 1);
+        size_t nseg = (size_t)stencil_colseg_rows(H) * (W + 1);   // column-scan scratch after the array
         size_t nl = 3 * (size_t)(W + 1) + 3 * (size_t)(H + 1);
-        if ((rc = p->st_diff.ensure(nd)) || (rc = p->st_lines.ensure(nl)) || (rc = p->st_glob.ensure(16))) return rc;
+        if ((rc = p->st_diff.ensure(nd + nseg)) || (rc = p->st_lines.ensure(nl)) || (rc = p->st_glob.ensure(16)))
+            return rc;
         SR_CK(cudaMemsetAsync(p->st_diff.p, 0, nd * 4, st));
         SR_CK(cudaMemsetAsync(p->st_lines.p, 0, nl * 4, st));
         SR_CK(cudaMemsetAsync(p->st_glob.p, 0, 16 * 8, st));
-        S = StencilCountArgs{p->st_diff.p, p->st_lines.p, p->st_glob.p};
+        S = StencilCountArgs{p->st_diff.p, p->st_lines.p, p->st_glob.p, p->st_diff.p + nd};
     }
     VertexStore vs{p->clip4.p, p->scr4.p, p->vary.p, (uint32_t)vslots};
     const bool skip_v = outputs_kept();
@@ -785,7 +787,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
     if (ev) cudaEventRecord(ev[4], st);
     if (P.stencil_active && !P.mode_b) {
         launch_stencil_apply(P, S, p->stencil, p->flags, st);
-        launches += 5;
+        launches += 6;
     }
     if (ev) cudaEventRecord(ev[5], st);
     p->last_launches = launches;

@@ -74,22 +74,46 @@ __global__ void check_pairs_kernel(uint32_t n, const uint32_t* __restrict__ poff
 }
 
 // the bbox rectangle's pairs of primitive t at its slice (row-major bins)
-__global__ void prim_emit_kernel(DrawParams P, uint32_t n_host, uint32_t n_launch, const uint2* __restrict__ binrect,
-                                 const uint32_t* __restrict__ poff, uint32_t* __restrict__ keys,
-                                 uint32_t* __restrict__ vals, DeviceFlags* flags) {
+// (order within a primitive's slice is free: each bin occurs once in it).
+// Rectangles of more than 16 bins are written by the whole warp, one bin per
+// lane, so a few large primitives do not serialise their warps.
+__global__ void __launch_bounds__(256) prim_emit_kernel(DrawParams P, uint32_t n_host, uint32_t n_launch,
+                                                        const uint2* __restrict__ binrect,
+                                                        const uint32_t* __restrict__ poff, uint32_t* __restrict__ keys,
+                                                        uint32_t* __restrict__ vals, DeviceFlags* flags) {
+    if (flags->poison) return;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t n = n_host ? n_host : (uint32_t)flags->n_gen_tris;
-    if (flags->poison || t >= n || t >= n_launch) return;
-    const uint2 br = binrect[t];
-    if (br.x == RECT_EMPTY) return;
-    const uint32_t bx0 = br.x & 0xffffu, by0 = br.x >> 16, bx1 = br.y & 0xffffu, by1 = br.y >> 16;
-    uint32_t o = poff[t];
-    for (uint32_t by = by0; by <= by1; ++by)
-        for (uint32_t bx = bx0; bx <= bx1; ++bx) {
-            keys[o] = by * P.bins_x + bx;
-            vals[o] = t;
-            ++o;
+    const uint32_t lane = threadIdx.x & 31;
+    uint2 br = make_uint2(RECT_EMPTY, RECT_EMPTY);
+    if (t < n && t < n_launch) br = binrect[t];
+    uint32_t bx0 = 1, by0 = 1, bx1 = 0, by1 = 0, nb = 0, o = 0;
+    if (br.x != RECT_EMPTY) {
+        bx0 = br.x & 0xffffu; by0 = br.x >> 16; bx1 = br.y & 0xffffu; by1 = br.y >> 16;
+        nb = (bx1 - bx0 + 1) * (by1 - by0 + 1);
+        o = poff[t];
+    }
+    if (nb && nb <= 16) {
+        for (uint32_t by = by0; by <= by1; ++by)
+            for (uint32_t bx = bx0; bx <= bx1; ++bx) {
+                keys[o] = by * P.bins_x + bx;
+                vals[o] = t;
+                ++o;
+            }
+    }
+    uint32_t big = __ballot_sync(0xffffffffu, nb > 16);
+    while (big) {
+        const uint32_t src = __ffs(big) - 1;
+        big &= big - 1;
+        const uint32_t sx0 = __shfl_sync(0xffffffffu, bx0, src), sy0 = __shfl_sync(0xffffffffu, by0, src);
+        const uint32_t sw = __shfl_sync(0xffffffffu, bx1, src) - sx0 + 1;
+        const uint32_t sn = __shfl_sync(0xffffffffu, nb, src), so = __shfl_sync(0xffffffffu, o, src);
+        const uint32_t st = __shfl_sync(0xffffffffu, t, src);
+        for (uint32_t i = lane; i < sn; i += 32) {
+            keys[so + i] = (sy0 + i / sw) * P.bins_x + sx0 + i % sw;
+            vals[so + i] = st;
         }
+    }
 }
 
 // the extension pairs of unsafe primitives, after their rectangle's pairs

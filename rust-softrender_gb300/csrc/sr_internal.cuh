@@ -120,7 +120,11 @@ struct StencilCountArgs {
     int* diff2d;                 // (W+1) x (H+1) 2D difference array
     int* lines;                  // CX, CXa, CXb (W+1 each), CY, CYl, CYr (H+1 each)
     unsigned long long* globals; // N, L, R, A, B, LA, LB, RA, RB
+    int* colseg;                 // column scan scratch: stencil_colseg_rows(H) x (W+1)
 };
+// rows of the column-scan scratch: one per STENCIL_SEG rows of the (H+1)-row array
+constexpr uint32_t STENCIL_SEG = 32;
+inline uint32_t stencil_colseg_rows(uint32_t H) { return (H + 1 + STENCIL_SEG - 1) / STENCIL_SEG; }
 
 // m = ceil(2^32 / t), so that floor(p / t) == umulhi32(p, m) for p < 2^15 and
 // 2 <= t < 2^16 (m = (2^32 + e) / t with e < t: the excess p e / (t 2^32)

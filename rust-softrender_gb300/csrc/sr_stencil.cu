@@ -49,12 +49,29 @@ __global__ void __launch_bounds__(256) row_prefix_kernel(int* a, uint32_t cols) 
     }
 }
 
-// inclusive prefix down the columns, one thread per column
-__global__ void col_prefix_kernel(int* a, uint32_t rows, uint32_t cols) {
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+// Inclusive prefix down the columns of a (rows x cols) int array, in two
+// passes over segments of STENCIL_SEG rows: the first sums each (segment,
+// column), the second starts each (segment, column) from the sums of the
+// segments above it and walks its rows.  One thread per (segment, column),
+// consecutive threads on consecutive columns (coalesced rows).
+__global__ void __launch_bounds__(256) col_seg_sum_kernel(const int* __restrict__ a, uint32_t rows, uint32_t cols,
+                                                          int* __restrict__ seg) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x, g = blockIdx.y;
+    if (c >= cols) return;
+    const uint32_t r0 = g * STENCIL_SEG, r1 = min(r0 + STENCIL_SEG, rows);
+    int acc = 0;
+    for (uint32_t r = r0; r < r1; ++r) acc += a[(size_t)r * cols + c];
+    seg[(size_t)g * cols + c] = acc;
+}
+
+__global__ void __launch_bounds__(256) col_seg_apply_kernel(int* __restrict__ a, uint32_t rows, uint32_t cols,
+                                                            const int* __restrict__ seg) {
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x, g = blockIdx.y;
     if (c >= cols) return;
     int acc = 0;
-    for (uint32_t r = 0; r < rows; ++r) {
+    for (uint32_t k = 0; k < g; ++k) acc += seg[(size_t)k * cols + c];
+    const uint32_t r0 = g * STENCIL_SEG, r1 = min(r0 + STENCIL_SEG, rows);
+    for (uint32_t r = r0; r < r1; ++r) {
         acc += a[(size_t)r * cols + c];
         a[(size_t)r * cols + c] = acc;
     }
@@ -111,21 +128,16 @@ __global__ void __launch_bounds__(256) stencil_apply_kernel(DrawParams P, Stenci
     stencil[i] = (uint8_t)stencil_power(P.stencil_op, P.stencil_wrap, s0, P.sref, K);
 }
 
-__global__ void line_prefix_kernel(int* a, uint32_t len, uint32_t count) {
-    uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= count) return;
-    int* r = a + (size_t)k * len;
-    int acc = 0;
-    for (uint32_t j = 0; j < len; ++j) { acc += r[j]; r[j] = acc; }
-}
-
 void launch_stencil_apply(const DrawParams& P, const StencilCountArgs& S, uint8_t* stencil, DeviceFlags* flags,
                           cudaStream_t st) {
     uint32_t W = P.W, H = P.H;
     row_prefix_kernel<<<H + 1, 256, 0, st>>>(S.diff2d, W + 1);
-    col_prefix_kernel<<<(W + 1 + 255) / 256, 256, 0, st>>>(S.diff2d, H + 1, W + 1);
-    line_prefix_kernel<<<1, 32, 0, st>>>(S.lines, W + 1, 3);
-    line_prefix_kernel<<<1, 32, 0, st>>>(S.lines + 3 * (size_t)(W + 1), H + 1, 3);
+    const dim3 cg((W + 1 + 255) / 256, stencil_colseg_rows(H));
+    col_seg_sum_kernel<<<cg, 256, 0, st>>>(S.diff2d, H + 1, W + 1, S.colseg);
+    col_seg_apply_kernel<<<cg, 256, 0, st>>>(S.diff2d, H + 1, W + 1, S.colseg);
+    // the line counts: CX, CXa, CXb (W+1 each), then CY, CYl, CYr (H+1 each)
+    row_prefix_kernel<<<3, 256, 0, st>>>(S.lines, W + 1);
+    row_prefix_kernel<<<3, 256, 0, st>>>(S.lines + 3 * (size_t)(W + 1), H + 1);
     uint32_t n = W * H;
     stencil_apply_kernel<<<(n + 255) / 256, 256, 0, st>>>(P, S, stencil, flags);
 }
