@@ -724,8 +724,9 @@ def main():
             "triangles_generated_per_frame": int(r["stats"]["triangles_generated"]),
             "triangles_rasterised_per_frame": int(r["stats"]["triangles_raster"]),
             "roofline": {"bound": "hbm",
-                         "kernel": "opaque raster stage: raster_small_kernel<32> + raster_big_kernel + "
-                                   "ext_direct_kernel + resolve_kernel<textured_blinn_phong,RGBA8>",
+                         "kernel": "opaque raster stage over 32x32 bins: ext_direct_kernel + bin_scan_kernel + "
+                                   "bin_scatter_kernel + bin_raster_kernel + "
+                                   "bin_resolve_kernel<textured_blinn_phong,RGBA8>",
                          "achieved": round(ach, 2), "peak": peak, "unit": "GB/s",
                          "frac": round(ach / peak, 4), "traffic": traffic_from_profiles(),
                          "algorithmic_bytes": int(rb), "kernel_ms": round(r_ms, 4),

@@ -70,8 +70,16 @@ template <> struct PixelColor<SR_COLOR_RGBA32F> { float4 v; };
 template <> struct PixelColor<SR_COLOR_RGBA8> { uint32_t v; };
 template <> struct PixelColor<SR_COLOR_NONE> { uint32_t v; };
 
+// Resident blocks per SM asked of the compiler: the light shaders (vertex
+// colour, constant) fit 48 registers, so five 256-thread blocks run per SM
+// instead of four; the lit shaders keep the default.
+template <int FS>
+struct OrdOccupancy { static constexpr int BLOCKS = 1; };
+template <> struct OrdOccupancy<FS_VERTEX_COLOR> { static constexpr int BLOCKS = 5; };
+template <> struct OrdOccupancy<FS_CONSTANT_COLOR> { static constexpr int BLOCKS = 5; };
+
 template <int FS, int FMT, int BLEND>
-__global__ void __launch_bounds__(ORD_THREADS) raster_ordered_kernel(
+__global__ void __launch_bounds__(ORD_THREADS, OrdOccupancy<FS>::BLOCKS) raster_ordered_kernel(
     DrawParams P, sr_uniforms U, const float4* __restrict__ setup, const uint32_t* __restrict__ bin_off,
     const uint32_t* __restrict__ entries, const uint32_t* __restrict__ vidx, const float* __restrict__ vary,
     const uint32_t* __restrict__ tex, void* __restrict__ color, float* __restrict__ depth, uint8_t* __restrict__ stencil,
@@ -83,7 +91,9 @@ __global__ void __launch_bounds__(ORD_THREADS) raster_ordered_kernel(
     // it (entries with small bin rectangles), and the entries every pixel
     // tests (larger rectangles, unsafe primitives, exhaustive mode)
     __shared__ uint32_t pmask[ORD_THREADS][ORD_CHUNK / 32];
-    __shared__ uint32_t lmask[ORD_CHUNK / 32];
+    // (double-buffered by chunk parity: a warp that finished its pixels of one
+    // chunk clears the other buffer while slower warps still read this one)
+    __shared__ uint32_t lmask_buf[2][ORD_CHUNK / 32];
     // the chunk entries' vertex varyings, staged once per chunk
     constexpr int NKQ = FsTraits<FS>::NK > 0 ? (FsTraits<FS>::NK + 3) / 4 : 1;
     __shared__ float4 svary[FsTraits<FS>::NK > 0 ? ORD_CHUNK : 1][3][NKQ];
@@ -119,11 +129,13 @@ __global__ void __launch_bounds__(ORD_THREADS) raster_ordered_kernel(
     // the block streams its list once per pass; kp differs per pixel
     int max_kp = __syncthreads_or(kp > 1) ? (__syncthreads_or(kp > 2) ? 4 : 2) : 1;
     unsigned long long frags = 0;
+    uint32_t parity = 0;
     for (int pass = 0; pass < max_kp; ++pass) {
         const bool my_pass = pass < kp;
         const int ri = my_pass ? pass / cs.count : 0, ci = my_pass ? pass % cs.count : 0;
-        for (uint32_t cb = 0; cb < cnt; cb += ORD_CHUNK) {
+        for (uint32_t cb = 0; cb < cnt; cb += ORD_CHUNK, parity ^= 1u) {
             uint32_t m = min((uint32_t)ORD_CHUNK, cnt - cb);
+            uint32_t* lmask = lmask_buf[parity];
 #pragma unroll
             for (int w = 0; w < ORD_CHUNK / 32; ++w) pmask[threadIdx.x][w] = 0;   // this pixel's previous chunk is done
             if (threadIdx.x < ORD_CHUNK / 32) lmask[threadIdx.x] = 0;
@@ -175,58 +187,62 @@ __global__ void __launch_bounds__(ORD_THREADS) raster_ordered_kernel(
             }
             __syncthreads();
             if (!my_pass) continue;
-            uint32_t mk[ORD_CHUNK / 32];
+            // the chunk's entries for this pixel, in submission order: one mask
+            // word at a time in a register (the unrolled word loop keeps the
+            // masks out of local memory)
 #pragma unroll
-            for (int w = 0; w < ORD_CHUNK / 32; ++w) mk[w] = pmask[threadIdx.x][w] | lmask[w];
-            for (int w = 0; w < ORD_CHUNK / 32; ++w) while (mk[w]) {
-                const uint32_t e = (uint32_t)w * 32 + (uint32_t)(__ffs(mk[w]) - 1);
-                mk[w] &= mk[w] - 1;
-                float4 r2 = rec[e][2];
-                uint32_t fl = __float_as_uint(r2.z);
-                if (!(fl & REC_RASTER)) continue;
-                int4 bb = rbb[e];
-                bool in_b = bb.x <= (int)px && (int)px <= bb.z && bb.y <= (int)py && (int)py <= bb.w;
-                bool ev;
-                if (P.mode_b || (!in_b && (fl & REC_UNSAFE))) {
-                    ev = clamp_axis(bb.x, bb.z, px, (uint32_t)(cs.first + ci), P.tile_w, P.W - 1) &&
-                         clamp_axis(bb.y, bb.w, py, (uint32_t)(rs.first + ri), P.tile_h, P.H - 1);
-                } else {
-                    ev = in_b;
-                }
-                if (!ev) continue;
-                if (P.mode_b) {
-                    if (!stencil_test(P.stencil_test, s, P.sref)) continue;
-                    if (P.has_stencil) s = stencil_op(P.stencil_op, P.stencil_wrap, s, P.sref);
-                } else if (!gate) {
-                    continue;
-                }
-                Bary b = barycentric(rec[e][0], rec[e][1], r2, px, py);
-                if (!b.covered || !(b.z < 0.0f)) continue;
-                if (pass == kp - 1) ++frags;
-                if (P.has_depth && !(b.z >= d)) continue;
-                constexpr int NK = FsTraits<FS>::NK;
-                float kv[NK > 0 ? ((NK + 3) / 4) * 4 : 4];
-                if (NK > 0) {
-                    // (ka*u + kb*v) + kc*w, interpolate.rs:43-52
-#pragma unroll
-                    for (int q = 0; q < NKQ; ++q) {
-                        const float4 xa = svary[e][0][q], xb = svary[e][1][q], xc = svary[e][2][q];
-                        kv[4 * q + 0] = (xa.x * b.u + xb.x * b.v) + xc.x * b.w;
-                        kv[4 * q + 1] = (xa.y * b.u + xb.y * b.v) + xc.y * b.w;
-                        kv[4 * q + 2] = (xa.z * b.u + xb.z * b.v) + xc.z * b.w;
-                        kv[4 * q + 3] = (xa.w * b.u + xb.w * b.v) + xc.w * b.w;
+            for (int w = 0; w < ORD_CHUNK / 32; ++w) {
+                uint32_t mw = pmask[threadIdx.x][w] | lmask[w];
+                while (mw) {
+                    const uint32_t e = (uint32_t)w * 32 + (uint32_t)(__ffs(mw) - 1);
+                    mw &= mw - 1;
+                    float4 r2 = rec[e][2];
+                    uint32_t fl = __float_as_uint(r2.z);
+                    if (!(fl & REC_RASTER)) continue;
+                    int4 bb = rbb[e];
+                    bool in_b = bb.x <= (int)px && (int)px <= bb.z && bb.y <= (int)py && (int)py <= bb.w;
+                    bool ev;
+                    if (P.mode_b || (!in_b && (fl & REC_UNSAFE))) {
+                        ev = clamp_axis(bb.x, bb.z, px, (uint32_t)(cs.first + ci), P.tile_w, P.W - 1) &&
+                             clamp_axis(bb.y, bb.w, py, (uint32_t)(rs.first + ri), P.tile_h, P.H - 1);
+                    } else {
+                        ev = in_b;
                     }
+                    if (!ev) continue;
+                    if (P.mode_b) {
+                        if (!stencil_test(P.stencil_test, s, P.sref)) continue;
+                        if (P.has_stencil) s = stencil_op(P.stencil_op, P.stencil_wrap, s, P.sref);
+                    } else if (!gate) {
+                        continue;
+                    }
+                    Bary b = barycentric(rec[e][0], rec[e][1], r2, px, py);
+                    if (!b.covered || !(b.z < 0.0f)) continue;
+                    if (pass == kp - 1) ++frags;
+                    if (P.has_depth && !(b.z >= d)) continue;
+                    constexpr int NK = FsTraits<FS>::NK;
+                    float kv[NK > 0 ? ((NK + 3) / 4) * 4 : 4];
+                    if (NK > 0) {
+                        // (ka*u + kb*v) + kc*w, interpolate.rs:43-52
+    #pragma unroll
+                        for (int q = 0; q < NKQ; ++q) {
+                            const float4 xa = svary[e][0][q], xb = svary[e][1][q], xc = svary[e][2][q];
+                            kv[4 * q + 0] = (xa.x * b.u + xb.x * b.v) + xc.x * b.w;
+                            kv[4 * q + 1] = (xa.y * b.u + xb.y * b.v) + xc.y * b.w;
+                            kv[4 * q + 2] = (xa.z * b.u + xb.z * b.v) + xc.z * b.w;
+                            kv[4 * q + 3] = (xa.w * b.u + xb.w * b.v) + xc.w * b.w;
+                        }
+                    }
+                    sr_v4 col = shade_fs<FS>(U, kv, tex, P);
+                    if (FMT == SR_COLOR_RGBA32F) {
+                        float4 dst = *(float4*)&pc.v;
+                        if (BLEND == BLEND_OVER) col = sr_blend_over_f32(col, sr_make_v4(dst.x, dst.y, dst.z, dst.w));
+                        *(float4*)&pc.v = make_float4(col.x, col.y, col.z, col.w);
+                    } else if (FMT == SR_COLOR_RGBA8) {
+                        uint32_t src = sr_to_rgba8(col);
+                        *(uint32_t*)&pc.v = BLEND == BLEND_OVER ? sr_blend_over_rgba8(src, *(uint32_t*)&pc.v) : src;
+                    }
+                    if (P.has_depth) d = b.z;
                 }
-                sr_v4 col = shade_fs<FS>(U, kv, tex, P);
-                if (FMT == SR_COLOR_RGBA32F) {
-                    float4 dst = *(float4*)&pc.v;
-                    if (BLEND == BLEND_OVER) col = sr_blend_over_f32(col, sr_make_v4(dst.x, dst.y, dst.z, dst.w));
-                    *(float4*)&pc.v = make_float4(col.x, col.y, col.z, col.w);
-                } else if (FMT == SR_COLOR_RGBA8) {
-                    uint32_t src = sr_to_rgba8(col);
-                    *(uint32_t*)&pc.v = BLEND == BLEND_OVER ? sr_blend_over_rgba8(src, *(uint32_t*)&pc.v) : src;
-                }
-                if (P.has_depth) d = b.z;
             }
         }
     }
