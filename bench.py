@@ -368,7 +368,7 @@ def run_batched():
             "batched_ms": round(batched * 1e3, 3), "batched_mtris_per_s": round(tris / batched / 1e6, 1),
             "plain_ms": round(plain * 1e3, 3), "plain_mtris_per_s": round(tris / plain / 1e6, 1),
             "speedup_vs_plain": round(plain / batched, 2), "cuda_graph": True,
-            "launch_config": {"prims_per_warp": cfg[0], "big_threshold": cfg[1], "raster_ctas_per_sm": cfg[2]},
+            "launch_config": {"bins_per_primitive": cfg[0], "big_threshold": cfg[1], "raster_ctas_per_sm": cfg[2]},
             "kernel_launches_per_batch": int(st["kernel_launches"]), "target0_equals_plain": same,
             "timing": "host wall clock per 256 draws incl. sync, best of repetitions"}
 
@@ -463,8 +463,9 @@ def profile_stress(args):
 def profile_batched(args):
     """The batched leg's draws alone, for launch lists and ncu captures: the
     first N instances of the batched workload rendered as one batch with the
-    launch configuration the tuner picks for the full workload (32 primitives
-    per warp, large-primitive threshold 2048, 8 raster CTAs per SM)."""
+    launch configuration the tuner picks for the full workload (primitives of
+    up to 16 bins listed, large-primitive threshold 16384 pixels, 8 bin raster
+    CTAs per SM)."""
     import softrender as sr
     from softrender import scenes
     inst = scenes.batch_instances()[:args.profile_batched]
@@ -475,7 +476,7 @@ def profile_batched(args):
         m = sr.Mesh(sc.planes, sc.indices)
         T.append((pl, m, sr.draw_for_scene(sc, m), sc))
     b = sr.Batch(use_graphs=False, autotune=False)
-    b.set_config(32, 2048, 8)
+    b.set_config(16, 16384, 8)
     arr = b.items([(pl, d, sc.clear_bytes()) for pl, m, d, sc in T])
     for _ in range(args.warmup):
         if b.render_items(arr) != 0 or b.sync() != 0:
@@ -505,6 +506,14 @@ def _timed(fn):
 
 
 SWEEP_RATES = (2000.0, 5000.0, 10000.0, 20000.0, 40000.0)
+
+
+def served_wait(srv, ticket):
+    """Waits for one served request (30 s at most: a request takes
+    milliseconds, so a longer wait means the serving loop stopped)."""
+    st = srv.wait(ticket, 30000)
+    if st != 0:
+        raise RuntimeError("served request %d failed or timed out: status %d" % (ticket, st))
 
 
 def run_served(rate=2000.0, duration=10.0, sat_duration=1.0, sweep=SWEEP_RATES, served_inflight=8):
@@ -553,7 +562,7 @@ def run_served(rate=2000.0, duration=10.0, sat_duration=1.0, sweep=SWEEP_RATES, 
                 out.popleft()
         offered = n / max(1e-9, time.perf_counter() - t0)
         while out:
-            srv.wait(out[0], 600000)
+            served_wait(srv, out[0])
             srv.release(out.popleft())
         st = srv.stats()
         st["offered_rps"] = offered
@@ -562,11 +571,11 @@ def run_served(rate=2000.0, duration=10.0, sat_duration=1.0, sweep=SWEEP_RATES, 
     def warm(srv):
         for k in range(min(2000, len(built))):
             st, t = srv.submit(built[k])
-            srv.wait(t, 600000)
+            served_wait(srv, t)
             srv.release(t)
         ts = [srv.submit(built[k])[1] for k in range(min(2000, len(built)))]
         for t in ts:
-            srv.wait(t, 600000)
+            served_wait(srv, t)
             srv.release(t)
         srv.reset_stats()
 
@@ -605,7 +614,7 @@ def run_served(rate=2000.0, duration=10.0, sat_duration=1.0, sweep=SWEEP_RATES, 
             for k in range(min(1000, len(built))):
                 t0 = time.perf_counter()
                 st, t = srv.submit(built[k])
-                srv.wait(t, 600000)
+                served_wait(srv, t)
                 lat.append((time.perf_counter() - t0) * 1e3)
                 srv.release(t)
             res[name]["single_request_ms"] = {"mean": round(float(np.mean(lat)), 3),

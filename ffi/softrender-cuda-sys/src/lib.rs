@@ -154,8 +154,8 @@ extern "C" {
     pub fn sr_batch_destroy(b: *mut sr_batch) -> c_int;
     pub fn sr_batch_set_stream(b: *mut sr_batch, stream: *mut c_void) -> c_int;
     pub fn sr_batch_set_options(b: *mut sr_batch, use_graphs: c_int, autotune: c_int) -> c_int;
-    pub fn sr_batch_set_config(b: *mut sr_batch, prims_per_warp: u32, big_threshold: u32, ctas_per_sm: u32) -> c_int;
-    pub fn sr_batch_get_config(b: *mut sr_batch, prims_per_warp: *mut u32, big_threshold: *mut u32,
+    pub fn sr_batch_set_config(b: *mut sr_batch, bins_per_primitive: u32, big_threshold: u32, ctas_per_sm: u32) -> c_int;
+    pub fn sr_batch_get_config(b: *mut sr_batch, bins_per_primitive: *mut u32, big_threshold: *mut u32,
                                ctas_per_sm: *mut u32) -> c_int;
     pub fn sr_batch_render(b: *mut sr_batch, items: *const sr_batch_item, n: u32) -> c_int;
     pub fn sr_batch_sync(b: *mut sr_batch) -> c_int;

@@ -348,11 +348,13 @@ SR_API int sr_batch_set_stream(sr_batch* b, void* stream);
  * autotune: measure the launch configurations once per batch size class and
  * keep the fastest (default 1). */
 SR_API int sr_batch_set_options(sr_batch* b, int use_graphs, int autotune);
-/* Forces a launch configuration (primitives per warp 1..32, power of two;
- * large-primitive threshold in bbox pixels; raster CTAs per SM 1..8); all
+/* Forces a launch configuration: the 32x32 bins a primitive may span and
+ * still be reduced in its bins' shared-memory keys (1..32, power of two),
+ * the bbox pixels above which a primitive takes the large-primitive pass
+ * instead, and the bin raster's CTAs per SM (1..8, capped at what fits); all
  * zero returns to the tuned / default choice.  Results do not depend on it. */
-SR_API int sr_batch_set_config(sr_batch* b, uint32_t prims_per_warp, uint32_t big_threshold, uint32_t ctas_per_sm);
-SR_API int sr_batch_get_config(sr_batch* b, uint32_t* prims_per_warp, uint32_t* big_threshold, uint32_t* ctas_per_sm);
+SR_API int sr_batch_set_config(sr_batch* b, uint32_t bins_per_primitive, uint32_t big_threshold, uint32_t ctas_per_sm);
+SR_API int sr_batch_get_config(sr_batch* b, uint32_t* bins_per_primitive, uint32_t* big_threshold, uint32_t* ctas_per_sm);
 /* Enqueues the batch (returns after enqueue; waits first for this batch
  * object's previous batch, whose host table it reuses). */
 SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, uint32_t n);

@@ -32,6 +32,7 @@
 #include "sr_scan.cuh"
 #include "sr_setup.cuh"
 #include "sr_vertex.cuh"
+#include "sr_binraster.cuh"
 
 namespace sr {
 
@@ -154,11 +155,19 @@ __global__ void __launch_bounds__(128) batch_vertex_kernel(BTables T, float4* __
 
 // ---------------------------------------------------------------- setup
 // The opaque branch of setup_kernel (sr_setup.cu) per batch primitive g:
-// cull, det, bbox, safety class, record, bbox pixel count, unsafe list.
+// cull, det, bbox, safety class, record, bbox pixel count, unsafe list.  A
+// primitive whose bbox meets at most `bin_limit` of its target's 32x32 bins
+// and `big_threshold` pixels is listed in those bins (its bin rectangle, and
+// a count per (draw, bin)); a larger one goes to the large-primitive list,
+// whose chunks batch_raster_big_kernel reduces through the key buffer.
 __global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float4* __restrict__ scr4,
                                                           float4* __restrict__ setup,
                                                           unsigned long long* __restrict__ area,
-                                                          uint32_t* __restrict__ unsafe_list, DeviceFlags* flags) {
+                                                          uint32_t* __restrict__ unsafe_list, uint2* __restrict__ binrect,
+                                                          uint32_t* __restrict__ bin_cnt, uint32_t bin_limit,
+                                                          uint32_t big_threshold, uint32_t* __restrict__ big_list,
+                                                          uint32_t* __restrict__ big_base,
+                                                          unsigned long long* __restrict__ queues, DeviceFlags* flags) {
     const uint32_t n = *T.n;
     const uint32_t total = __ldg(T.tbase + n);
     const uint32_t stride = gridDim.x * blockDim.x;
@@ -171,6 +180,7 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float
         if (lane == 0) i0 = owner_of(T.tbase, n, gw);
         i0 = __shfl_sync(0xffffffffu, i0, 0);
         const uint32_t g = gw + lane;
+        uint32_t single_fb = 0xffffffffu;   // the (draw, bin) of a one-bin listed primitive
         if (g < total) {
             const uint32_t i = owner_from(T.tbase, n, i0, g);
             const BInst& I = T.inst[i];
@@ -191,6 +201,7 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float
             }
             culled = culled || bad;
             area[g] = 0;
+            binrect[g] = make_uint2(RECT_EMPTY, RECT_EMPTY);
             setup[4 * (size_t)g + 2] = make_float4(0.0f, 0.0f, __uint_as_float(0u), 0.0f);
             if (!culled) {
                 const float det = (y2 - y3) * (x1 - x3) + (x3 - x2) * (y1 - y3);
@@ -221,13 +232,42 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float
                                 ++n_unsafe;
                                 unsafe_list[atomicAdd(&flags->n_unsafe_list, 1ull)] = g;
                             }
-                            area[g] = b_in ? (unsigned long long)(qx1 - qx0 + 1) * (unsigned long long)(qy1 - qy0 + 1)
-                                           : 0ull;
+                            const unsigned long long at =
+                                b_in ? (unsigned long long)(qx1 - qx0 + 1) * (unsigned long long)(qy1 - qy0 + 1) : 0ull;
+                            area[g] = at;
+                            if (b_in) {
+                                const uint32_t rx0 = (uint32_t)qx0 >> TL_BIN_LOG2, rx1 = (uint32_t)qx1 >> TL_BIN_LOG2;
+                                const uint32_t ry0 = (uint32_t)qy0 >> TL_BIN_LOG2, ry1 = (uint32_t)qy1 >> TL_BIN_LOG2;
+                                const uint32_t nb = (rx1 - rx0 + 1) * (ry1 - ry0 + 1);
+                                if (nb <= bin_limit && at <= big_threshold) {
+                                    binrect[g] = make_uint2(rx0 | (ry0 << 16), rx1 | (ry1 << 16));
+                                    const uint32_t fb0 = __ldg(T.bbase + i);
+                                    if (nb == 1) {
+                                        single_fb = fb0 + ry0 * P.bins_x + rx0;   // counted per warp below
+                                    } else {
+                                        for (uint32_t by = ry0; by <= ry1; ++by)
+                                            for (uint32_t bx = rx0; bx <= rx1; ++bx)
+                                                atomicAdd(bin_cnt + fb0 + by * P.bins_x + bx, 1u);
+                                    }
+                                } else {
+                                    // one packed counter keeps list order and chunk offsets consistent
+                                    const unsigned long long nch = (at + BIG_CHUNK - 1) / BIG_CHUNK;
+                                    const unsigned long long old = atomicAdd(queues + Q_BIG, (1ull << 40) | nch);
+                                    big_list[old >> 40] = g;
+                                    big_base[old >> 40] = (uint32_t)(old & ((1ull << 40) - 1));
+                                    // the count has 24 bits: past them the batch reports SR_EOVERFLOW
+                                    if ((old >> 40) >= (1ull << 24) - 1) atomicOr(&flags->overflow_bits, 1u);
+                                }
+                            }
                         }
                     }
                 }
             }
         }
+        // one atomic per warp and bin for the one-bin primitives (a mesh's
+        // consecutive primitives mostly share bins)
+        const uint32_t peers = __match_any_sync(0xffffffffu, single_fb);
+        if (single_fb != 0xffffffffu && lane == __ffs(peers) - 1) atomicAdd(bin_cnt + single_fb, (uint32_t)__popc(peers));
     }
     for (int o = 16; o > 0; o >>= 1) {
         n_raster += __shfl_down_sync(0xffffffffu, n_raster, o);
@@ -241,134 +281,151 @@ __global__ void __launch_bounds__(256) batch_setup_kernel(BTables T, const float
     }
 }
 
-// ---------------------------------------------------------------- raster
-// raster_small_kernel (sr_opaque.cu) over batch primitives: each warp takes G
-// consecutive batch primitives, which may belong to different draws; every
-// staged primitive carries its draw index.
-template <uint32_t G>
-// 6 resident CTAs per SM (at most 40 registers, a few bytes spilled) measured
-// faster than the unconstrained 46 registers (5 CTAs) and than 32 (8 CTAs)
-__global__ void __launch_bounds__(256, 6) batch_raster_small_kernel(BTables T, const float4* __restrict__ setup,
-                                                                 const unsigned long long* __restrict__ area,
-                                                                 uint32_t big_threshold,
-                                                                 uint32_t* __restrict__ big_list,
-                                                                 uint32_t* __restrict__ big_base,
-                                                                 unsigned long long* __restrict__ tlist,
-                                                                 unsigned long long* __restrict__ queues,
-                                                                 DeviceFlags* flags) {
-    // per staged primitive: record, bbox origin and width, and the scalars of
-    // its draw's target (so the per-pixel loop reads no global tables)
-    struct Slot {
-        uint32_t wh;        // W | H << 16
-        uint32_t tiles;     // tile_w | tile_h << 16
-        uint32_t mx, my;
-        uint32_t n_depth;   // N | has_depth << 31
-        uint32_t t;         // primitive index within the draw
-        unsigned long long* gkeys;
-    };
-    __shared__ float4 srec[8][32][3];
-    __shared__ uint32_t sxy[8][32];
-    __shared__ uint32_t sw[8][32];
-    __shared__ uint32_t sst[8][32];     // first item of the staged primitive
-    __shared__ Slot sslot[8][32];
-    __shared__ unsigned long long smag[8][32];
+// ---------------------------------------------------------------- bins
+// The listed primitives are reduced per (draw, 32x32 bin) as in sr_render's
+// binned path (sr_tiled.cu, sr_binraster.cuh): the draws' bins are numbered
+// consecutively (bin j of draw i is T.bbase[i] + j), each bin's count becomes
+// its list offset and its number of work items (chunks of TL_CHUNK
+// primitives) in one scan of packed u64 values (entries << 32 | items), the
+// primitives scatter into the lists, and persistent CTAs reduce the work
+// items in shared memory.  The winners land in each target's per-pixel key
+// buffer, where the large primitives (batch_raster_big_kernel) and the
+// extension fragments (batch_ext_kernel) already left theirs, and every bin
+// with keys is marked in the target's bitmap, so batch_collect_kernel,
+// batch_clear_kernel and batch_resolve_kernel work on them unchanged.
+
+// Packed count of bin j (< cap): entries << 32 | work items; zero past the
+// batch's bins.  The counts are reset for the next batch here (and the
+// slot cursors by the bin raster), so a batch needs no clearing launches.
+__global__ void __launch_bounds__(256) batch_bin_pack_kernel(BTables T, uint32_t cap, uint32_t* __restrict__ bin_cnt,
+                                                             unsigned long long* __restrict__ packed) {
+    const uint32_t total = __ldg(T.bbase + *T.n);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < cap; j += gridDim.x * blockDim.x) {
+        unsigned long long v = 0;
+        if (j < total) {
+            const uint32_t e = bin_cnt[j];
+            if (e) bin_cnt[j] = 0;
+            v = ((unsigned long long)e << 32) | ((e + TL_CHUNK - 1) / TL_CHUNK);
+        }
+        packed[j] = v;
+    }
+}
+
+// Every listed primitive into the list of each bin of its rectangle (draw-
+// local primitive numbers; order within a list is free).  `cursor` (cap
+// entries, zero) counts the slots taken per bin.
+__global__ void __launch_bounds__(256) batch_bin_scatter_kernel(BTables T, const uint2* __restrict__ binrect,
+                                                                const unsigned long long* __restrict__ off,
+                                                                uint32_t* __restrict__ cursor,
+                                                                uint32_t* __restrict__ entries, uint64_t entry_cap,
+                                                                DeviceFlags* flags) {
     const uint32_t n = *T.n;
     const uint32_t total = __ldg(T.tbase + n);
-    const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t gw = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); gw < total; gw += gridDim.x * blockDim.x) {
+        uint32_t i0 = 0;
+        if (lane == 0) i0 = owner_of(T.tbase, n, gw);
+        i0 = __shfl_sync(0xffffffffu, i0, 0);
+        const uint32_t g = gw + lane;
+        uint32_t single = 0xffffffffu, t = 0;
+        uint2 br = make_uint2(RECT_EMPTY, RECT_EMPTY);
+        uint32_t fb0 = 0, bins_x = 0;
+        if (g < total) {
+            br = binrect[g];
+            if (br.x != RECT_EMPTY) {
+                const uint32_t i = owner_from(T.tbase, n, i0, g);
+                fb0 = __ldg(T.bbase + i);
+                bins_x = T.inst[i].P.bins_x;
+                t = g - __ldg(T.tbase + i);
+                if (br.x == br.y) single = fb0 + (br.x >> 16) * bins_x + (br.x & 0xffffu);
+            }
+        }
+        const uint32_t peers = __match_any_sync(0xffffffffu, single);
+        const uint32_t leader = __ffs(peers) - 1;
+        uint32_t base = 0;
+        if (single != 0xffffffffu && lane == leader) base = atomicAdd(cursor + single, (uint32_t)__popc(peers));
+        base = __shfl_sync(0xffffffffu, base, leader);
+        // (the lists were sized on the host; a slot past them is reported
+        // as SR_EOVERFLOW rather than written)
+        if (single != 0xffffffffu) {
+            const uint64_t k = (off[single] >> 32) + base + __popc(peers & ((1u << lane) - 1u));
+            if (k < entry_cap) entries[k] = t;
+            else atomicOr(&flags->overflow_bits, 1u);
+        } else if (br.x != RECT_EMPTY) {
+            for (uint32_t by = br.x >> 16; by <= (br.y >> 16); ++by)
+                for (uint32_t bx = br.x & 0xffffu; bx <= (br.y & 0xffffu); ++bx) {
+                    const uint32_t fb = fb0 + by * bins_x + bx;
+                    const uint64_t k = (off[fb] >> 32) + atomicAdd(cursor + fb, 1u);
+                    if (k < entry_cap) entries[k] = t;
+                    else atomicOr(&flags->overflow_bits, 1u);
+                }
+        }
+    }
+}
+
+// Persistent CTAs take work items from a counter: item -> (draw, bin) by
+// binary search over the scanned item offsets, then bin_item reduces it.  A
+// bin in one item starts from the keys already in the key buffer when its
+// bitmap bit says so, and stores its non-zero keys there; a bin in several
+// items merges them with atomicMax.  Each item marks its bin in the bitmap.
+__global__ void __launch_bounds__(TL_THREADS, 6) batch_bin_raster_kernel(
+    BTables T, const float4* __restrict__ setup, const unsigned long long* __restrict__ off, uint32_t cap,
+    const uint32_t* __restrict__ entries, uint64_t entry_cap, uint32_t* __restrict__ cursor, DeviceFlags* flags) {
+    __shared__ BinSmem sm;
+    __shared__ DrawParams sP;
+    __shared__ uint32_t sitem, sbin, sdraw;
+    __shared__ bool sext;
+    __shared__ unsigned long long sfrags;
+    const uint32_t n = *T.n;
+    const uint32_t n_items = (uint32_t)(off[cap] & 0xffffffffull);
+    if (threadIdx.x == 0) sfrags = 0;
     unsigned long long frags = 0;
     for (;;) {
-        // dynamic work queue: a warp takes the next G batch primitives
-        uint32_t t0 = 0, i0 = 0;
-        if (lane == 0) {
-            t0 = (uint32_t)min(atomicAdd(&flags->work_raster, (unsigned long long)G), 0xffffffffull);
-            if (t0 < total) i0 = owner_of(T.tbase, n, t0);
-        }
-        t0 = __shfl_sync(0xffffffffu, t0, 0);
-        if (t0 >= total) break;
-        i0 = __shfl_sync(0xffffffffu, i0, 0);
-        const uint32_t g = t0 + lane;
-        // items: horizontal pairs of bbox pixels, ceil(w / 2) per bbox row
-        uint32_t a = 0, i = 0, x0 = 0, y0 = 0, x1 = 0, y1 = 0;
-        if (lane < G && g < total) {
-            const unsigned long long at = area[g];
-            if (at > big_threshold) {
-                // one packed counter keeps list order and chunk offsets consistent
-                const unsigned long long nch = (at + BIG_CHUNK - 1) / BIG_CHUNK;
-                const unsigned long long old = atomicAdd(queues + Q_BIG, (1ull << 40) | nch);
-                big_list[old >> 40] = g;
-                big_base[old >> 40] = (uint32_t)(old & ((1ull << 40) - 1));
-            } else if (at) {
-                i = owner_from(T.tbase, n, i0, g);
-                const float4 r3 = __ldg(setup + 4 * (size_t)g + 3);
-                x0 = (uint32_t)max(__float_as_int(r3.x), 0);
-                y0 = (uint32_t)max(__float_as_int(r3.y), 0);
-                x1 = (uint32_t)min(__float_as_int(r3.z), (int)T.inst[i].P.W - 1);
-                y1 = (uint32_t)min(__float_as_int(r3.w), (int)T.inst[i].P.H - 1);
-                a = (y1 - y0 + 1) * ((x1 - x0 + 2) >> 1);
+        if (threadIdx.x == 0) {
+            const uint32_t item = (uint32_t)min(atomicAdd(&flags->work_raster, 1ull), 0xffffffffull);
+            sitem = item;
+            if (item < n_items) {
+                // the item's bin: the last j whose first item is <= item
+                uint32_t lo = 0, hi = cap;
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if ((uint32_t)(off[mid] & 0xffffffffull) <= item) lo = mid; else hi = mid;
+                }
+                sbin = lo;
+                sdraw = owner_of(T.bbase, n, lo);
             }
         }
-        const uint32_t inc = warp_inclusive_scan(a);
-        const uint32_t tot = __shfl_sync(0xffffffffu, inc, 31);
-        const uint32_t ex = inc - a;
-        const uint32_t nonempty = __ballot_sync(0xffffffffu, a != 0);
-        if (a) {
-            // compacted slot: the rank of this primitive among the non-empty ones
-            const uint32_t lane_c = __popc(nonempty & ((1u << lane) - 1u));
-            const BInst& I = T.inst[i];
-            const float4* r = setup + 4 * (size_t)g;
-            srec[wl][lane_c][0] = __ldg(r);
-            srec[wl][lane_c][1] = __ldg(r + 1);
-            srec[wl][lane_c][2] = __ldg(r + 2);
-            const uint32_t W = I.P.W, H = I.P.H;
-            const uint32_t w = x1 - x0 + 1, wp = (w + 1) >> 1;
-            mark_rect(I.bitmap, (W + 31) >> 5, x0, y0, x1, y1);
-            const uint32_t sb = seam_bits(x0, y0, x1, y1, I.P);
-            sxy[wl][lane_c] = x0 | (y0 << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
-            sw[wl][lane_c] = wp | (w << 16);
-            Slot S;
-            S.wh = W | (H << 16);
-            S.tiles = I.P.tile_w | (I.P.tile_h << 16);
-            S.mx = I.mx;
-            S.my = I.my;
-            S.n_depth = I.P.n_raster_host | (I.P.has_depth ? 0x80000000u : 0u);
-            S.t = g - I.tbase;
-            S.gkeys = I.gkeys;
-            sslot[wl][lane_c] = S;
-            sst[wl][lane_c] = ex;
-            smag[wl][lane_c] = ((1ull << 32) + wp - 1) / wp;
+        __syncthreads();   // the previous item is done with the shared arrays
+        const uint32_t item = sitem;
+        if (item >= n_items) break;
+        const uint32_t fb = sbin, i = sdraw;
+        const BInst& I = T.inst[i];
+        for (uint32_t k = threadIdx.x; k < sizeof(DrawParams) / 4; k += blockDim.x)
+            reinterpret_cast<uint32_t*>(&sP)[k] = reinterpret_cast<const uint32_t*>(&I.P)[k];
+        const uint32_t b = fb - __ldg(T.bbase + i);
+        const unsigned long long o0 = off[fb], o1 = off[fb + 1];
+        const uint32_t e_bin = (uint32_t)(o0 >> 32), cnt_bin = (uint32_t)(o1 >> 32) - e_bin;
+        const uint32_t c_first = (uint32_t)(o0 & 0xffffffffull), n_chunks = (uint32_t)(o1 & 0xffffffffull) - c_first;
+        const uint32_t c0 = (item - c_first) * TL_CHUNK;
+        uint32_t cnt = cnt_bin > c0 ? min(cnt_bin - c0, TL_CHUNK) : 0u;
+        if ((uint64_t)e_bin + c0 + cnt > entry_cap) cnt = 0;   // flagged by the scatter
+        const bool whole = n_chunks == 1;
+        if (threadIdx.x == 0) {
+            if (c0 == 0) cursor[fb] = 0;   // the bin's scatter is done: reset for the next batch
+            const uint32_t word = I.bitmap[b >> 5], bit = 1u << (b & 31);
+            sext = (word & bit) != 0;   // keys of large primitives or extension fragments
+            if (!(word & bit)) atomicOr(I.bitmap + (b >> 5), bit);
         }
-        __syncwarp();
-        const uint32_t le = (2u << lane) - 1u;   // lanes 0..lane
-        uint32_t before = 0;                     // primitive starts before the window
-        for (uint32_t base = 0; base < tot; base += 32) {
-            const uint32_t q = base + lane;
-            const uint32_t rel = ex - base;
-            const uint32_t starts = __reduce_or_sync(0xffffffffu, (a && rel < 32u) ? (1u << rel) : 0u);
-            const uint32_t lo = before + __popc(starts & le) - 1u;
-            before += __popc(starts);
-            if (q < tot) {
-                const uint32_t local = q - sst[wl][lo];
-                const uint32_t wpw = sw[wl][lo], wp = wpw & 0xffffu;
-                const uint32_t row = (uint32_t)(((unsigned long long)local * smag[wl][lo]) >> 32);  // local / wp
-                const uint32_t col = 2 * (local - row * wp);
-                const uint32_t xy = sxy[wl][lo];
-                const Slot& S = sslot[wl][lo];
-                const float4 r0 = srec[wl][lo][0], r1 = srec[wl][lo][1], r2 = srec[wl][lo][2];
-                const uint32_t px = (xy & 0x7fffu) + col, py = ((xy >> 16) & 0x7fffu) + row;
-                const uint32_t seams = ((xy >> 15) & 1u) | ((xy >> 30) & 2u);
-                frag_emit(S.wh & 0xffffu, S.wh >> 16, S.tiles & 0xffffu, S.tiles >> 16, S.mx, S.my, seams,
-                          (S.n_depth >> 31) != 0, r0, r1, r2, S.t, px, py, S.n_depth & 0x7fffffffu, S.gkeys,
-                          nullptr, 0u, 0u, 0u, frags);
-                if (col + 1 < (wpw >> 16))
-                    frag_emit(S.wh & 0xffffu, S.wh >> 16, S.tiles & 0xffffu, S.tiles >> 16, S.mx, S.my, seams,
-                              (S.n_depth >> 31) != 0, r0, r1, r2, S.t, px + 1, py, S.n_depth & 0x7fffffffu, S.gkeys,
-                              nullptr, 0u, 0u, 0u, frags);
-            }
-        }
-        __syncwarp();
+        __syncthreads();
+        const bool seed = whole && sext;
+        const uint32_t X0 = (b % sP.bins_x) << TL_BIN_LOG2, Y0 = (b / sP.bins_x) << TL_BIN_LOG2;
+        bin_item(sm, sP, X0, Y0, setup + 4 * (size_t)I.tbase, entries + e_bin + c0, cnt, sP.n_raster_host, nullptr,
+                 0u, whole, seed, I.gkeys, nullptr, frags);
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
-    if (lane == 0 && frags) atomicAdd(&flags->fragments, frags);
+    if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&sfrags, frags);
+    __syncthreads();
+    if (threadIdx.x == 0 && sfrags) atomicAdd(&flags->fragments, sfrags);
 }
 
 // raster_big_kernel over the batch's large primitives, split into chunks of
@@ -527,9 +584,9 @@ using namespace sr;
 namespace {
 
 struct BatchConfig {
-    uint32_t G = 32;          // primitives per warp in the raster pass
-    uint32_t big = RG_BIG;    // bbox pixels above which a primitive gets a whole block
-    uint32_t ctas = 8;        // raster CTAs per SM
+    uint32_t G = 8;           // bins a listed primitive may cover (more: the large-primitive pass)
+    uint32_t big = 8192;      // bbox pixels above which a primitive takes the large-primitive pass
+    uint32_t ctas = 8;        // bin raster CTAs per SM (at most the kernel's resident count)
     bool operator==(const BatchConfig& o) const { return G == o.G && big == o.big && ctas == o.ctas; }
 };
 
@@ -586,6 +643,11 @@ struct sr_batch {
     DevBuf<unsigned long long> area;
     DevBuf<uint32_t> big_list, big_base, unsafe_list;
     DevBuf<unsigned long long> tlist;       // touched (draw, block) list
+    DevBuf<uint2> binrect;                  // per primitive: its bin rectangle, or RECT_EMPTY
+    DevBuf<uint32_t> bin_cnt, bin_cursor;   // per (draw, bin): listed primitives, slots taken
+    DevBuf<unsigned long long> bin_pack, bin_off, bin_tmp;   // packed counts, their exclusive scan, scan scratch
+    DevBuf<uint32_t> entries;               // the bins' primitive lists
+    uint32_t bin_cap = 0;                   // (draw, bin) capacity the graphs were recorded for
     DeviceFlags* flags = nullptr;
     DeviceFlags* hflags = nullptr;
     unsigned long long* queues = nullptr;   // work-queue counters of the resolve launches
@@ -595,7 +657,7 @@ struct sr_batch {
     bool use_graphs = true, autotune = true;
     BatchConfig forced{0, 0, 0};
     std::map<uint64_t, BatchConfig> tuned;
-    struct Graph { uint32_t NB; BatchConfig cfg; uint64_t gen; uint32_t combos; cudaGraphExec_t exec; };
+    struct Graph { uint32_t NB; BatchConfig cfg; uint64_t gen; uint32_t combos; uint32_t bin_cap; cudaGraphExec_t exec; };
     std::vector<Graph> graphs;
     uint64_t gen = 1;            // bumped whenever a device buffer moves
     BatchConfig last_cfg;
@@ -642,23 +704,21 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     cudaMemsetAsync(b->flags, 0, sizeof(DeviceFlags), st);
     cudaMemsetAsync(b->queues, 0, N_QUEUES * sizeof(unsigned long long), st);
     batch_vertex_kernel<<<resident_grid(batch_vertex_kernel, 128, 16), 128, 0, st>>>(T, b->scr4.p, b->vary.p);
-    batch_setup_kernel<<<resident_grid(batch_setup_kernel, 256, 8), 256, 0, st>>>(T, b->scr4.p, b->setup.p, b->area.p,
-                                                                                b->unsafe_list.p, b->flags);
-#define SR_BRS(g) batch_raster_small_kernel<g><<<resident_grid(batch_raster_small_kernel<g>, 256, (int)c.ctas), 256, 0, st>>>( \
-        T, b->setup.p, b->area.p, c.big, b->big_list.p, b->big_base.p, b->tlist.p, b->queues, b->flags)
-    switch (c.G) {
-    case 1: SR_BRS(1); break;
-    case 2: SR_BRS(2); break;
-    case 4: SR_BRS(4); break;
-    case 8: SR_BRS(8); break;
-    case 16: SR_BRS(16); break;
-    default: SR_BRS(32); break;
-    }
-#undef SR_BRS
+    const uint32_t cap = b->bin_cap;
+    batch_setup_kernel<<<resident_grid(batch_setup_kernel, 256, 8), 256, 0, st>>>(
+        T, b->scr4.p, b->setup.p, b->area.p, b->unsafe_list.p, b->binrect.p, b->bin_cnt.p, c.G, c.big, b->big_list.p,
+        b->big_base.p, b->queues, b->flags);
     batch_raster_big_kernel<<<resident_grid(batch_raster_big_kernel, 256, 8), 256, 0, st>>>(
         T, b->setup.p, b->area.p, b->big_list.p, b->big_base.p, b->tlist.p, b->queues, b->flags);
     batch_ext_kernel<<<resident_grid(batch_ext_kernel, 256, 4), 256, 0, st>>>(T, b->setup.p, b->unsafe_list.p,
                                                                              b->tlist.p, b->queues, b->flags);
+    batch_bin_pack_kernel<<<resident_grid(batch_bin_pack_kernel, 256, 8), 256, 0, st>>>(T, cap, b->bin_cnt.p,
+                                                                                        b->bin_pack.p);
+    exclusive_scan<unsigned long long>(b->bin_pack.p, cap, b->bin_off.p, b->bin_tmp.p, st);
+    batch_bin_scatter_kernel<<<resident_grid(batch_bin_scatter_kernel, 256, 8), 256, 0, st>>>(
+        T, b->binrect.p, b->bin_off.p, b->bin_cursor.p, b->entries.p, b->entries.cap, b->flags);
+    batch_bin_raster_kernel<<<resident_grid(batch_bin_raster_kernel, TL_THREADS, (int)c.ctas), TL_THREADS, 0, st>>>(
+        T, b->setup.p, b->bin_off.p, cap, b->entries.p, b->entries.cap, b->bin_cursor.p, b->flags);
     batch_collect_kernel<<<resident_grid(batch_collect_kernel, 256, 8), 256, 0, st>>>(T, b->tlist.p, b->queues);
     batch_clear_kernel<<<resident_grid(batch_clear_kernel, 256, 8), 256, 0, st>>>(T);
     for (int fs = 0; fs < FS_COUNT; ++fs)
@@ -691,7 +751,8 @@ int launch_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     }
     cudaGraphExec_t exec = nullptr;
     for (auto& g : b->graphs)
-        if (g.NB == NB && g.cfg == c && g.gen == b->gen && g.combos == b->combos) exec = g.exec;
+        if (g.NB == NB && g.cfg == c && g.gen == b->gen && g.combos == b->combos && g.bin_cap == b->bin_cap)
+            exec = g.exec;
     if (!exec) {
         cudaGraph_t graph = nullptr;
         SR_CK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -702,7 +763,7 @@ int launch_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
         cudaGraphDestroy(graph);
         if (e != cudaSuccess) { last_cuda_error() = e; return SR_ECUDA; }
         if (b->graphs.size() >= 32) { cudaGraphExecDestroy(b->graphs.front().exec); b->graphs.erase(b->graphs.begin()); }
-        b->graphs.push_back({NB, c, b->gen, b->combos, exec});
+        b->graphs.push_back({NB, c, b->gen, b->combos, b->bin_cap, exec});
     }
     SR_CK(cudaGraphLaunch(exec, b->stream));
     return SR_OK;
@@ -710,16 +771,16 @@ int launch_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
 
 // Measures every candidate configuration on this batch (rendering it is
 // idempotent: same inputs, same winners) and returns the fastest.
-BatchConfig tune(sr_batch* b, uint32_t NB) {
-    static const uint32_t Gs[] = {4, 8, 16, 32};
-    static const uint32_t bigs[] = {512, 2048, 8192};
+BatchConfig tune(sr_batch* b, uint32_t NB, uint32_t g_max) {
+    static const uint32_t Gs[] = {4, 16, 32};
+    static const uint32_t bigs[] = {4096, 16384, 65536};
     static const uint32_t ctas[] = {4, 8};
     BatchConfig best;
     float best_ms = 1e30f;
     for (uint32_t g : Gs)
         for (uint32_t bg : bigs)
             for (uint32_t ct : ctas) {
-                BatchConfig c{g, bg, ct};
+                BatchConfig c{std::min(g, g_max), bg, ct};
                 enqueue_batch(b, NB, c);   // warm
                 cudaEventRecord(b->ev0, b->stream);
                 enqueue_batch(b, NB, c);
@@ -869,8 +930,34 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         (rc = grow(b, b->vary, (slots + 4) * VSTRIDE)) || (rc = grow(b, b->setup, 4 * (tris + 1))) ||
         (rc = grow(b, b->area, tris + 1)) || (rc = grow(b, b->big_list, tris + 1)) ||
         (rc = grow(b, b->big_base, tris + 1)) || (rc = grow(b, b->unsafe_list, tris + 1)) ||
-        (rc = grow(b, b->tlist, blocks + 1)))
+        (rc = grow(b, b->tlist, blocks + 1)) || (rc = grow(b, b->binrect, tris + 1)))
         return rc;
+    // (draw, bin) buffers for a power-of-two capacity of bins (the graphs are
+    // recorded per capacity); the lists hold up to `bins per listed
+    // primitive` entries per primitive, so they are sized for the largest
+    // value this batch may use (the tuner's candidates go up to 32)
+    uint32_t bin_cap = 1024;
+    while (bin_cap < blocks) bin_cap <<= 1;
+    BatchConfig pre;
+    const uint64_t cls = ((uint64_t)bucket_of(n) << 40) | ((uint64_t)log2_floor(tris + 1) << 20) | log2_floor(px + 1);
+    const auto tuned_it = b->tuned.find(cls);
+    uint32_t g_max = pre.G;
+    if (b->forced.G) g_max = b->forced.G;
+    else if (tuned_it != b->tuned.end()) g_max = tuned_it->second.G;
+    else if (b->autotune) g_max = 32;
+    while (g_max > 1 && (uint64_t)g_max * tris >= 0xffffffffull) g_max >>= 1;
+    const size_t cnt_cap0 = b->bin_cnt.cap, cur_cap0 = b->bin_cursor.cap;
+    if ((rc = grow(b, b->bin_cnt, bin_cap)) || (rc = grow(b, b->bin_cursor, bin_cap)) ||
+        (rc = grow(b, b->bin_pack, bin_cap)) || (rc = grow(b, b->bin_off, (size_t)bin_cap + 1)) ||
+        (rc = grow(b, b->bin_tmp, (size_t)scan_blocks(bin_cap) + 2)) ||
+        (rc = grow(b, b->entries, (size_t)g_max * tris + 1)))
+        return rc;
+    // the counts and cursors are zeroed whenever they are (re)allocated (a
+    // new allocation may reuse the old address, so the capacity tells); the
+    // batch's own kernels reset what they used
+    if (b->bin_cnt.cap != cnt_cap0) SR_CK(cudaMemsetAsync(b->bin_cnt.p, 0, b->bin_cnt.cap * 4, b->stream));
+    if (b->bin_cursor.cap != cur_cap0) SR_CK(cudaMemsetAsync(b->bin_cursor.p, 0, b->bin_cursor.cap * 4, b->stream));
+    b->bin_cap = bin_cap;
     // ---- host table
     std::memset(b->htab, 0, L.bytes);
     *reinterpret_cast<uint32_t*>(b->htab + L.off_n) = n;
@@ -960,23 +1047,14 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
     BatchConfig cfg;
     if (b->forced.G) {
         cfg = b->forced;
-    } else {
-        const uint64_t cls = ((uint64_t)NB << 40) | ((uint64_t)log2_floor(tris + 1) << 20) | log2_floor(px + 1);
-        auto f = b->tuned.find(cls);
-        if (f != b->tuned.end()) {
-            cfg = f->second;
-        } else if (b->autotune) {
-            cfg = tune(b, NB);
-            b->tuned[cls] = cfg;
-        } else {
-            // untuned: as many primitives per warp as still leave every SM
-            // its full complement of warps (a few large primitives on a big
-            // frame need one warp each, or most of the GPU idles)
-            while (cfg.G > 1 && tris / cfg.G < (uint64_t)sm_count() * 48u) cfg.G >>= 1;
-        }
+    } else if (tuned_it != b->tuned.end()) {
+        cfg = tuned_it->second;
+    } else if (b->autotune) {
+        cfg = tune(b, NB, g_max);
+        b->tuned[cls] = cfg;
     }
-    // the large-primitive counter packs the count into 24 bits
-    if (tris >= (1ull << 24)) cfg.big = 0xffffffffu;
+    // the lists were sized for g_max entries per primitive
+    if (cfg.G > g_max) cfg.G = g_max;
     if ((rc = launch_batch(b, NB, cfg))) return rc;
     SR_CK(cudaEventRecord(b->done, b->stream));
     b->in_flight = true;
@@ -1002,9 +1080,10 @@ extern "C" SR_API int sr_batch_sync(sr_batch* b) {
     s.unsafe_triangles = f.unsafe;
     s.fragments = f.fragments;
     s.nan_bbox = f.nan_bbox;
-    s.kernel_launches = 7 + (uint32_t)__builtin_popcount(b->combos);
+    s.kernel_launches = 12 + (uint32_t)__builtin_popcount(b->combos);
     b->stats_valid = true;
     if (f.bad_index) return SR_EINVAL;
+    if (f.overflow_bits) return SR_EOVERFLOW;
     if (f.nan_total) return SR_ENAN;
     return SR_OK;
 }

@@ -29,15 +29,9 @@
 #include "sr_shade.cuh"
 #include "sr_opaque.cuh"
 #include "sr_setup.cuh"
+#include "sr_binraster.cuh"
 
 namespace sr {
-
-constexpr uint32_t TL_THREADS = 256;
-constexpr uint32_t TL_WARPS = TL_THREADS / 32;
-constexpr uint32_t TL_BIN_LOG2 = 5;   // bins of 32 x 32 pixels (the touched-block bitmap's granularity)
-static_assert(TL_BIN_LOG2 == TOUCH_LOG2, "the extension keys' bitmap marks bins");
-
-constexpr uint32_t TL_CHUNK = TL_THREADS;   // primitives a raster work item stages (one per thread)
 
 // Exclusive scans, in one CTA, of the n bins' primitive counts (list offsets)
 // and of their work items: ceil(count / TL_CHUNK) chunks per bin, one for a
@@ -160,71 +154,25 @@ __global__ void __launch_bounds__(256) bin_scatter_kernel(uint32_t n_host, uint3
     }
 }
 
-constexpr uint32_t TL_QCAP = 160;    // pixels a warp's stack holds: 31 waiting + 4 x 32 pushed
-
-// Per staged primitive, the sign pre-test's three rejection thresholds (see
-// bin_raster_kernel); the edge coefficients, anchor and det come from the
-// setup record, the sign s from its last word.
-struct PreRec {
-    float tu, tv, tw;
-};
-
-// Work item = one chunk of up to TL_CHUNK primitives of one 32x32 bin's list
-// (bin_scan_kernel numbers them).  Persistent CTAs take items from a counter.
-// For each item the CTA reduces the winner key of each pixel of the bin in
-// shared memory; a bin with one item writes the keys' low words (pass * N +
-// primitive + 1, 0 for no fragment) to its 1024 slots of `gids`, a bin with
-// several items -- a long list, as a dense mesh on a small frame gives --
-// merges each non-zero key into the pixel's slot of the global key buffer
-// with a 64-bit atomicMax, which also holds any extension keys of the bin;
-// bin_resolve_kernel shades either.  Each chunk primitive's bbox clipped to
-// the bin gives its items (runs of four horizontally adjacent pixels,
-// ceil(w / 4) per row), a CTA-wide scan numbers them, and they are split into
-// equal contiguous ranges, one per warp.  Every binned primitive's bbox meets
-// its bin, so every primitive of a chunk has items and their first items are
-// strictly increasing: a warp finds the owner of its first item by binary
-// search and then, per window of 32 items, the primitives starting inside the
-// window from one load per lane.
-//
-// Pre-test.  With s = det_sign(det) (non-zero for 0 < |det| < 1e18), the run's
-// first pixel gets eu = (sA) dx + (sB) dy and ev = (sC) dx + (sD) dy with the
-// reference's operations, i.e. exactly s nu and s nv of the reference; the
-// next pixels add sA and sC (the exact edge functions step by exactly that).
-// Each addition errs by at most 2^-24 of its result, and the reference's own
-// numerators differ from the exact edge functions by at most 3.0001 2^-24 S,
-// S = |A| Xr + |B| Yr over the clipped bbox (Xr, Yr bounding |x - x3|,
-// |y - y3|), so eu stays within 9.01 2^-24 Su of s nu:
-//   eu < -(1e-18 + 2^-20 Su)   proves s nu < -1e-18, i.e. u < 0;  v alike;
-//   ew = (|det| - eu) - ev < -2^-20 (|det| + Su + Sv) - 2^-140 |det|
-// proves w = (1-u)-v < 0 (frag_key's third-edge argument, whose slack is
-// 3.01 2^-24 |det| + 13.1 2^-24 (Su + Sv) with these approximations).  The
-// pixels the pre-test keeps -- those covered and a thin margin along the
-// edges -- go onto a per-warp stack in shared memory, and whenever 32 wait the
-// whole warp evaluates them exactly (frag_key: the reference's divisions, z,
-// the key) with every lane busy.
+// Persistent CTAs take work items (bin_scan_kernel numbers them: chunks of
+// TL_CHUNK primitives of one bin's list) from a counter and reduce each with
+// bin_item (sr_binraster.cuh): a bin in one item writes its winners to its
+// slots of `gids` (seeded with its extension keys when it has some), a bin in
+// several items merges its keys into `gkeys`, where bin_resolve_kernel finds
+// them.
 __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
     DrawParams P, const float4* __restrict__ setup, const uint32_t* __restrict__ bin_off,
     const uint32_t* __restrict__ chunk_off, const uint32_t* __restrict__ entries, const uint8_t* __restrict__ stencil,
     uint32_t gate_with_stencil, unsigned long long* __restrict__ gkeys, const uint32_t* __restrict__ bitmap,
     uint32_t* __restrict__ gids, DeviceFlags* flags) {
-    __shared__ unsigned long long keys[1u << (2 * TL_BIN_LOG2)];
-    __shared__ float4 srec[TL_CHUNK][3];
-    __shared__ PreRec spre[TL_CHUNK];
+    __shared__ BinSmem sm;
     __shared__ unsigned long long sfrags;
     __shared__ uint32_t sitem;
-    __shared__ uint32_t sst[TL_CHUNK + 1];            // first item of each primitive; [n] = items
-    __shared__ uint32_t sxy[TL_CHUNK];                // x0 | y0 << 16 (bin-relative) | seam bits 15, 31
-    __shared__ uint32_t sw[TL_CHUNK];                 // runs per row | clipped width << 16
-    __shared__ uint32_t smag[TL_CHUNK];               // ceil(2^32 / runs per row), 0 for one run
-    __shared__ uint32_t st[TL_CHUNK];                 // primitive index
-    __shared__ uint32_t squeue[TL_WARPS][TL_QCAP];    // pre-tested pixels: chunk slot << 10 | y << 5 | x
     if (flags->poison) return;
     const uint32_t n_bins = P.bins_x * P.bins_y;
     const uint32_t n_items = chunk_off[n_bins];
     const uint32_t N = P.n_raster_host ? P.n_raster_host : (uint32_t)flags->n_gen_tris;
-    const uint32_t lane = threadIdx.x & 31, wl = threadIdx.x >> 5;
-    const uint32_t mx = P.magic_w, my = P.magic_h;
-    const uint32_t lt = (1u << lane) - 1u;   // lanes below this one
+    const uint32_t lane = threadIdx.x & 31;
     if (threadIdx.x == 0) sfrags = 0;
     unsigned long long frags = 0;
     for (;;) {
@@ -249,146 +197,8 @@ __global__ void __launch_bounds__(TL_THREADS, 6) bin_raster_kernel(
         const uint32_t n = cnt_bin > c0 ? min(cnt_bin - c0, TL_CHUNK) : 0u;
         const bool ext = (bitmap[b >> 5] >> (b & 31)) & 1u;
         const uint32_t X0 = (b % P.bins_x) << TL_BIN_LOG2, Y0 = (b / P.bins_x) << TL_BIN_LOG2;
-        const uint32_t X1 = min(X0 + (1u << TL_BIN_LOG2) - 1, P.W - 1), Y1 = min(Y0 + (1u << TL_BIN_LOG2) - 1, P.H - 1);
-        for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS) {
-            unsigned long long k = 0;
-            if (whole && ext) {   // seed with the bin's extension keys (they stay in gkeys otherwise)
-                const uint32_t px = X0 + (i & 31), py = Y0 + (i >> TL_BIN_LOG2);
-                if (px <= X1 && py <= Y1) {
-                    const size_t gi = (size_t)py * P.W + px;
-                    k = gkeys[gi];
-                    if (k) gkeys[gi] = 0;
-                }
-            }
-            keys[i] = k;
-        }
-        uint32_t a = 0;
-        if (threadIdx.x < n) {
-            const uint32_t t = __ldg(entries + e_bin + c0 + threadIdx.x);
-            const float4* r = setup + 4 * (size_t)t;
-            const float4 r0 = __ldg(r), r1 = __ldg(r + 1), r2 = __ldg(r + 2), r3 = __ldg(r + 3);
-            const uint32_t x0 = (uint32_t)max(__float_as_int(r3.x), (int)X0);
-            const uint32_t y0 = (uint32_t)max(__float_as_int(r3.y), (int)Y0);
-            const uint32_t x1 = (uint32_t)min(__float_as_int(r3.z), (int)X1);
-            const uint32_t y1 = (uint32_t)min(__float_as_int(r3.w), (int)Y1);
-            const uint32_t w = x1 - x0 + 1, wq = (w + 3) >> 2;
-            a = (y1 - y0 + 1) * wq;
-            srec[threadIdx.x][0] = r0;
-            srec[threadIdx.x][1] = r1;
-            srec[threadIdx.x][2] = r2;
-            PreRec pr;
-            if (r2.w != 0.0f) {
-                // bounds of |x - x3| and |y - y3| over the clipped bbox's pixel centres
-                const float xr = fmaxf(fabsf(((float)x0 + 0.5f) - r1.x), fabsf(((float)x1 + 0.5f) - r1.x)) * 1.001f;
-                const float yr = fmaxf(fabsf(((float)y0 + 0.5f) - r1.y), fabsf(((float)y1 + 0.5f) - r1.y)) * 1.001f;
-                const float su = fabsf(r0.x) * xr + fabsf(r0.y) * yr, sv = fabsf(r0.z) * xr + fabsf(r0.w) * yr;
-                const float ad = fabsf(r1.z);
-                pr.tu = 1.0e-18f + 0x1p-20f * su;
-                pr.tv = 1.0e-18f + 0x1p-20f * sv;
-                pr.tw = 0x1p-20f * ((ad + su) + sv) + 0x1p-140f * ad;
-            } else {   // no sign information: keep every pixel for the exact test
-                const float INF = __int_as_float(0x7f800000);
-                pr.tu = INF; pr.tv = INF; pr.tw = INF;
-            }
-            spre[threadIdx.x] = pr;
-            const uint32_t sb = seam_bits(x0, y0, x1, y1, P);
-            sxy[threadIdx.x] = (x0 - X0) | ((y0 - Y0) << 16) | ((sb & 1u) << 15) | ((sb & 2u) << 30);
-            sw[threadIdx.x] = wq | (w << 16);
-            st[threadIdx.x] = t;
-            smag[threadIdx.x] = wq == 1 ? 0u : 0xffffffffu / wq + 1u;   // ceil(2^32 / wq) for wq >= 2
-        }
-        uint32_t total;
-        const uint32_t ex = block_exclusive_scan<uint32_t, TL_THREADS>(a, &total);
-        if (threadIdx.x < n) sst[threadIdx.x] = ex;
-        if (threadIdx.x == 0) sst[n] = total;
-        __syncthreads();
-        // this warp's items [q0, q1): equal shares in whole windows of 32
-        const uint32_t per = ((total + TL_WARPS * 32 - 1) / (TL_WARPS * 32)) * 32;
-        const uint32_t q0 = min(wl * per, total), q1 = min(q0 + per, total);
-        uint32_t cur = 0;   // owner of item q0: the last primitive whose first item is <= q0
-        {
-            uint32_t lo = 0, hi = n;   // sst[lo] <= q0 < sst[hi]
-            while (hi - lo > 1) {
-                const uint32_t mid = (lo + hi) >> 1;
-                if (sst[mid] <= q0) lo = mid; else hi = mid;
-            }
-            cur = lo;
-        }
-        uint32_t qn = 0;   // pixels waiting on the warp's stack (warp-uniform)
-        for (uint32_t base = q0; base < q1; base += 32) {
-            // primitives cur+1 .. cur+32 that start inside [base, base + 32)
-            const uint32_t j = cur + 1 + lane;
-            const uint32_t sj = j < n ? sst[j] : 0xffffffffu;
-            const uint32_t starts = __reduce_or_sync(0xffffffffu, sj - base < 32u ? (1u << (sj - base)) : 0u);
-            const uint32_t o = cur + __popc(starts & (lt | (1u << lane)));
-            cur += __popc(starts);
-            const uint32_t q = base + lane;
-            uint32_t cm = 0, lx = 0, ly = 0;   // candidate pixels of this lane's run (bit k: pixel lx + k)
-            if (q < q1) {
-                const uint32_t local = q - sst[o];
-                const uint32_t wqw = sw[o], wq = wqw & 0xffffu, mg = smag[o];
-                const uint32_t row = mg ? __umulhi(local, mg) : local;
-                const uint32_t col = 4 * (local - row * wq);
-                const uint32_t xy = sxy[o];
-                lx = (xy & 0x7fffu) + col;
-                ly = ((xy >> 16) & 0x7fffu) + row;
-                const uint32_t left = min((wqw >> 16) - col, 4u);
-                const PreRec pr = spre[o];
-                const float4 r0 = srec[o][0], r1 = srec[o][1];
-                const float sg = srec[o][2].w;   // det_sign(det)
-                const float sa = sg * r0.x, sb = sg * r0.y, sc = sg * r0.z, sd = sg * r0.w, ad = sg * r1.z;
-                const float dx = ((float)(X0 + lx) + 0.5f) - r1.x;
-                const float dy = ((float)(Y0 + ly) + 0.5f) - r1.y;
-                float eu = sa * dx + sb * dy;
-                float ev = sc * dx + sd * dy;
-#pragma unroll
-                for (uint32_t k = 0; k < 4; ++k) {
-                    if (k) { eu = eu + sa; ev = ev + sc; }
-                    const float ew = (ad - eu) - ev;
-                    const bool keep = !(eu < -pr.tu) && !(ev < -pr.tv) && !(ew < -pr.tw);
-                    if (k < left && keep) cm |= 1u << k;
-                }
-            }
-            // push the candidates (slots in lane order per pixel position k)
-            uint32_t pos = qn;
-#pragma unroll
-            for (uint32_t k = 0; k < 4; ++k) {
-                const uint32_t bal = __ballot_sync(0xffffffffu, (cm >> k) & 1u);
-                if ((cm >> k) & 1u) squeue[wl][pos + __popc(bal & lt)] = (o << 10) | (ly << 5) | (lx + k);
-                pos += __popc(bal);
-            }
-            qn = pos;
-            __syncwarp();
-            // exact evaluation, 32 pixels at a time from the top of the stack
-            // (what is left after the warp's last window, too)
-            while (qn >= 32 || (qn && base + 32 >= q1)) {
-                const uint32_t m = min(qn, 32u);
-                if (lane < m) {
-                    const uint32_t e = squeue[wl][qn - m + lane];
-                    const uint32_t oo = e >> 10, ex_ = e & 31u, ey = (e >> 5) & 31u;
-                    const uint32_t xy = sxy[oo];
-                    const uint32_t seams = ((xy >> 15) & 1u) | ((xy >> 30) & 2u);
-                    const unsigned long long k =
-                        frag_key(P.W, P.H, P.tile_w, P.tile_h, mx, my, seams, P.has_depth != 0, srec[oo][0],
-                                 srec[oo][1], srec[oo][2], st[oo], X0 + ex_, Y0 + ey, N, stencil, gate_with_stencil,
-                                 P.stencil_test, P.sref, frags);
-                    if (k) atomicMax(keys + (ey << TL_BIN_LOG2) + ex_, k);
-                }
-                qn -= m;
-                __syncwarp();
-            }
-        }
-        __syncthreads();   // every warp's keys are final
-        if (whole) {
-            uint32_t* out = gids + ((size_t)b << (2 * TL_BIN_LOG2));
-            for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS)
-                out[i] = (uint32_t)(keys[i] & 0xffffffffull);
-        } else {
-            for (uint32_t i = threadIdx.x; i < (1u << (2 * TL_BIN_LOG2)); i += TL_THREADS) {
-                const unsigned long long k = keys[i];
-                if (k) atomicMax(gkeys + (size_t)(Y0 + (i >> TL_BIN_LOG2)) * P.W + X0 + (i & 31), k);
-            }
-        }
+        bin_item(sm, P, X0, Y0, setup, entries + e_bin + c0, n, N, stencil, gate_with_stencil, whole, whole && ext,
+                 gkeys, gids + ((size_t)b << (2 * TL_BIN_LOG2)), frags);
     }
     // one atomic per CTA for the fragment count
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);

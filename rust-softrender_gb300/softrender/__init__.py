@@ -479,8 +479,8 @@ class Batch:
         check(lib().sr_batch_set_stream(self.handle, C.c_void_p(stream_ptr) if stream_ptr else None),
               "sr_batch_set_stream")
 
-    def set_config(self, prims_per_warp=0, big_threshold=0, ctas_per_sm=0):
-        check(lib().sr_batch_set_config(self.handle, prims_per_warp, big_threshold, ctas_per_sm),
+    def set_config(self, bins_per_primitive=0, big_threshold=0, ctas_per_sm=0):
+        check(lib().sr_batch_set_config(self.handle, bins_per_primitive, big_threshold, ctas_per_sm),
               "sr_batch_set_config")
 
     def config(self):
