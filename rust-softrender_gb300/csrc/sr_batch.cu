@@ -311,6 +311,17 @@ __global__ void __launch_bounds__(256) batch_bin_pack_kernel(BTables T, uint32_t
     }
 }
 
+// The work-item table: the (draw, bin) of every work item, from the scanned
+// item offsets.
+__global__ void __launch_bounds__(256) batch_bin_items_kernel(BTables T, const unsigned long long* __restrict__ off,
+                                                              uint32_t* __restrict__ item_bin, uint64_t item_cap) {
+    const uint32_t total = __ldg(T.bbase + *T.n);
+    for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < total; j += gridDim.x * blockDim.x) {
+        const uint32_t c0 = (uint32_t)(off[j] & 0xffffffffull), c1 = (uint32_t)(off[j + 1] & 0xffffffffull);
+        for (uint32_t k = c0; k < c1 && k < item_cap; ++k) item_bin[k] = j;
+    }
+}
+
 // Every listed primitive into the list of each bin of its rectangle (draw-
 // local primitive numbers; order within a list is free).  `cursor` (cap
 // entries, zero) counts the slots taken per bin.
@@ -363,49 +374,55 @@ __global__ void __launch_bounds__(256) batch_bin_scatter_kernel(BTables T, const
     }
 }
 
-// Persistent CTAs take work items from a counter: item -> (draw, bin) by
-// binary search over the scanned item offsets, then bin_item reduces it.  A
-// bin in one item starts from the keys already in the key buffer when its
-// bitmap bit says so, and stores its non-zero keys there; a bin in several
-// items merges them with atomicMax.  Each item marks its bin in the bitmap.
+// Persistent CTAs take work items from a counter: the work-item table gives
+// the item's (draw, bin), and bin_item reduces it.  A bin in one item starts
+// from the keys already in the key buffer when its bitmap bit says so, and
+// stores its non-zero keys there; a bin in several items merges them with
+// atomicMax.  Each item marks its bin in the bitmap.  The next item is fetched
+// while the current one is reduced.
 __global__ void __launch_bounds__(TL_THREADS, 6) batch_bin_raster_kernel(
     BTables T, const float4* __restrict__ setup, const unsigned long long* __restrict__ off, uint32_t cap,
-    const uint32_t* __restrict__ entries, uint64_t entry_cap, uint32_t* __restrict__ cursor, DeviceFlags* flags) {
+    const uint32_t* __restrict__ item_bin, uint64_t item_cap, const uint32_t* __restrict__ entries,
+    uint64_t entry_cap, uint32_t* __restrict__ cursor, DeviceFlags* flags) {
     __shared__ BinSmem sm;
     __shared__ DrawParams sP;
-    __shared__ uint32_t sitem, sbin, sdraw;
+    __shared__ uint4 snext[2];   // per parity: item, (draw, bin), draw, 0
+    __shared__ ulonglong2 soff[2];   // per parity: the bin's packed offsets and the next bin's
     __shared__ bool sext;
     __shared__ unsigned long long sfrags;
     const uint32_t n = *T.n;
     const uint32_t n_items = (uint32_t)(off[cap] & 0xffffffffull);
-    if (threadIdx.x == 0) sfrags = 0;
-    unsigned long long frags = 0;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            const uint32_t item = (uint32_t)min(atomicAdd(&flags->work_raster, 1ull), 0xffffffffull);
-            sitem = item;
-            if (item < n_items) {
-                // the item's bin: the last j whose first item is <= item
-                uint32_t lo = 0, hi = cap;
-                while (hi - lo > 1) {
-                    const uint32_t mid = (lo + hi) >> 1;
-                    if ((uint32_t)(off[mid] & 0xffffffffull) <= item) lo = mid; else hi = mid;
-                }
-                sbin = lo;
-                sdraw = owner_of(T.bbase, n, lo);
-            }
+    auto fetch = [&](uint32_t item, uint32_t par) {
+        uint4 v = make_uint4(item, 0, 0, 0);
+        ulonglong2 o = make_ulonglong2(0, 0);
+        if (item < n_items && item < item_cap) {
+            const uint32_t fb = min(__ldg(item_bin + item), cap - 1);
+            v = make_uint4(item, fb, owner_of(T.bbase, n, fb), 0);
+            o = make_ulonglong2(off[fb], off[fb + 1]);
         }
-        __syncthreads();   // the previous item is done with the shared arrays
-        const uint32_t item = sitem;
+        snext[par] = v;
+        soff[par] = o;
+    };
+    if (threadIdx.x == 0) {
+        sfrags = 0;
+        fetch((uint32_t)min(atomicAdd(&flags->work_raster, 1ull), 0xffffffffull), 0);
+    }
+    __syncthreads();
+    unsigned long long frags = 0;
+    for (uint32_t par = 0;; par ^= 1u) {
+        const uint4 it = snext[par];
+        const ulonglong2 oo = soff[par];
+        const uint32_t item = it.x;
         if (item >= n_items) break;
-        const uint32_t fb = sbin, i = sdraw;
+        uint32_t nxt = 0;
+        if (threadIdx.x == 0) nxt = (uint32_t)min(atomicAdd(&flags->work_raster, 1ull), 0xffffffffull);
+        const uint32_t fb = it.y, i = it.z;
         const BInst& I = T.inst[i];
         for (uint32_t k = threadIdx.x; k < sizeof(DrawParams) / 4; k += blockDim.x)
             reinterpret_cast<uint32_t*>(&sP)[k] = reinterpret_cast<const uint32_t*>(&I.P)[k];
         const uint32_t b = fb - __ldg(T.bbase + i);
-        const unsigned long long o0 = off[fb], o1 = off[fb + 1];
-        const uint32_t e_bin = (uint32_t)(o0 >> 32), cnt_bin = (uint32_t)(o1 >> 32) - e_bin;
-        const uint32_t c_first = (uint32_t)(o0 & 0xffffffffull), n_chunks = (uint32_t)(o1 & 0xffffffffull) - c_first;
+        const uint32_t e_bin = (uint32_t)(oo.x >> 32), cnt_bin = (uint32_t)(oo.y >> 32) - e_bin;
+        const uint32_t c_first = (uint32_t)(oo.x & 0xffffffffull), n_chunks = (uint32_t)(oo.y & 0xffffffffull) - c_first;
         const uint32_t c0 = (item - c_first) * TL_CHUNK;
         uint32_t cnt = cnt_bin > c0 ? min(cnt_bin - c0, TL_CHUNK) : 0u;
         if ((uint64_t)e_bin + c0 + cnt > entry_cap) cnt = 0;   // flagged by the scatter
@@ -421,6 +438,8 @@ __global__ void __launch_bounds__(TL_THREADS, 6) batch_bin_raster_kernel(
         const uint32_t X0 = (b % sP.bins_x) << TL_BIN_LOG2, Y0 = (b / sP.bins_x) << TL_BIN_LOG2;
         bin_item(sm, sP, X0, Y0, setup + 4 * (size_t)I.tbase, entries + e_bin + c0, cnt, sP.n_raster_host, nullptr,
                  0u, whole, seed, I.gkeys, nullptr, frags);
+        if (threadIdx.x == 0) fetch(nxt, par ^ 1u);
+        __syncthreads();   // the next item is known, and this one is done with the shared arrays
     }
     for (int o = 16; o > 0; o >>= 1) frags += __shfl_down_sync(0xffffffffu, frags, o);
     if ((threadIdx.x & 31) == 0 && frags) atomicAdd(&sfrags, frags);
@@ -647,6 +666,7 @@ struct sr_batch {
     DevBuf<uint32_t> bin_cnt, bin_cursor;   // per (draw, bin): listed primitives, slots taken
     DevBuf<unsigned long long> bin_pack, bin_off, bin_tmp;   // packed counts, their exclusive scan, scan scratch
     DevBuf<uint32_t> entries;               // the bins' primitive lists
+    DevBuf<uint32_t> item_bin;              // the (draw, bin) of each work item
     uint32_t bin_cap = 0;                   // (draw, bin) capacity the graphs were recorded for
     DeviceFlags* flags = nullptr;
     DeviceFlags* hflags = nullptr;
@@ -715,10 +735,14 @@ void enqueue_batch(sr_batch* b, uint32_t NB, const BatchConfig& c) {
     batch_bin_pack_kernel<<<resident_grid(batch_bin_pack_kernel, 256, 8), 256, 0, st>>>(T, cap, b->bin_cnt.p,
                                                                                         b->bin_pack.p);
     exclusive_scan<unsigned long long>(b->bin_pack.p, cap, b->bin_off.p, b->bin_tmp.p, st);
+    batch_bin_items_kernel<<<resident_grid(batch_bin_items_kernel, 256, 8), 256, 0, st>>>(T, b->bin_off.p,
+                                                                                          b->item_bin.p,
+                                                                                          b->item_bin.cap);
     batch_bin_scatter_kernel<<<resident_grid(batch_bin_scatter_kernel, 256, 8), 256, 0, st>>>(
         T, b->binrect.p, b->bin_off.p, b->bin_cursor.p, b->entries.p, b->entries.cap, b->flags);
     batch_bin_raster_kernel<<<resident_grid(batch_bin_raster_kernel, TL_THREADS, (int)c.ctas), TL_THREADS, 0, st>>>(
-        T, b->setup.p, b->bin_off.p, cap, b->entries.p, b->entries.cap, b->bin_cursor.p, b->flags);
+        T, b->setup.p, b->bin_off.p, cap, b->item_bin.p, b->item_bin.cap, b->entries.p, b->entries.cap,
+        b->bin_cursor.p, b->flags);
     batch_collect_kernel<<<resident_grid(batch_collect_kernel, 256, 8), 256, 0, st>>>(T, b->tlist.p, b->queues);
     batch_clear_kernel<<<resident_grid(batch_clear_kernel, 256, 8), 256, 0, st>>>(T);
     for (int fs = 0; fs < FS_COUNT; ++fs)
@@ -824,6 +848,8 @@ extern "C" SR_API int sr_batch_destroy(sr_batch* b) {
     drop_graphs(b);
     b->dtab.release(); b->scr4.release(); b->vary.release(); b->setup.release();
     b->area.release(); b->big_list.release(); b->big_base.release(); b->unsafe_list.release(); b->tlist.release();
+    b->binrect.release(); b->bin_cnt.release(); b->bin_cursor.release(); b->bin_pack.release();
+    b->bin_off.release(); b->bin_tmp.release(); b->entries.release(); b->item_bin.release();
     if (b->htab) cudaFreeHost(b->htab);
     if (b->flags) cudaFree(b->flags);
     if (b->hflags) cudaFreeHost(b->hflags);
@@ -950,7 +976,8 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
     if ((rc = grow(b, b->bin_cnt, bin_cap)) || (rc = grow(b, b->bin_cursor, bin_cap)) ||
         (rc = grow(b, b->bin_pack, bin_cap)) || (rc = grow(b, b->bin_off, (size_t)bin_cap + 1)) ||
         (rc = grow(b, b->bin_tmp, (size_t)scan_blocks(bin_cap) + 2)) ||
-        (rc = grow(b, b->entries, (size_t)g_max * tris + 1)))
+        (rc = grow(b, b->entries, (size_t)g_max * tris + 1)) ||
+        (rc = grow(b, b->item_bin, bin_item_cap((uint64_t)g_max * tris, bin_cap))))
         return rc;
     // the counts and cursors are zeroed whenever they are (re)allocated (a
     // new allocation may reuse the old address, so the capacity tells); the
@@ -1080,7 +1107,7 @@ extern "C" SR_API int sr_batch_sync(sr_batch* b) {
     s.unsafe_triangles = f.unsafe;
     s.fragments = f.fragments;
     s.nan_bbox = f.nan_bbox;
-    s.kernel_launches = 12 + (uint32_t)__builtin_popcount(b->combos);
+    s.kernel_launches = 13 + (uint32_t)__builtin_popcount(b->combos);
     b->stats_valid = true;
     if (f.bad_index) return SR_EINVAL;
     if (f.overflow_bits) return SR_EOVERFLOW;

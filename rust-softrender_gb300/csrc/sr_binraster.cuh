@@ -14,6 +14,7 @@ constexpr uint32_t TL_WARPS = TL_THREADS / 32;
 constexpr uint32_t TL_BIN_LOG2 = 5;   // bins of 32 x 32 pixels (the touched-block bitmap's granularity)
 static_assert(TL_BIN_LOG2 == TOUCH_LOG2, "the extension keys' bitmap marks bins");
 constexpr uint32_t TL_CHUNK = TL_THREADS;   // primitives a raster work item stages (one per thread)
+static_assert(TL_CHUNK == BIN_CHUNK, "work items of the bin scans");
 constexpr uint32_t TL_QCAP = 64;            // pixels a warp's stack holds: 31 waiting + 32 pushed
 
 // Per staged primitive, the sign pre-test's three rejection thresholds (see

@@ -376,6 +376,14 @@ struct OpaqueArgs {
 int launch_opaque(const DrawParams& P, const sr_uniforms& U, const OpaqueArgs& A, cudaStream_t st);
 // Opaque draws over 32x32 screen bins (sr_tiled.cu), after setup has counted
 // each bin's primitives; returns the number of kernels launched.
+// Primitives of one bin a raster work item reduces (the bin raster's CTA
+// size); a bin of e listed primitives has ceil(e / BIN_CHUNK) work items.
+constexpr uint32_t BIN_CHUNK = 256;
+// Capacity of a work-item -> bin table (the batched bin raster's) for
+// `entries` list entries over `bins` bins: ceil(e_b / BIN_CHUNK) items per
+// bin, one for a bin with only keys from elsewhere.
+inline uint64_t bin_item_cap(uint64_t entries, uint64_t bins) { return entries / BIN_CHUNK + 2 * bins + 1; }
+
 struct TiledArgs {
     const float4* setup;
     const uint2* binrect;            // per raster primitive: its bbox's bin rectangle (setup output)
