@@ -84,6 +84,25 @@ __global__ void copy_plane_kernel(const DeviceFlags* __restrict__ flags, uint32_
     if (i < n - 4 * n4) dst[4 * n4 + i] = src[4 * n4 + i];
 }
 
+// The unit expansion of n RGBA8 texels: each channel c as c / 255
+// (sr_u8_unit, the sampler's own conversion).
+__global__ void expand_texels_kernel(const uint32_t* __restrict__ src, float4* __restrict__ dst, size_t n) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const sr_v4 c = sr_from_rgba8(src[i]);
+        dst[i] = make_float4(c.x, c.y, c.z, c.w);
+    }
+}
+
+// Rebuilds an RGBA8 texture's unit expansion from its texels on `st`.
+int texture_expand(sr_texture* t, cudaStream_t st) {
+    if (!t || t->f32 || t->view || !t->unit) return SR_OK;
+    const size_t n = (size_t)t->w * t->h;
+    const unsigned grid = (unsigned)std::min<size_t>((n + 255) / 256, 152 * 16);
+    expand_texels_kernel<<<grid, 256, 0, st>>>(t->data, t->unit, n);
+    SR_CK(cudaGetLastError());
+    return SR_OK;
+}
+
 int fs_min_varyings(int fs) {
     switch (fs) {
     case FS_TEXTURED_BLINN_PHONG: return 10;
@@ -432,10 +451,14 @@ extern "C" SR_API int sr_texture_upload(const uint32_t* rgba8, uint32_t w, uint3
     t->w = w;
     t->h = h;
     cudaError_t e = cudaMalloc(&t->data, (size_t)w * h * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&t->unit, (size_t)w * h * 16);
     if (e == cudaSuccess) e = cudaMemcpy(t->data, rgba8, (size_t)w * h * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && texture_expand(t, nullptr) != SR_OK) e = last_cuda_error();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(nullptr);
     if (e != cudaSuccess) {
         last_cuda_error() = e;
         if (t->data) cudaFree(t->data);
+        if (t->unit) cudaFree(t->unit);
         delete t;
         return e == cudaErrorMemoryAllocation ? SR_ENOMEM : SR_ECUDA;
     }
@@ -485,6 +508,8 @@ extern "C" SR_API int sr_texture_update(sr_texture* t, const uint32_t* rgba8, ui
     if (!t || !rgba8 || w != t->w || h != t->h || t->f32 || t->view) return SR_EINVAL;
     cudaStream_t st = (cudaStream_t)stream;
     SR_CK(cudaMemcpyAsync(t->data, rgba8, (size_t)w * h * 4, cudaMemcpyHostToDevice, st));
+    const int rc = texture_expand(t, st);
+    if (rc != SR_OK) return rc;
     if (!stream) SR_CK(cudaStreamSynchronize(st));
     return SR_OK;
 }
@@ -494,7 +519,7 @@ static int enqueue_texture_copy(sr_pipeline* p, const sr_texture* t) {
     const unsigned grid = (unsigned)std::min<size_t>((n / 4 + 4 + 255) / 256, 152 * 16);
     copy_plane_kernel<<<grid, 256, 0, p->stream>>>(p->flags, t->data, static_cast<const uint32_t*>(p->color), n);
     SR_CK(cudaGetLastError());
-    return SR_OK;
+    return texture_expand(const_cast<sr_texture*>(t), p->stream);
 }
 
 extern "C" SR_API int sr_texture_from_framebuffer(sr_pipeline* p, sr_texture* t) {
@@ -518,6 +543,7 @@ void sr::texture_unref(const sr_texture* ct) {
     if (!t || t->refs.fetch_sub(1, std::memory_order_acq_rel) != 1) return;
     if (t->view) color_plane_unref(t->plane);
     else if (t->data) cudaFree(t->data);
+    if (t->unit) cudaFree(t->unit);
     delete t;
 }
 
@@ -555,7 +581,9 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
     P.color_format = p->fb.color_format;
     P.draw_id = draw_id;
     P.force_unsafe = p->force_unsafe ? 1u : 0u;
-    if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; P.tex_f32 = d->texture->f32; }
+    uint32_t tex_f32 = 0;
+    const uint32_t* tex_data = sampled_texels(d->texture, &tex_f32);
+    if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; P.tex_f32 = tex_f32; }
     P.tex_filter = d->tex_filter; P.tex_edge = d->tex_edge;
     // stencil mode (src/stencil.rs; a missing attachment behaves as `()`)
     uint32_t test = pd.stencil_test, op = pd.stencil_op;
@@ -644,7 +672,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
             launch_lp_geometry(P, pd.gU, m, vs, prim_n, d->gs_mode, (uint32_t)d->gs, lv, p->lpvalid.p, p->flags, st);
         if (ev) { cudaEventRecord(ev[2], st); cudaEventRecord(ev[3], st); }
         const uint32_t tex_launches = 0;
-        const uint32_t* tex = d->texture ? d->texture->data : nullptr;
+        const uint32_t* tex = tex_data;
         const uint32_t ph = launch_lp_raster(P, pd.U, lv, p->lpvalid.p, n_out, prim_out, tex, p->color, p->depth,
                                              p->stencil, p->flags, st);
         if (ev) { cudaEventRecord(ev[4], st); cudaEventRecord(ev[5], st); }
@@ -768,7 +796,7 @@ int enqueue_draw(sr_pipeline* p, const PendingDraw& pd, uint32_t draw_id, bool r
         launches += 7 + 2 * ((bits + 7) / 8) + 3;   // counts, scan, check, emits, radix passes, ranges
     }
     if (ev) cudaEventRecord(ev[3], st);
-    const uint32_t* tex = d->texture ? d->texture->data : nullptr;
+    const uint32_t* tex = tex_data;
     if (ordered) {
         launch_ordered(P, pd.U, p->setup.p, P.mode_b ? nullptr : p->ranges.p, bin_list, vidx, p->vary.p, tex, p->color,
                        p->depth, p->stencil, gate, p->flags, st);

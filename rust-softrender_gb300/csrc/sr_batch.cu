@@ -1031,7 +1031,9 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         P.color_format = p->fb.color_format;
         P.stencil_test = SR_STENCIL_ALWAYS; P.stencil_op = SR_STENCIL_KEEP; P.stencil_wrap = 1;
         P.force_unsafe = p->force_unsafe ? 1u : 0u;
-        if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; P.tex_f32 = d->texture->f32; }
+        uint32_t tex_f32 = 0;
+        const uint32_t* tex_data = sampled_texels(d->texture, &tex_f32);
+        if (d->texture) { P.tex_w = d->texture->w; P.tex_h = d->texture->h; P.tex_f32 = tex_f32; }
         P.tex_filter = d->tex_filter; P.tex_edge = d->tex_edge;
         P.bin_w_log2 = 5; P.bin_h_log2 = 5;
         P.bins_x = (W + 31) >> 5; P.bins_y = (H + 31) >> 5;
@@ -1043,7 +1045,7 @@ extern "C" SR_API int sr_batch_render(sr_batch* b, const sr_batch_item* items, u
         I.vpm = viewport_matrix(P.vp);
         I.planes = m->planes;
         I.indices = m->indices;
-        I.tex = d->texture ? d->texture->data : nullptr;
+        I.tex = tex_data;
         I.color = p->color;
         I.depth = p->depth;
         I.gkeys = p->gkeys.p;

@@ -306,10 +306,24 @@ struct sr_texture {
     uint32_t* data = nullptr;       // RGBA8 texels, or RGBA f32 texels (4 floats each) when f32
     uint32_t w = 0, h = 0;
     uint32_t f32 = 0;               // 1: RGBA f32 texels
+    // RGBA8 textures that the library writes (uploads, updates, framebuffer
+    // copies; not views): every texel also as its four c / 255 values, kept
+    // in step with `data` on the same streams, which is what draws sample
+    float4* unit = nullptr;
     bool view = false;              // reads a pipeline's colour plane in place (`plane`, referenced)
     sr_color_plane* plane = nullptr;
     std::atomic<uint32_t> refs{1};
 };
+
+// The texels a draw samples and whether they are RGBA f32 (sr_sample): an
+// RGBA8 texture's unit expansion when it has one -- the same values the
+// sampler would derive from its bytes -- else its own texels.
+inline const uint32_t* sampled_texels(const sr_texture* t, uint32_t* f32) {
+    if (!t) { *f32 = 0; return nullptr; }
+    if (!t->f32 && t->unit) { *f32 = 1; return reinterpret_cast<const uint32_t*>(t->unit); }
+    *f32 = t->f32;
+    return t->data;
+}
 
 // ------------------------------------------------------- grid sizing (host)
 // Streaming-multiprocessor count of the current device (cached per device).
