@@ -942,6 +942,7 @@ extern "C" SR_API int sr_sync(sr_pipeline* p) {
             }
             if (f.nan_total) status = SR_ENAN;
             if (f.bad_index) status = SR_EINVAL;
+            if (f.copy_timeout) status = SR_ECUDA;
             break;
         }
         // grow what overflowed and replay from the first poisoned draw

@@ -54,7 +54,7 @@ struct DeviceFlags {
     unsigned int poison_draw;     // id of the first draw that overflowed (atomicMin)
     unsigned int nan_total;       // primitives met with an all-NaN bbox since the last sync
     unsigned int bad_index;       // a mesh index >= vertex count was met (primitive skipped)
-    unsigned int pad0;
+    unsigned int copy_timeout;    // a tile copy's bounded wait gave up (the tile was skipped)
     unsigned long long need_gen_tris;
     unsigned long long need_gen_verts;
     unsigned long long need_entries;

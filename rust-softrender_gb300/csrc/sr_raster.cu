@@ -19,6 +19,7 @@
 #include "sr_internal.cuh"
 #include "sr_scan.cuh"
 #include "sr_shade.cuh"
+#include "sr_tma.cuh"
 
 namespace sr {
 
@@ -83,7 +84,16 @@ __global__ void __launch_bounds__(ORD_THREADS, OrdOccupancy<FS>::BLOCKS) raster_
     DrawParams P, sr_uniforms U, const float4* __restrict__ setup, const uint32_t* __restrict__ bin_off,
     const uint32_t* __restrict__ entries, const uint32_t* __restrict__ vidx, const float* __restrict__ vary,
     const uint32_t* __restrict__ tex, void* __restrict__ color, float* __restrict__ depth, uint8_t* __restrict__ stencil,
-    uint32_t gate_with_stencil, DeviceFlags* flags) {
+    uint32_t gate_with_stencil, DeviceFlags* flags, uint32_t tma, const __grid_constant__ CUtensorMap tm_color,
+    const __grid_constant__ CUtensorMap tm_depth, const __grid_constant__ CUtensorMap tm_stencil) {
+    // the bin's framebuffer tile (with `tma`): colour, depth and stencil are
+    // loaded by tensor copies, read and written by the bin's pixels in
+    // registers, and stored back the same way
+    constexpr uint32_t CW = FMT == SR_COLOR_RGBA32F ? 4u : 1u;   // colour words per pixel
+    __shared__ alignas(128) uint32_t t_color[ORD_THREADS * CW];
+    __shared__ alignas(128) float t_depth[ORD_THREADS];
+    __shared__ alignas(128) uint8_t t_stencil[ORD_THREADS];
+    __shared__ alignas(8) uint64_t t_bar;
     __shared__ float4 rec[ORD_CHUNK][3];
     __shared__ int4 rbb[ORD_CHUNK];
     __shared__ uint32_t rtri[ORD_CHUNK];
@@ -115,7 +125,36 @@ __global__ void __launch_bounds__(ORD_THREADS, OrdOccupancy<FS>::BLOCKS) raster_
     PixelColor<FMT> pc;
     float d = 0.0f;
     uint32_t s = 0;
-    if (active) {
+    // tile coordinates in the tensor maps' elements (colour RGBA32F: 4 words a pixel)
+    const int tx = (int)(bx * BW), ty = (int)(by * BH), tcx = (int)(bx * BW * CW);
+    if (tma) {
+        if (threadIdx.x == 0) {
+            mbar_init(&t_bar, 1);
+            uint32_t bytes = 0;
+            if (FMT != SR_COLOR_NONE) bytes += ORD_THREADS * CW * 4;
+            if (P.has_depth) bytes += ORD_THREADS * 4;
+            if (P.has_stencil) bytes += ORD_THREADS;
+            mbar_arrive_expect_tx(&t_bar, bytes);
+            if (FMT != SR_COLOR_NONE) tma_load_2d(t_color, &tm_color, tcx, ty, &t_bar);
+            if (P.has_depth) tma_load_2d(t_depth, &tm_depth, tx, ty, &t_bar);
+            if (P.has_stencil) tma_load_2d(t_stencil, &tm_stencil, tx, ty, &t_bar);
+        }
+        __syncthreads();   // the barrier is initialised before it is polled
+        bool done = false;
+        for (uint32_t polls = 0; !done && polls < TMA_WAIT_POLLS; ++polls) done = mbar_try_wait(&t_bar, 0);
+        if (!__syncthreads_and(done)) {
+            // the copies did not arrive in time: report, wait (bounded again)
+            // until they are no longer writing this CTA's shared memory, skip
+            // the tile
+            if (threadIdx.x == 0) atomicOr(&flags->copy_timeout, 1u);
+            for (uint32_t polls = 0; !done && polls < TMA_WAIT_POLLS; ++polls) done = mbar_try_wait(&t_bar, 0);
+            return;
+        }
+        if (FMT == SR_COLOR_RGBA32F) *(float4*)&pc.v = reinterpret_cast<const float4*>(t_color)[threadIdx.x];
+        else if (FMT == SR_COLOR_RGBA8) *(uint32_t*)&pc.v = t_color[threadIdx.x];
+        if (P.has_depth) d = t_depth[threadIdx.x];
+        if (P.has_stencil) s = t_stencil[threadIdx.x];
+    } else if (active) {
         if (FMT == SR_COLOR_RGBA32F) *(float4*)&pc.v = reinterpret_cast<float4*>(color)[gi];
         else if (FMT == SR_COLOR_RGBA8) *(uint32_t*)&pc.v = reinterpret_cast<uint32_t*>(color)[gi];
         if (P.has_depth) d = depth[gi];
@@ -246,7 +285,25 @@ __global__ void __launch_bounds__(ORD_THREADS, OrdOccupancy<FS>::BLOCKS) raster_
             }
         }
     }
-    if (active) {
+    if (tma) {
+        // the tile back through the copy engine; its pixels outside the frame
+        // are not written
+        if (active) {
+            if (FMT == SR_COLOR_RGBA32F) reinterpret_cast<float4*>(t_color)[threadIdx.x] = *(float4*)&pc.v;
+            else if (FMT == SR_COLOR_RGBA8) t_color[threadIdx.x] = *(uint32_t*)&pc.v;
+            if (P.has_depth) t_depth[threadIdx.x] = d;
+            if (P.has_stencil && P.mode_b) t_stencil[threadIdx.x] = (uint8_t)s;
+        }
+        fence_async_smem();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (FMT != SR_COLOR_NONE) tma_store_2d(&tm_color, tcx, ty, t_color);
+            if (P.has_depth) tma_store_2d(&tm_depth, tx, ty, t_depth);
+            if (P.has_stencil && P.mode_b) tma_store_2d(&tm_stencil, tx, ty, t_stencil);
+            bulk_commit();
+            bulk_wait();
+        }
+    } else if (active) {
         if (FMT == SR_COLOR_RGBA32F) reinterpret_cast<float4*>(color)[gi] = *(float4*)&pc.v;
         else if (FMT == SR_COLOR_RGBA8) reinterpret_cast<uint32_t*>(color)[gi] = *(uint32_t*)&pc.v;
         if (P.has_depth) depth[gi] = d;
@@ -257,23 +314,79 @@ __global__ void __launch_bounds__(ORD_THREADS, OrdOccupancy<FS>::BLOCKS) raster_
 }
 
 // ---------------------------------------------------------------- launch
+// Tensor maps of a draw's framebuffer planes for the ordered kernel's tile
+// copies (16 x 16 pixel boxes), when the planes allow them: row strides a
+// multiple of 16 bytes (RGBA8 colour and depth: a width that is a multiple
+// of 4; stencil: of 16) and 16-byte aligned planes.  Encoded on the host with
+// the driver's cuTensorMapEncodeTiled, looked up once through the runtime.
+struct FbMaps {
+    uint32_t tma = 0;
+    CUtensorMap color{}, depth{}, stencil{};
+};
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q{};
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) !=
+                cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            f = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(f);
+    }();
+    return fn;
+}
+
+static bool encode_plane(CUtensorMap* m, CUtensorMapDataType type, uint32_t elem_bytes, void* base, uint64_t cols,
+                         uint64_t rows, uint32_t box_cols, uint32_t box_rows) {
+    const EncodeTiledFn fn = encode_tiled();
+    if (!fn || !base || (reinterpret_cast<uintptr_t>(base) & 15) || (cols * elem_bytes) % 16) return false;
+    const cuuint64_t dims[2] = {cols, rows};
+    const cuuint64_t strides[1] = {cols * elem_bytes};
+    const cuuint32_t box[2] = {box_cols, box_rows};
+    const cuuint32_t estr[2] = {1, 1};
+    return fn(m, type, 2, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+              CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+static FbMaps fb_maps(const DrawParams& P, void* color, float* depth, uint8_t* stencil) {
+    FbMaps M;
+    const uint32_t BW = 1u << P.bin_w_log2, BH = 1u << P.bin_h_log2;
+    if (BW * BH != (uint32_t)ORD_THREADS) return M;
+    bool ok = true;
+    if (P.color_format == SR_COLOR_RGBA8)
+        ok = ok && encode_plane(&M.color, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, color, P.W, P.H, BW, BH);
+    else if (P.color_format == SR_COLOR_RGBA32F)   // four words a pixel
+        ok = ok && encode_plane(&M.color, CU_TENSOR_MAP_DATA_TYPE_UINT32, 4, color, 4ull * P.W, P.H, 4 * BW, BH);
+    if (P.has_depth) ok = ok && encode_plane(&M.depth, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, depth, P.W, P.H, BW, BH);
+    if (P.has_stencil)
+        ok = ok && encode_plane(&M.stencil, CU_TENSOR_MAP_DATA_TYPE_UINT8, 1, stencil, P.W, P.H, BW, BH);
+    M.tma = ok ? 1u : 0u;
+    return M;
+}
+
 template <int FS, int FMT, int BLEND>
 static void launch_ordered_t(const DrawParams& P, const sr_uniforms& U, const float4* setup, const uint32_t* bin_off,
                              const uint32_t* entries, const uint32_t* vidx, const float* vary, const uint32_t* tex,
                              void* color, float* depth, uint8_t* stencil, uint32_t gate, DeviceFlags* flags,
-                             cudaStream_t st) {
+                             const FbMaps& M, cudaStream_t st) {
     uint32_t nb = P.bins_x * P.bins_y;
-    raster_ordered_kernel<FS, FMT, BLEND><<<nb, ORD_THREADS, 0, st>>>(P, U, setup, bin_off, entries, vidx, vary,
-                                                                          tex, color, depth, stencil, gate, flags);
+    raster_ordered_kernel<FS, FMT, BLEND><<<nb, ORD_THREADS, 0, st>>>(P, U, setup, bin_off, entries, vidx, vary, tex,
+                                                                      color, depth, stencil, gate, flags, M.tma,
+                                                                      M.color, M.depth, M.stencil);
 }
 
 template <int FS>
 static void dispatch_fmt(const DrawParams& P, const sr_uniforms& U, const float4* setup, const uint32_t* bin_off,
                          const uint32_t* entries, const uint32_t* vidx, const float* vary, const uint32_t* tex,
                          void* color, float* depth, uint8_t* stencil, uint32_t gate, DeviceFlags* flags,
-                         cudaStream_t st) {
+                         const FbMaps& M, cudaStream_t st) {
 #define SR_ORD(FMT, BL) launch_ordered_t<FS, FMT, BL>(P, U, setup, bin_off, entries, vidx, vary, tex, color, depth, \
-                                                       stencil, gate, flags, st)
+                                                       stencil, gate, flags, M, st)
     if (P.color_format == SR_COLOR_RGBA32F) {
         if (P.blend == BLEND_OVER) SR_ORD(SR_COLOR_RGBA32F, BLEND_OVER);
         else SR_ORD(SR_COLOR_RGBA32F, BLEND_REPLACE);
@@ -289,7 +402,9 @@ static void dispatch_fmt(const DrawParams& P, const sr_uniforms& U, const float4
 void launch_ordered(const DrawParams& P, const sr_uniforms& U, const float4* setup, const uint32_t* bin_off,
                     const uint32_t* entries, const uint32_t* vidx, const float* vary, const uint32_t* tex, void* color,
                     float* depth, uint8_t* stencil, uint32_t gate, DeviceFlags* flags, cudaStream_t st) {
-#define SR_DISPATCH(F) dispatch_fmt<F>(P, U, setup, bin_off, entries, vidx, vary, tex, color, depth, stencil, gate, flags, st)
+    const FbMaps M = fb_maps(P, color, depth, stencil);
+#define SR_DISPATCH(F) dispatch_fmt<F>(P, U, setup, bin_off, entries, vidx, vary, tex, color, depth, stencil, gate, \
+                                       flags, M, st)
     switch (P.fs) {
     case FS_BLINN_PHONG_DIR: SR_DISPATCH(FS_BLINN_PHONG_DIR); break;
     case FS_TEXTURED_BLINN_PHONG: SR_DISPATCH(FS_TEXTURED_BLINN_PHONG); break;
