@@ -33,7 +33,8 @@ struct BinSmem {
     uint32_t sxy[TL_CHUNK];                // x0 | y0 << 16 (bin-relative) | seam bits 15, 31
     uint32_t sw[TL_CHUNK];                 // clipped width
     uint32_t st[TL_CHUNK];                 // primitive index
-    uint32_t squeue[TL_WARPS][TL_QCAP];    // pre-tested pixels: chunk slot << 10 | y << 5 | x
+    uint32_t squeue[TL_WARPS][TL_QCAP];    // pixels waiting for the exact test: chunk slot << 10 | y << 5 | x
+    uint32_t next_row;                     // the next window of rows a warp takes
 };
 
 // Work item = one chunk of up to TL_CHUNK primitives of one 32x32 bin's list.
@@ -47,12 +48,11 @@ struct BinSmem {
 // fragments, large primitives) the reduction starts from those keys.
 //
 // Rows.  Each chunk primitive's bbox clipped to the bin gives its rows; a
-// CTA-wide scan numbers them and they are split into equal contiguous ranges,
-// one per warp.  Every listed primitive's bbox meets its bin, so every
+// CTA-wide scan numbers them, and the warps take windows of 32 rows from a
+// shared counter.  Every listed primitive's bbox meets its bin, so every
 // primitive of a chunk has rows and their first rows are strictly increasing:
-// a warp finds the owner of its first row by binary search and then, per
-// window of 32 rows, the primitives starting inside the window from one load
-// per lane.  Each lane reduces its row to the span of pixels that can be
+// a warp finds the owner of its window's first row by binary search and the
+// primitives starting inside the window from one load per lane.  Each lane reduces its row to the span of pixels that can be
 // covered; the window's spans go onto a per-warp stack in shared memory, and
 // whenever 32 wait the whole warp evaluates them exactly (frag_key: the
 // reference's divisions, z, the key) with every lane busy.
@@ -139,29 +139,36 @@ __device__ __forceinline__ void bin_item(BinSmem& sm, const DrawParams& P, uint3
     uint32_t total;
     const uint32_t ex = block_exclusive_scan<uint32_t, TL_THREADS>(a, &total);
     if (threadIdx.x < n) sm.sst[threadIdx.x] = ex;
-    if (threadIdx.x == 0) sm.sst[n] = total;
-    __syncthreads();
-    // this warp's rows [q0, q1): equal shares in whole windows of 32
-    const uint32_t per = ((total + TL_WARPS * 32 - 1) / (TL_WARPS * 32)) * 32;
-    const uint32_t q0 = min(wl * per, total), q1 = min(q0 + per, total);
-    uint32_t cur = 0;   // owner of row q0: the last primitive whose first row is <= q0
-    {
-        uint32_t lo = 0, hi = n;   // sm.sst[lo] <= q0 < sm.sst[hi]
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (sm.sst[mid] <= q0) lo = mid; else hi = mid;
-        }
-        cur = lo;
+    if (threadIdx.x == 0) {
+        sm.sst[n] = total;
+        sm.next_row = 0;
     }
+    __syncthreads();
+    // windows of 32 rows, taken by the warps one at a time from a shared
+    // counter (rows differ in cost, so equal shares would leave warps waiting)
+    const uint32_t q1 = total;
     uint32_t qn = 0;   // pixels waiting on the warp's stack (warp-uniform, < 32 between rounds)
     const float INF = __int_as_float(0x7f800000);
-    for (uint32_t base = q0; base < q1; base += 32) {
+    for (;;) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&sm.next_row, 32u);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= q1) break;
+        // the owner of row `base`: the last primitive whose first row is <= base
+        uint32_t cur = 0;
+        {
+            uint32_t lo = 0, hi = n;   // sm.sst[lo] <= base < sm.sst[hi]
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) >> 1;
+                if (sm.sst[mid] <= base) lo = mid; else hi = mid;
+            }
+            cur = lo;
+        }
         // primitives cur+1 .. cur+32 that start inside [base, base + 32)
         const uint32_t j = cur + 1 + lane;
         const uint32_t sj = j < n ? sm.sst[j] : 0xffffffffu;
         const uint32_t starts = __reduce_or_sync(0xffffffffu, sj - base < 32u ? (1u << (sj - base)) : 0u);
         const uint32_t o = cur + __popc(starts & (lt | (1u << lane)));
-        cur += __popc(starts);
         const uint32_t q = base + lane;
         // this lane's row: the span [ka, kb] of its pixels that can be covered
         uint32_t len = 0, pinfo = 0;
