@@ -662,6 +662,20 @@ SR_HD bool sr_pow_bounded(float x, float y, float* val, float* err) {
     if (!(y > 0.0f && y <= 256.0f)) return false;
     if (x == 0.0f) { *val = sr_powf(x, y); *err = 0.0f; return true; }   /* exact zero (+0 or -0) */
     if (!(x >= 0x1p-100f && x <= 1.0f)) return false;
+    /* y = 2^k, k = 1..7 (the Blinn-Phong shininess of the examples gives
+     * 64): k squarings.  Each rounds once, so the relative error is at most
+     * (2^k - 1) 2^-24 while the squares are normal; subnormal squares add at
+     * most 2^-150 each, at most doubled by each later squaring (x <= 1), so
+     * under 2^-143 in all.  sr_powf is within 0.51 ulp of x^y. */
+    const uint32_t yb = sr_f2u(y);
+    if ((yb & 0x007fffffu) == 0u && y >= 2.0f && y <= 128.0f) {
+        const int k = (int)((yb >> 23) & 0xffu) - 127;
+        float p = x;
+        for (int i = 0; i < k; ++i) p = p * p;
+        *val = p;
+        *err = p * ((float)(1 << k) * 0x1p-23f + 0x1p-22f) + 0x1p-138f;   /* twice the bound */
+        return true;
+    }
     const float t = sr_ylog2_fast(x, y);
     if (t < -120.0f) { *val = 0.0f; *err = 0x1p-119f; return true; }  /* exact value < 2^-119.9 */
     if (!(t <= 120.0f)) return false;

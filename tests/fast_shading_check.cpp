@@ -3,7 +3,8 @@
 // tests/test_fast_shading.py (g++, -ffp-contract=off, the oracle's flags).
 //
 //   pow      sr_exp2_fast(sr_ylog2_fast(x, y)) against sr_powf(x, y): the
-//            observed relative error stays under half of sr_fast_pow_err
+//            observed relative error stays under half of sr_fast_pow_err;
+//            sr_pow_bounded by squaring (y = 2^k) within its stated bound
 //   bytes    sr_encode_byte_fast(u, 0, g) next to every byte boundary
 //            (u = (k/255)^(1/g) and its 512 float neighbours each side):
 //            a decided byte equals trunc(sr_powf(u, g) * 255)
@@ -70,6 +71,18 @@ int main(int argc, char** argv) {
         if (ratio > worst) worst = ratio;
     }
     if (!(worst < 0.5)) ++mismatches;
+
+    // ---- pow by squaring (exponents 2^k): within the stated absolute bound
+    double worst_sq = 0.0;
+    for (long k = 0; k < n_pow; ++k) {
+        const float y = (float)(1 << (1 + (int)(k % 7)));
+        const float x = (k & 1) ? uni(0.0f, 1.0f) : std::exp2(uni(-100.0f, 0.0f));
+        float val = 0.0f, err = 0.0f;
+        if (!sr_pow_bounded(x, y, &val, &err)) continue;
+        const double d = std::fabs((double)val - (double)sr_powf(x, y));
+        if (err > 0.0f && d / (double)err > worst_sq) worst_sq = d / (double)err;
+        if (d > (double)err) ++mismatches;
+    }
 
     // ---- bytes at every boundary
     long byte_cases = 0, byte_fallbacks = 0;
@@ -169,8 +182,9 @@ int main(int argc, char** argv) {
         if (w != exact_rgba8(&U, pos, nrm, c)) ++mismatches;
         ++near_cases;
     }
-    printf("pow_max_ratio=%.4f byte_cases=%ld byte_fallbacks=%ld shade_cases=%ld shade_fallbacks=%ld "
+    printf("sq_max_ratio=%.4f pow_max_ratio=%.4f byte_cases=%ld byte_fallbacks=%ld shade_cases=%ld shade_fallbacks=%ld "
            "near_cases=%ld near_fallbacks=%ld mismatches=%ld\n",
-           worst, byte_cases, byte_fallbacks, shade_cases, shade_fallbacks, near_cases, near_fallbacks, mismatches);
+           worst_sq, worst, byte_cases, byte_fallbacks, shade_cases, shade_fallbacks, near_cases, near_fallbacks,
+           mismatches);
     return mismatches ? 1 : 0;
 }

@@ -34,8 +34,10 @@ def _run(exe, n_pow, n_shade, seed):
 def test_fast_shading_matches_exact(checker, seed):
     rc, f, text = _run(checker, 300000, 300000, seed)
     assert rc == 0 and int(f["mismatches"]) == 0, text
-    # the fast power stays well inside its stated bound
+    # the fast power stays well inside its stated bound, and so do the
+    # squarings for power-of-two exponents
     assert float(f["pow_max_ratio"]) < 0.5, text
+    assert float(f["sq_max_ratio"]) < 0.6, text
     # and decides almost every pixel of a random scene (fallback is rare)
     assert int(f["shade_fallbacks"]) < 0.01 * int(f["shade_cases"]), text
     # near a byte boundary most cases fall back, and none is decided wrongly
