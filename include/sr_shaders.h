@@ -103,11 +103,22 @@ SR_HD float sr_sqrt(float x) {  /* IEEE correctly rounded on both sides */
 #endif
 }
 
-/* Rust `f as u8` (saturating cast): NaN -> 0, truncation toward zero. */
+/* Rust `f as u8` (saturating cast): NaN -> 0, truncation toward zero.  On
+ * the device the same function as a clamp and one truncating conversion:
+ * fmaxf returns its other operand for a quiet NaN (IEEE maxNum), so NaN and
+ * everything <= 0 clamp to 0 and everything >= 255 to 255, and the clamped
+ * value truncates as the cast does.  Equal for every input but a signalling
+ * NaN, which no arithmetic result is (every caller passes a product or a
+ * sum); checked over all 2^32 bit patterns by the tests. */
+SR_HD uint8_t sr_f32_to_u8_clamp(float x) { return (uint8_t)(uint32_t)fminf(fmaxf(x, 0.0f), 255.0f); }
 SR_HD uint8_t sr_f32_to_u8(float x) {
+#if defined(__CUDA_ARCH__)
+    return sr_f32_to_u8_clamp(x);
+#else
     if (!(x > 0.0f)) return 0;
     if (x >= 255.0f) return 255;
     return (uint8_t)(int)x;
+#endif
 }
 
 /* ---------------------------------------------------------------- vectors */
@@ -338,24 +349,48 @@ SR_HD uint32_t sr_to_rgba8(sr_v4 c) {
                          sr_f32_to_u8(c.z * 255.0f), sr_f32_to_u8(c.w * 255.0f));
 }
 /* c as f32 / 255.0 for a byte c: the correctly rounded quotient, computed as
- * q = c * (1/255) refined once with the exact residual c - 255 q (fused);
- * equal to the IEEE division for all 256 values (checked exhaustively by the
- * tests). */
+ * one fused c * r_hi + (c * r_lo) with r_hi + r_lo = 1/255 to 2^-57.  The sum
+ * is within 2^-24 ulp of c/255 and c/255 is at least 2^-9 ulp from every
+ * rounding midpoint (2 c 2^k - 255 (2 m + 1) is odd, so never 0), so the one
+ * rounding gives the quotient's; equal to the IEEE division for all 256
+ * values (checked exhaustively by the tests). */
 SR_HD float sr_u8_unit(uint32_t c) {
-    const float r = 1.0f / 255.0f;
-    float x = (float)c;
-    float q = x * r;
-    float e = sr_fma(-q, 255.0f, x);
-    return sr_fma(e, r, q);
+    const float r_hi = 0x1.010102p-8f;     /* 1/255 rounded */
+    const float r_lo = -0x1.fdfdfep-33f;   /* 1/255 - r_hi rounded */
+    const float x = (float)c;
+    return sr_fma(x, r_hi, x * r_lo);
 }
 /* RGBA8 -> f32 as in from_image_texel (full_example/src/texture.rs:38-45): c as f32 / 255.0 */
 SR_HD sr_v4 sr_from_rgba8(uint32_t p) {
     return sr_make_v4(sr_u8_unit(p & 0xffu), sr_u8_unit((p >> 8) & 0xffu),
                       sr_u8_unit((p >> 16) & 0xffu), sr_u8_unit(p >> 24));
 }
-/* Over operator on RGBA8: channels to f32 (c/255), over, back with `as u8`. */
+/* n / d correctly rounded given r = 1/d correctly rounded, for the operands
+ * of the RGBA8 over operator below: the quotient q0 = n r and one correction
+ * by the exact residual n - d q0 (Markstein's division step).  Equal to the
+ * IEEE quotient for every (colour, alpha) byte combination the operator can
+ * see, checked exhaustively by the tests; not a general division. */
+SR_HD float sr_over_div(float n, float d, float r) {
+    const float q0 = n * r;
+    const float e = sr_fma(-q0, d, n);
+    return sr_fma(e, r, q0);
+}
+/* Over operator on RGBA8: channels to f32 (c/255), over, back with `as u8`
+ * (sr_blend_over_f32 on the unit values).  The three colour quotients share
+ * one denominator, which is also the result's alpha; its reciprocal is taken
+ * once. */
 SR_HD uint32_t sr_blend_over_rgba8(uint32_t src, uint32_t dst) {
-    return sr_to_rgba8(sr_blend_over_f32(sr_from_rgba8(src), sr_from_rgba8(dst)));
+    const sr_v4 s = sr_from_rgba8(src), t = sr_from_rgba8(dst);
+    const float a = s.w, b = t.w;
+    const float a1 = 1.0f - a;
+    const float den = a + b * a1;
+    const float r = 1.0f / den;
+    sr_v4 c;
+    c.x = sr_over_div(s.x * a + (t.x * b) * a1, den, r);
+    c.y = sr_over_div(s.y * a + (t.y * b) * a1, den, r);
+    c.z = sr_over_div(s.z * a + (t.z * b) * a1, den, r);
+    c.w = den;
+    return sr_to_rgba8(c);
 }
 
 /* decode_gamma / encode_gamma (full_example/src/color.rs:41-57) */
@@ -625,7 +660,7 @@ SR_HD float sr_fast_pow_err(float y, float t) {
 }
 
 /* `as u8` of a value known to be non-NaN */
-SR_HD uint32_t sr_u8_of(float v) { return v >= 255.0f ? 255u : (v > 0.0f ? (uint32_t)v : 0u); }
+SR_HD uint32_t sr_u8_of(float v) { return (uint32_t)sr_f32_to_u8(v); }
 
 /*
  * The stored byte of one gamma-encoded channel, trunc(u^g * 255) with
