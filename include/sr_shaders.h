@@ -48,6 +48,34 @@ extern "C++" {
 
 struct sr_v4 { float x, y, z, w; };
 
+/* Paired single-precision operations of sm_100 and later (mul and fma on
+ * .f32x2): one instruction gives two IEEE round-to-nearest results, each
+ * equal to the scalar operation's.  The device uses them for two colour
+ * channels of the RGBA8 conversions and of the over operator's quotients;
+ * the host and every other target compute the same values one at a time. */
+#if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
+#define SR_PAIRED 1
+/* Written as PTX.  The code generator fuses a paired product with a paired
+ * sum that consumes it even when fused multiply-adds are disabled, so a
+ * paired product is used only where no addition consumes it (a clamp, a
+ * multiplicand, the addend of a fused multiply-add); sums of products stay
+ * scalar, two roundings as the reference computes them. */
+__device__ __forceinline__ float2 sr_mul2(float2 a, float2 b) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mul.rn.f32x2 pd, pa, pb;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 sr_fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pc, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
+        "mov.b64 pc, {%6, %7};\n\tfma.rn.f32x2 pd, pa, pb, pc;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y) : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+#endif
+
 SR_HD sr_v4 sr_make_v4(float x, float y, float z, float w) { sr_v4 r; r.x = x; r.y = y; r.z = z; r.w = w; return r; }
 
 SR_HD uint32_t sr_f2u(float f) {
@@ -345,8 +373,14 @@ SR_HD uint32_t sr_pack_rgba8(uint8_t r, uint8_t g, uint8_t b, uint8_t a) {
 }
 /* RGBA f32 in [0,1] -> RGBA8 via (c * 255.0) as u8 per channel. */
 SR_HD uint32_t sr_to_rgba8(sr_v4 c) {
+#if defined(SR_PAIRED)
+    const float2 k = make_float2(255.0f, 255.0f);
+    const float2 rg = sr_mul2(make_float2(c.x, c.y), k), ba = sr_mul2(make_float2(c.z, c.w), k);
+    return sr_pack_rgba8(sr_f32_to_u8(rg.x), sr_f32_to_u8(rg.y), sr_f32_to_u8(ba.x), sr_f32_to_u8(ba.y));
+#else
     return sr_pack_rgba8(sr_f32_to_u8(c.x * 255.0f), sr_f32_to_u8(c.y * 255.0f),
                          sr_f32_to_u8(c.z * 255.0f), sr_f32_to_u8(c.w * 255.0f));
+#endif
 }
 /* c as f32 / 255.0 for a byte c: the correctly rounded quotient, computed as
  * one fused c * r_hi + (c * r_lo) with r_hi + r_lo = 1/255 to 2^-57.  The sum
@@ -354,16 +388,24 @@ SR_HD uint32_t sr_to_rgba8(sr_v4 c) {
  * rounding midpoint (2 c 2^k - 255 (2 m + 1) is odd, so never 0), so the one
  * rounding gives the quotient's; equal to the IEEE division for all 256
  * values (checked exhaustively by the tests). */
+#define SR_R255_HI 0x1.010102p-8f     /* 1/255 rounded */
+#define SR_R255_LO (-0x1.fdfdfep-33f) /* 1/255 - SR_R255_HI rounded */
 SR_HD float sr_u8_unit(uint32_t c) {
-    const float r_hi = 0x1.010102p-8f;     /* 1/255 rounded */
-    const float r_lo = -0x1.fdfdfep-33f;   /* 1/255 - r_hi rounded */
     const float x = (float)c;
-    return sr_fma(x, r_hi, x * r_lo);
+    return sr_fma(x, SR_R255_HI, x * SR_R255_LO);
 }
 /* RGBA8 -> f32 as in from_image_texel (full_example/src/texture.rs:38-45): c as f32 / 255.0 */
 SR_HD sr_v4 sr_from_rgba8(uint32_t p) {
+#if defined(SR_PAIRED)
+    const float2 hi = make_float2(SR_R255_HI, SR_R255_HI), lo = make_float2(SR_R255_LO, SR_R255_LO);
+    const float2 rg = make_float2((float)(p & 0xffu), (float)((p >> 8) & 0xffu));
+    const float2 ba = make_float2((float)((p >> 16) & 0xffu), (float)(p >> 24));
+    const float2 urg = sr_fma2(rg, hi, sr_mul2(rg, lo)), uba = sr_fma2(ba, hi, sr_mul2(ba, lo));
+    return sr_make_v4(urg.x, urg.y, uba.x, uba.y);
+#else
     return sr_make_v4(sr_u8_unit(p & 0xffu), sr_u8_unit((p >> 8) & 0xffu),
                       sr_u8_unit((p >> 16) & 0xffu), sr_u8_unit(p >> 24));
+#endif
 }
 /* n / d correctly rounded given r = 1/d correctly rounded, for the operands
  * of the RGBA8 over operator below: the quotient q0 = n r and one correction
@@ -386,8 +428,19 @@ SR_HD uint32_t sr_blend_over_rgba8(uint32_t src, uint32_t dst) {
     const float den = a + b * a1;
     const float r = 1.0f / den;
     sr_v4 c;
+#if defined(SR_PAIRED)
+    /* red and green quotients as one pair (the numerators are scalar sums);
+     * fma(q0, -d, n) is fma(-q0, d, n) exactly */
+    const float2 n = make_float2(s.x * a + (t.x * b) * a1, s.y * a + (t.y * b) * a1);
+    const float2 R = make_float2(r, r), ND = make_float2(-den, -den);
+    const float2 q0 = sr_mul2(n, R);
+    const float2 q = sr_fma2(sr_fma2(q0, ND, n), R, q0);
+    c.x = q.x;
+    c.y = q.y;
+#else
     c.x = sr_over_div(s.x * a + (t.x * b) * a1, den, r);
     c.y = sr_over_div(s.y * a + (t.y * b) * a1, den, r);
+#endif
     c.z = sr_over_div(s.z * a + (t.z * b) * a1, den, r);
     c.w = den;
     return sr_to_rgba8(c);
