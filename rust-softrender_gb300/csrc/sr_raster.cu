@@ -236,8 +236,7 @@ __global__ void __launch_bounds__(ORD_THREADS, OrdOccupancy<FS>::BLOCKS) raster_
                     const uint32_t e = (uint32_t)w * 32 + (uint32_t)(__ffs(mw) - 1);
                     mw &= mw - 1;
                     float4 r2 = rec[e][2];
-                    uint32_t fl = __float_as_uint(r2.z);
-                    if (!(fl & REC_RASTER)) continue;
+                    uint32_t fl = __float_as_uint(r2.z);   // (only raster entries have mask bits)
                     int4 bb = rbb[e];
                     bool in_b = bb.x <= (int)px && (int)px <= bb.z && bb.y <= (int)py && (int)py <= bb.w;
                     bool ev;
