@@ -531,7 +531,7 @@ def served_wait(srv, ticket):
         raise RuntimeError("served request %d failed or timed out: status %d" % (ticket, st))
 
 
-def run_served(rate=2000.0, duration=10.0, sat_duration=1.0, sweep=SWEEP_RATES, served_inflight=8):
+def run_served(rate=2000.0, duration=10.0, sat_duration=1.0, sweep=SWEEP_RATES, served_inflight=2):
     """Poisson request stream against the serving loop and against the plain
     per-request loop (same server code, one request at a time through
     sr_render + sr_sync): p50/p99 latency and throughput at `rate`, the plain
@@ -701,7 +701,7 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-draws measurement")
     ap.add_argument("--no-frames", action="store_true", help="skip the small and stress frame measurements")
     ap.add_argument("--no-served", action="store_true", help="skip the serving-loop measurement")
-    ap.add_argument("--served-inflight", type=int, default=8, help="batches the serving loop keeps on the GPU")
+    ap.add_argument("--served-inflight", type=int, default=2, help="batches the serving loop keeps on the GPU")
     ap.add_argument("--profile-stress", action="store_true",
                     help="profiling aid: the ordered stress frame at 1024x1024 (--warmup untimed, --steps timed "
                          "frames), its timing only")
