@@ -18,14 +18,15 @@ Reported (one JSON line on rank 0):
          colour and depth planes back (wall clock per step)
   roofline  HBM roofline of the raster kernel (and of the whole frame)
   cpu_baseline  the CPU restatement of the reference path (oracle/), all
-         host threads, on a bounded sample extrapolated to the frame
+         host threads, timed on one whole frame
   other_frames  the small plain frame (icosphere, 1024^2) and the ordering /
          tiny-triangle stress frame (16.8M tiny + 4,096 alpha triangles)
   batched  256 draws of uneven sizes: one batch (one launch per stage, CUDA
          graph) against the plain per-draw pipeline
   served   a Poisson request stream (2,000 req/s) through the serving loop
          and through the plain per-request loop: p50/p99 latency, throughput,
-         saturated throughput of both
+         saturated throughput of both, and a sweep of offered rates against
+         the latency bound (2 x the plain single-request p99)
 
 --impl reference times the reference's CPU path (the oracle restatement; the
 Rust reference cannot be built here) on the same workload and metric.
