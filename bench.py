@@ -108,25 +108,34 @@ class ClockSampler:
         except Exception:
             self.proc.kill()
         self.out.close()
-        sm, mx, reasons = [], None, set()
-        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
         with open(self.out.name) as f:
-            for line in f:
-                c = [x.strip() for x in line.split(",")]
-                if len(c) < 9 or (self.uuid and self.uuid not in c[0]):
-                    continue
-                try:
-                    sm.append(float(c[1]))
-                    mx = float(c[2])
-                except ValueError:
-                    continue
-                for n, v in zip(names, c[5:9]):
-                    if v.lower().startswith("active"):
-                        reasons.add(n)
+            res = parse_clock_samples(f, self.uuid)
         os.unlink(self.out.name)
-        if not sm:
-            return None
-        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+        return res
+
+
+def parse_clock_samples(lines, uuid=""):
+    """Median SM clock, the maximum clock and the throttle reasons seen in
+    nvidia-smi samples of ClockSampler.FIELDS (csv, no header, no units),
+    keeping the lines of the GPU `uuid` (all when empty); None without
+    samples."""
+    sm, mx, reasons = [], None, set()
+    names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+    for line in lines:
+        c = [x.strip() for x in line.split(",")]
+        if len(c) < 9 or (uuid and uuid not in c[0]):
+            continue
+        try:
+            sm.append(float(c[1]))
+            mx = float(c[2])
+        except ValueError:
+            continue
+        for n, v in zip(names, c[5:9]):
+            if v.lower().startswith("active"):
+                reasons.add(n)
+    if not sm:
+        return None
+    return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
 def subsample_scene(scene, every):
