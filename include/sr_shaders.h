@@ -729,9 +729,19 @@ SR_HD uint32_t sr_encode_byte_fast(float u, float du, float g) {
     if (!(sr_fabs(t) <= 120.0f)) return 256u;
     const float G = sr_exp2_fast(t);
     /* |G - sr_powf(u_exact, g)| <= R G: the fast power's error and the
-     * input's, |(1 +- d)^g - 1| <= 1.25 |g| d, which holds because R <= 2^-8
-     * below keeps |g| d under 2^-8 */
-    const float R = sr_fast_pow_err(g, t) + 1.25f * sr_fabs(g) * (du / u);
+     * input's, |(1 +- d)^g - 1| <= 1.25 |g| d with d = du / u, which holds
+     * because R <= 2^-8 below keeps |g| d under 2^-8.  On the device d is
+     * bounded from above without a division: the hardware reciprocal of the
+     * normal u (PTX rcp.approx.f32, within 1 ulp, 2^-23, of 1/u) and two
+     * roundings (2^-24 each) stay under the 2^-20 added. */
+#if defined(__CUDA_ARCH__)
+    float ru;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(ru) : "f"(u));
+    const float d = (du * ru) * (1.0f + 0x1p-20f);
+#else
+    const float d = du / u;
+#endif
+    const float R = sr_fast_pow_err(g, t) + 1.25f * sr_fabs(g) * d;
     if (!(R <= 0x1p-8f)) return 256u;
     const float v = G * 255.0f;
     /* both sides round G * 255 (2^-24 each); 2 ulp(v) more keep the rounded
