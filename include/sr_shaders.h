@@ -55,11 +55,12 @@ struct sr_v4 { float x, y, z, w; };
  * the host and every other target compute the same values one at a time. */
 #if defined(__CUDA_ARCH__) && (__CUDA_ARCH__ >= 1000)
 #define SR_PAIRED 1
-/* Written as PTX.  The code generator fuses a paired product with a paired
- * sum that consumes it even when fused multiply-adds are disabled, so a
- * paired product is used only where no addition consumes it (a clamp, a
- * multiplicand, the addend of a fused multiply-add); sums of products stay
- * scalar, two roundings as the reference computes them. */
+/* Written as PTX.  The code generator was seen to fuse a paired product
+ * with a paired sum consuming it although fused multiply-adds are disabled
+ * (the GPU parity tests caught 1-ulp differences), so a paired product is
+ * used only where no addition consumes it (a clamp, a multiplicand, the
+ * addend of a fused multiply-add); sums of products stay scalar, two
+ * roundings as the reference computes them. */
 __device__ __forceinline__ float2 sr_mul2(float2 a, float2 b) {
     float2 d;
     asm("{\n\t.reg .b64 pa, pb, pd;\n\tmov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\t"
